@@ -1,0 +1,150 @@
+/*
+ * gbsdf.h — C ABI of the GB300 mesh-to-SDF engine.
+ *
+ * Drop-in boundary for the reference's "Fast SDF" path (golemid/rhizome_v24.15):
+ *
+ *   static bool CudaRasterizer::compute_mesh_sdf(
+ *       const std::vector<CudaTriangle>& triangles, float voxel_size,
+ *       glm::ivec3 min_coord, glm::ivec3 max_coord,
+ *       std::vector<float>& out_distances, float& out_time_ms);
+ *     declared native/src/engine/sdf/cuda_rasterizer.hpp:21-28,
+ *     defined  native/src/engine/sdf/cuda_rasterizer.cu:1163-1265
+ *     (fast path rhi_compute_mesh_sdf_fast, cuda_rasterizer.cu:796-1159)
+ *
+ *   static std::shared_ptr<CudaVolumeGrid> CudaRasterizer::build_from_mesh(
+ *       const TriangleMesh& mesh, float voxel_size, float& out_time_ms);
+ *     declared native/src/engine/sdf/cuda_rasterizer.hpp:31-35,
+ *     defined  native/src/engine/sdf/cuda_rasterizer.cu:1340-1435
+ *
+ * Plain pointers and sizes only. Grid contract (cuda_rasterizer.cu:117-118):
+ * dims = max - min + 1 (inclusive lattice), value at (x, y, z) is for the world
+ * point ((min.x+x) h, (min.y+y) h, (min.z+z) h), dense, x fastest; negative
+ * inside, inside <=> |generalized winding number| >= 0.5.
+ *
+ * Errors: every entry point returns a gbsdf_status; 0 is success. On any
+ * non-zero status the output buffer is left untouched (the reference's
+ * "output untouched on failure" contract, cuda_rasterizer.cu:788-791), and a
+ * one-line reason is written to err (if err != NULL and errlen > 0).
+ * There is no CPU fallback: without a usable CUDA device the call fails.
+ */
+#ifndef GBSDF_H
+#define GBSDF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Triangle record, layout of the reference's CudaTriangle
+ * (native/src/engine/sdf/cuda_types.hpp:18-21): v0, v1, v2, unit normal; 48 bytes.
+ * The normal is carried but not used by the SDF. */
+typedef struct gbsdf_tri {
+    float v0[3];
+    float v1[3];
+    float v2[3];
+    float n[3];
+} gbsdf_tri;
+
+typedef enum gbsdf_status {
+    GBSDF_OK = 0,
+    GBSDF_EINVAL = 1,   /* bad arguments, empty mesh, non-finite or out-of-range coordinates */
+    GBSDF_EGUARD = 2,   /* reference int-range guard declines the fast path (cuda_rasterizer.cu:816-820) */
+    GBSDF_ECSR = 3,     /* reference supercell-CSR guard declines (cuda_rasterizer.cu:867-869) */
+    GBSDF_EVERIFY = 4,  /* sign verification found systematic divergence (cuda_rasterizer.cu:1124-1132):
+                           the caller falls back to the legacy exact path */
+    GBSDF_ENOMEM = 5,   /* device or pinned host allocation failed (cuda_rasterizer.cu:913-917) */
+    GBSDF_ECUDA = 6,    /* CUDA runtime error */
+    GBSDF_ENODEV = 7    /* no usable CUDA device */
+} gbsdf_status;
+
+typedef enum gbsdf_mode {
+    /* The reference's algorithm: its Godunov update, its round loop (<= 8 rounds of
+     * 6 sweeps, audit-gated extra rounds, clamp), parity signs, 3 x 4096 stratified
+     * probes and r = 24 patch boxes, its decline conditions. Sweeps are lockstep
+     * (deterministic); winding signs are decided exactly. */
+    GBSDF_MODE_REFERENCE = 0,
+    /* Corrected, monotone Godunov update run to its (unique) fixed point; no
+     * int-range / CSR guards. */
+    GBSDF_MODE_EXACT = 1
+} gbsdf_mode;
+
+typedef enum gbsdf_path {
+    GBSDF_PATH_AUTO = 0,   /* reference dispatch: legacy exact kernel below 32M voxels,
+                              fast path at or above (cuda_rasterizer.cu:1189) */
+    GBSDF_PATH_FAST = 1,   /* always the fast path */
+    GBSDF_PATH_LEGACY = 2  /* always the legacy exact kernel (cuda_rasterizer.cu:97-185) */
+} gbsdf_path;
+
+typedef struct gbsdf_options {
+    int32_t mode;          /* gbsdf_mode */
+    int32_t path;          /* gbsdf_path */
+    int32_t device;        /* CUDA device ordinal */
+    int32_t tris_on_device;/* 1: `tris` is a device pointer */
+    int32_t max_rounds;    /* exact mode: safety cap on sweep rounds (0 = default 4096) */
+    int32_t reserved[7];
+} gbsdf_options;
+
+typedef struct gbsdf_stats {
+    int32_t status;
+    int32_t path_taken;    /* gbsdf_path actually run (FAST or LEGACY) */
+    float ms_total;        /* wall time of the call */
+    float ms_h2d, ms_prep, ms_splat, ms_parity, ms_fixup, ms_eikonal, ms_verify, ms_apply, ms_d2h;
+    int32_t eikonal_rounds;
+    int32_t extra_rounds;
+    int32_t probes;
+    int32_t sites;
+    int32_t patch_rounds;
+    int32_t pad0;
+    int64_t unknown_columns;
+    int64_t fixup_voxels;
+    int64_t far_residual;
+    int64_t safe_clamped;
+    int64_t patched_voxels;
+    int64_t fp64_rechecks;
+    int64_t band_voxels;
+    int64_t splat_evals;   /* exact point-triangle distance evaluations */
+    int64_t gwn_pairs;     /* point-triangle solid-angle evaluations */
+    int64_t brick_pairs;   /* (triangle, brick) pairs binned for the splat */
+    int64_t csr_entries;   /* entries of the reference's supercell CSR */
+    int64_t kernel_launches; /* CUDA kernels this call launched */
+    int64_t reserved[7];
+} gbsdf_stats;
+
+/* Fill `opt` with defaults: reference mode, AUTO path, device 0, host triangles. */
+void gbsdf_default_options(gbsdf_options* opt);
+
+/* Replaces CudaRasterizer::compute_mesh_sdf (cuda_rasterizer.hpp:21-28,
+ * cuda_rasterizer.cu:1163-1265). `out` holds dims.x*dims.y*dims.z floats, on the
+ * device when out_on_device != 0, else in host memory (pinned or pageable). */
+int gbsdf_compute_mesh_sdf(const gbsdf_tri* tris, int64_t n_tris, float voxel_size, const int32_t min_coord[3],
+                           const int32_t max_coord[3], float* out, int32_t out_on_device,
+                           const gbsdf_options* opt, gbsdf_stats* stats, char* err, size_t errlen);
+
+/* Lattice of CudaRasterizer::build_from_mesh (cuda_rasterizer.cu:1354-1372): bounding box
+ * of all vertices, padded by 10 voxels, floor/ceil onto the voxel lattice. */
+int gbsdf_mesh_lattice(const float* verts, int64_t n_verts, float voxel_size, int32_t min_coord[3],
+                       int32_t max_coord[3], char* err, size_t errlen);
+
+/* Replaces CudaRasterizer::build_from_mesh (cuda_rasterizer.cu:1340-1435): builds the
+ * triangles on the device (degenerate |cross|^2 <= 1e-12 and out-of-range faces dropped,
+ * kept in index order, math_utils.cuh:484-514) and computes the SDF on the lattice given
+ * by gbsdf_mesh_lattice. `indices` has n_indices entries (3 per face). */
+int gbsdf_build_from_mesh(const float* verts, int64_t n_verts, const uint32_t* indices, int64_t n_indices,
+                          float voxel_size, const int32_t min_coord[3], const int32_t max_coord[3], float* out,
+                          int32_t out_on_device, const gbsdf_options* opt, gbsdf_stats* stats, char* err,
+                          size_t errlen);
+
+/* Releases the cached device workspace of `device` (buffers are otherwise reused
+ * across calls on the same device). */
+void gbsdf_release_workspace(int32_t device);
+
+/* Library version string. */
+const char* gbsdf_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBSDF_H */

@@ -1,0 +1,250 @@
+"""ctypes binding of the CPU oracle (oracle/sdf_oracle.cpp) -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline / reference arm
+import this module. It checks the product; it is never the product.
+
+Every function cites the reference code it restates (paths relative to the
+reference project): the fast SDF path in native/src/engine/sdf/cuda_rasterizer.cu
+(RAST) and the primitives in native/src/core/math_utils.cuh (MATH).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "liboracle.so"
+SRC = HERE / "sdf_oracle.cpp"
+REF_LIB_PATH = HERE / "_ref" / "libref_math.so"
+
+# fast-path status codes (orc_fast_stats.status)
+OK, INVALID, INT_GUARD, CSR_GUARD, VERIFY_DIVERGED = 0, 1, 2, 3, 4
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle with g++ (no FP contraction, so x86 and Arm agree)."""
+    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < SRC.stat().st_mtime:
+        cmd = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
+               str(SRC), "-o", str(LIB_PATH)]
+        subprocess.check_call(cmd)
+    return LIB_PATH
+
+
+def build_ref() -> Path | None:
+    """Compile the reference's own primitives into oracle/_ref (only where the
+    reference tree exists)."""
+    subprocess.check_call(["bash", str(HERE / "build_ref.sh")])
+    return REF_LIB_PATH if REF_LIB_PATH.exists() else None
+
+
+class FastParams(C.Structure):
+    _fields_ = [("fsm_mode", C.c_int), ("gwn_mode", C.c_int), ("threads", C.c_int),
+                ("max_conv_rounds", C.c_int), ("skip_verify", C.c_int)]
+
+
+class FastStats(C.Structure):
+    _fields_ = [("status", C.c_int), ("unknown_columns", C.c_int), ("fixup_voxels", C.c_longlong),
+                ("eikonal_rounds", C.c_int), ("extra_rounds", C.c_int), ("far_residual", C.c_longlong),
+                ("safe_clamped", C.c_longlong), ("probes", C.c_int), ("sites", C.c_int),
+                ("patch_rounds", C.c_int), ("patched_voxels", C.c_longlong), ("fp64_rechecks", C.c_longlong),
+                ("band_voxels", C.c_longlong),
+                ("ms_splat", C.c_double), ("ms_parity", C.c_double), ("ms_fixup", C.c_double),
+                ("ms_eikonal", C.c_double), ("ms_verify", C.c_double), ("ms_apply", C.c_double),
+                ("ms_total", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB_PATH))
+        P = C.c_void_p
+        L.orc_point_triangle_distance_sq.restype = C.c_float
+        L.orc_triangle_solid_angle.restype = C.c_float
+        L.orc_triangle_solid_angle_f64.restype = C.c_double
+        L.orc_godunov.restype = C.c_float
+        L.orc_godunov.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float]
+        L.orc_splat_band.restype = C.c_longlong
+        L.orc_parity_signs.restype = C.c_longlong
+        L.orc_fixup_unknown.restype = C.c_longlong
+        L.orc_fsm_sweep.restype = C.c_int
+        L.orc_eikonal.restype = C.c_int
+        L.orc_verify_patch.restype = C.c_int
+        L.orc_fast_sdf.restype = C.c_int
+        L.orc_lattice.restype = C.c_int
+        L.orc_build_triangles.restype = C.c_longlong
+        L.orc_fast_min_voxels.restype = C.c_longlong
+        for name in ("orc_splat_band", "orc_parity_signs", "orc_fixup_unknown", "orc_fast_sdf",
+                     "orc_legacy_sdf", "orc_gwn_points_f64", "orc_gwn_sign_voxels", "orc_ptd_batch",
+                     "orc_solid_angle_batch", "orc_lattice", "orc_build_triangles", "orc_fsm_sweep",
+                     "orc_eikonal", "orc_apply_signs", "orc_verify_patch"):
+            getattr(L, name).restype = getattr(L, name).restype
+        _ = P
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _ivec(v):
+    return np.ascontiguousarray(np.asarray(v, np.int32).reshape(3))
+
+
+def _tris(t):
+    t = np.ascontiguousarray(np.asarray(t, np.float32).reshape(-1, 12))
+    return t, len(t)
+
+
+def default_threads() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+# ---- primitives (MATH:43-132) -------------------------------------------------------
+def ptd_batch(pts, tris9):
+    pts = np.ascontiguousarray(pts, np.float32)
+    tris9 = np.ascontiguousarray(tris9, np.float32)
+    out = np.empty(len(pts), np.float32)
+    lib().orc_ptd_batch(_p(pts), _p(tris9), C.c_longlong(len(pts)), _p(out))
+    return out
+
+
+def solid_angle_batch(pts, tris9):
+    pts = np.ascontiguousarray(pts, np.float32)
+    tris9 = np.ascontiguousarray(tris9, np.float32)
+    out = np.empty(len(pts), np.float32)
+    lib().orc_solid_angle_batch(_p(pts), _p(tris9), C.c_longlong(len(pts)), _p(out))
+    return out
+
+
+def godunov(ax, ay, az, h):
+    """rhi_eikonal_godunov, RAST:405-425."""
+    return lib().orc_godunov(float(ax), float(ay), float(az), float(h))
+
+
+def gwn_points_f64(tris, pts, threads=None):
+    t, T = _tris(tris)
+    pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+    out = np.empty(len(pts), np.float64)
+    lib().orc_gwn_points_f64(_p(t), C.c_int(T), _p(pts), C.c_longlong(len(pts)), _p(out),
+                             C.c_int(threads or default_threads()))
+    return out
+
+
+def gwn_sign_voxels(tris, h, mn, dims, vidx, mode=1, threads=None):
+    t, T = _tris(tris)
+    vidx = np.ascontiguousarray(vidx, np.int64)
+    out = np.empty(len(vidx), np.uint8)
+    lib().orc_gwn_sign_voxels(_p(t), C.c_int(T), C.c_float(h), _p(_ivec(mn)), _p(_ivec(dims)), _p(vidx),
+                              C.c_longlong(len(vidx)), C.c_int(mode), _p(out), C.c_int(threads or default_threads()))
+    return out
+
+
+# ---- stages ----------------------------------------------------------------------------
+def splat_band(tris, h, mn, dims, threads=None):
+    """[init]+[A]: sentinel fill and exact band splat (RAST:194-268). Returns (dist, band_count)."""
+    t, T = _tris(tris)
+    dims = _ivec(dims)
+    dist = np.empty(int(np.prod(dims.astype(np.int64))), np.float32)
+    n = lib().orc_splat_band(_p(t), C.c_int(T), C.c_float(h), _p(_ivec(mn)), _p(dims), _p(dist),
+                             C.c_int(threads or default_threads()))
+    return dist, n
+
+
+def parity_signs(tris, h, mn, dims, threads=None):
+    """[B]: scanline parity (RAST:279-368, CSR RAST:824-882). Returns (sign u8, unknown_columns)."""
+    t, T = _tris(tris)
+    dims = _ivec(dims)
+    sign = np.empty(int(np.prod(dims.astype(np.int64))), np.uint8)
+    n = lib().orc_parity_signs(_p(t), C.c_int(T), C.c_float(h), _p(_ivec(mn)), _p(dims), _p(sign),
+                               C.c_int(threads or default_threads()))
+    return sign, n
+
+
+def fixup_unknown(tris, h, mn, dims, sign, gwn_mode=1, threads=None):
+    """[C]: exact winding for sign==2 voxels (RAST:374-400). In place; returns count."""
+    t, T = _tris(tris)
+    rech = C.c_longlong(0)
+    n = lib().orc_fixup_unknown(_p(t), C.c_int(T), C.c_float(h), _p(_ivec(mn)), _p(_ivec(dims)), _p(sign),
+                                C.c_int(gwn_mode), C.c_int(threads or default_threads()), C.byref(rech))
+    return n
+
+
+def fsm_sweep(g, dims, h, axis, direction, threads=None):
+    """[D]: one directional sweep (RAST:433-513), in place. Returns changed flag."""
+    return lib().orc_fsm_sweep(_p(g), _p(_ivec(dims)), C.c_float(h), C.c_int(axis), C.c_int(direction),
+                               C.c_int(threads or default_threads()))
+
+
+def eikonal(g, sign, dims, h, fsm_mode=1, max_conv_rounds=100000, threads=None):
+    """[D]/[D2]/[D3]: FSM rounds, audit, clamp (RAST:987-1064), in place."""
+    extra = C.c_int(0)
+    resid = C.c_longlong(0)
+    clamped = C.c_longlong(0)
+    r = lib().orc_eikonal(_p(g), _p(sign), _p(_ivec(dims)), C.c_float(h), C.c_int(fsm_mode),
+                          C.c_int(max_conv_rounds), C.c_int(threads or default_threads()), C.byref(extra),
+                          C.byref(resid), C.byref(clamped))
+    return dict(rounds=r, extra_rounds=extra.value, far_residual=resid.value, safe_clamped=clamped.value)
+
+
+def fast_sdf(tris, h, mn, mx, fsm_mode=1, gwn_mode=1, threads=None, skip_verify=False, max_conv_rounds=100000):
+    """The whole fast path (RAST:796-1159). Returns (status, dist or None, sign, stats dict)."""
+    t, T = _tris(tris)
+    mn, mx = _ivec(mn), _ivec(mx)
+    dims = mx.astype(np.int64) - mn + 1
+    N = int(np.prod(dims)) if (dims > 0).all() else 0
+    dist = np.empty(max(N, 1), np.float32)
+    sign = np.empty(max(N, 1), np.uint8)
+    prm = FastParams(fsm_mode, gwn_mode, threads or default_threads(), max_conv_rounds, 1 if skip_verify else 0)
+    st = FastStats()
+    s = lib().orc_fast_sdf(_p(t), C.c_int(T), C.c_float(h), _p(mn), _p(mx), C.byref(prm), _p(dist), _p(sign),
+                           C.byref(st))
+    return s, (dist[:N] if s == OK else None), sign[:N], st.as_dict()
+
+
+def legacy_sdf(tris, h, mn, mx, gwn_mode=1, threads=None):
+    """Legacy exact kernel mesh_to_sdf_kernel (RAST:97-185)."""
+    t, T = _tris(tris)
+    mn, mx = _ivec(mn), _ivec(mx)
+    N = int(np.prod(mx.astype(np.int64) - mn + 1))
+    out = np.empty(N, np.float32)
+    lib().orc_legacy_sdf(_p(t), C.c_int(T), C.c_float(h), _p(mn), _p(mx), C.c_int(gwn_mode), _p(out),
+                         C.c_int(threads or default_threads()))
+    return out
+
+
+def lattice(verts, h):
+    """build_from_mesh lattice (RAST:1354-1372)."""
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+    mn = np.zeros(3, np.int32)
+    mx = np.zeros(3, np.int32)
+    lib().orc_lattice(_p(v), C.c_longlong(len(v)), C.c_float(h), _p(mn), _p(mx))
+    return mn, mx
+
+
+def build_triangles(verts, faces):
+    """Deterministic gpu_build_cuda_triangles_kernel (RAST:1321-1337, MATH:484-514)."""
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+    f = np.ascontiguousarray(faces, np.uint32).reshape(-1, 3)
+    out = np.empty((len(f), 12), np.float32)
+    k = lib().orc_build_triangles(_p(v), C.c_longlong(len(v)), _p(f), C.c_longlong(len(f)), _p(out))
+    return out[:k]
+
+
+# ---- the reference's own primitives (oracle/_ref), where available ------------------
+def ref_lib():
+    if not REF_LIB_PATH.exists():
+        return None
+    L = C.CDLL(str(REF_LIB_PATH))
+    return L

@@ -1,0 +1,616 @@
+// engine.cu — host orchestration and C ABI of the GB300 mesh-to-SDF engine.
+//
+// One call runs the whole path on one GPU, on one CUDA stream of a per-device
+// workspace whose buffers persist across calls (the reference allocates and frees
+// every buffer per call, cuda_rasterizer.cu:884-918 and :1141):
+//
+//   H2D triangles -> [prep] per-triangle records, brick / strip counts
+//   -> [bin] counting-sort lists  -> [init] sentinel fill -> [A] brick splat
+//   -> [B] parity ballots -> [C] exact winding of unknown columns
+//   -> [D] eikonal sweeps (+ audit / clamp) -> [E] stratified verify + patch boxes
+//   -> [F] sign apply -> D2H (host output) .
+//
+// Host synchronisation points: one after binning (list sizes, guards), one after
+// the parity pass (unknown-voxel count), one at the end (status); the eikonal round
+// loop and the verify / patch loop are driven by device-side state.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/gbsdf.h"
+#include "gbsdf_device.cuh"
+#include "gbsdf_internal.h"
+
+namespace gbsdf {
+
+unsigned long long& launch_counter() {
+    static thread_local unsigned long long n = 0;
+    return n;
+}
+
+namespace {
+
+struct Buf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct Workspace {
+    int device = -1;
+    int num_sms = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[12] = {};
+    std::mutex mu;
+    Buf A, B, S, U, t12, t9, stt, ptt, bcount, bcur, boff, active, blist, scount, scur, soff, slist, scan, list,
+        recheck, hb, verts, idx, flags, fpos;
+    DevState* ds = nullptr;
+    DevState* hs = nullptr;  // pinned host mirror
+};
+
+Workspace g_ws[64];
+std::mutex g_ws_mu;
+
+struct Err {
+    char* buf;
+    size_t len;
+    int set(int status, const char* fmt, ...) {
+        if (buf && len > 0) {
+            va_list ap;
+            va_start(ap, fmt);
+            vsnprintf(buf, len, fmt, ap);
+            va_end(ap);
+        }
+        return status;
+    }
+};
+
+#define GB_CK(call)                                                                                     \
+    do {                                                                                                \
+        cudaError_t _e = (call);                                                                        \
+        if (_e != cudaSuccess) {                                                                        \
+            return e.set(_e == cudaErrorMemoryAllocation ? GBSDF_ENOMEM : GBSDF_ECUDA, "%s: %s (%s:%d)", \
+                         #call, cudaGetErrorString(_e), __FILE__, __LINE__);                            \
+        }                                                                                               \
+    } while (0)
+
+cudaError_t ensure(Buf& b, size_t bytes) {
+    if (bytes <= b.bytes && b.p) return cudaSuccess;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    size_t want = bytes + bytes / 8 + 256;
+    cudaError_t err = cudaMalloc(&b.p, want);
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        return err;
+    }
+    b.bytes = want;
+    return cudaSuccess;
+}
+
+template <class T>
+T* P(Buf& b) {
+    return static_cast<T*>(b.p);
+}
+
+int init_ws(Workspace& w, int device, Err& e) {
+    if (w.device == device) return GBSDF_OK;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return e.set(GBSDF_ENODEV, "no CUDA device available");
+    }
+    if (device < 0 || device >= n) return e.set(GBSDF_ENODEV, "device %d out of range (%d devices)", device, n);
+    GB_CK(cudaSetDevice(device));
+    GB_CK(cudaDeviceGetAttribute(&w.num_sms, cudaDevAttrMultiProcessorCount, device));
+    GB_CK(cudaStreamCreateWithFlags(&w.st, cudaStreamNonBlocking));
+    for (auto& ev : w.ev) GB_CK(cudaEventCreate(&ev));
+    GB_CK(cudaMalloc(&w.ds, sizeof(DevState)));
+    GB_CK(cudaMallocHost(&w.hs, sizeof(DevState)));
+    w.device = device;
+    return GBSDF_OK;
+}
+
+void free_ws(Workspace& w) {
+    if (w.device < 0) return;
+    cudaSetDevice(w.device);
+    Buf* bufs[] = {&w.A, &w.B, &w.S, &w.U, &w.t12, &w.t9, &w.stt, &w.ptt, &w.bcount, &w.bcur, &w.boff,
+                   &w.active, &w.blist, &w.scount, &w.scur, &w.soff, &w.slist, &w.scan, &w.list, &w.recheck,
+                   &w.hb, &w.verts, &w.idx, &w.flags, &w.fpos};
+    for (Buf* b : bufs) {
+        if (b->p) cudaFree(b->p);
+        *b = Buf{};
+    }
+    if (w.ds) cudaFree(w.ds);
+    if (w.hs) cudaFreeHost(w.hs);
+    for (auto& ev : w.ev)
+        if (ev) cudaEventDestroy(ev);
+    if (w.st) cudaStreamDestroy(w.st);
+    w.ds = nullptr;
+    w.hs = nullptr;
+    w.st = nullptr;
+    for (auto& ev : w.ev) ev = nullptr;
+    w.device = -1;
+}
+
+Lattice make_lattice(const int32_t mn[3], const int32_t mx[3], float h) {
+    Lattice L{};
+    for (int k = 0; k < 3; ++k) {
+        L.mn[k] = mn[k];
+        L.dims[k] = mx[k] - mn[k] + 1;
+    }
+    L.h = h;
+    L.N = (long long)L.dims[0] * L.dims[1] * L.dims[2];
+    L.wx = (L.dims[0] + 31) / 32;
+    L.nwords = (long long)L.wx * L.dims[1] * L.dims[2];
+    for (int k = 0; k < 3; ++k) L.nb[k] = (L.dims[k] + kBrick - 1) / kBrick;
+    L.nbricks = (long long)L.nb[0] * L.nb[1] * L.nb[2];
+    L.nsx = (L.dims[0] + kStrip - 1) / kStrip;
+    L.nstrips = (long long)L.nsx * L.dims[1];
+    return L;
+}
+
+float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+        cudaGetLastError();
+        return 0.0f;
+    }
+    return ms;
+}
+
+constexpr long long kListCap = 8ll * 1024 * 1024;  // >= 64 patch boxes of 49^3 voxels
+
+// Exact winding of every voxel flagged in U (initial unknown columns): compaction
+// into the dense list, FP32 pass, FP64 re-checks; repeats while the list overflowed.
+int fixup_unknown(Workspace& w, const Lattice& L, long long T, Err& e) {
+    cudaStream_t st = w.st;
+    for (int pass = 0; pass < 1 << 20; ++pass) {
+        GB_CK(cudaMemsetAsync(&w.ds->listed, 0, sizeof(unsigned long long), st));
+        GB_CK(cudaMemsetAsync(&w.ds->list_overflow, 0, sizeof(unsigned long long), st));
+        GB_CK(cudaMemsetAsync(&w.ds->recheck_n, 0, sizeof(unsigned long long), st));
+        launch_list_unknown(P<uint32_t>(w.U), P<uint32_t>(w.S), L, P<long long>(w.list), kListCap, w.ds, 0, st);
+        GB_CK(cudaMemcpyAsync(w.hs, w.ds, sizeof(DevState), cudaMemcpyDeviceToHost, st));
+        GB_CK(cudaStreamSynchronize(st));
+        long long n = std::min<long long>((long long)w.hs->listed, kListCap);
+        if (n <= 0) return GBSDF_OK;
+        if (n < 64 * 1024)
+            launch_gwn_small(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, P<uint32_t>(w.S),
+                             P<long long>(w.recheck), kListCap, w.ds, n, st);
+        else
+            launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 0, P<uint32_t>(w.S),
+                       P<long long>(w.recheck), kListCap, w.ds, w.num_sms, st);
+        launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
+                           w.ds, w.num_sms, st);
+        GB_CK(cudaGetLastError());
+        if (w.hs->list_overflow == 0) return GBSDF_OK;
+    }
+    return e.set(GBSDF_ECUDA, "unknown-voxel fixup did not drain");
+}
+
+int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o, float* out, bool out_dev,
+             gbsdf_stats* stats, Err& e) {
+    cudaStream_t st = w.st;
+    const bool ref_mode = (o.mode == GBSDF_MODE_REFERENCE);
+    const long long N = L.N;
+    // ---- buffers
+    GB_CK(ensure(w.A, (size_t)N * 4));
+    GB_CK(ensure(w.B, (size_t)N * 4));
+    GB_CK(ensure(w.S, (size_t)L.nwords * 4));
+    GB_CK(ensure(w.U, (size_t)L.nwords * 4));
+    GB_CK(ensure(w.t9, (size_t)T * 36));
+    GB_CK(ensure(w.stt, (size_t)T * sizeof(SplatTri)));
+    GB_CK(ensure(w.ptt, (size_t)T * sizeof(ParTri)));
+    GB_CK(ensure(w.bcount, (size_t)L.nbricks * 4));
+    GB_CK(ensure(w.bcur, (size_t)L.nbricks * 4));
+    GB_CK(ensure(w.boff, (size_t)L.nbricks * 8));
+    GB_CK(ensure(w.active, (size_t)L.nbricks * 4));
+    GB_CK(ensure(w.scount, (size_t)L.nstrips * 4));
+    GB_CK(ensure(w.scur, (size_t)L.nstrips * 4));
+    GB_CK(ensure(w.soff, (size_t)L.nstrips * 8));
+    GB_CK(ensure(w.scan, (size_t)std::max(scan_tmp_elems(L.nbricks), scan_tmp_elems(L.nstrips)) * 8));
+    GB_CK(ensure(w.list, (size_t)kListCap * 8));
+    GB_CK(ensure(w.recheck, (size_t)kListCap * 8));
+
+    // ---- [prep] + counts
+    GB_CK(cudaMemsetAsync(w.ds, 0, sizeof(DevState), st));
+    GB_CK(cudaMemsetAsync(w.bcount.p, 0, (size_t)L.nbricks * 4, st));
+    GB_CK(cudaMemsetAsync(w.scount.p, 0, (size_t)L.nstrips * 4, st));
+    launch_prep(P<float>(w.t12), T, L, P<SplatTri>(w.stt), P<ParTri>(w.ptt), P<unsigned>(w.bcount),
+                P<unsigned>(w.scount), w.ds, st);
+    launch_exclusive_scan(P<unsigned>(w.bcount), P<unsigned long long>(w.boff), L.nbricks,
+                          P<unsigned long long>(w.scan), 0, st);
+    launch_exclusive_scan(P<unsigned>(w.scount), P<unsigned long long>(w.soff), L.nstrips,
+                          P<unsigned long long>(w.scan), 0, st);
+    launch_active_bricks(P<unsigned>(w.bcount), L.nbricks, P<unsigned>(w.active), w.ds, st);
+    launch_pack_tri9(P<float>(w.t12), T, P<float>(w.t9), st);
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaMemcpyAsync(w.hs, w.ds, sizeof(DevState), cudaMemcpyDeviceToHost, st));
+    GB_CK(cudaStreamSynchronize(st));
+    if (w.hs->invalid_tris > 0)
+        return e.set(GBSDF_EINVAL, "%llu triangles have non-finite or out-of-range coordinates",
+                     (unsigned long long)w.hs->invalid_tris);
+    if (ref_mode && (w.hs->csr_entries == 0 || w.hs->csr_entries > 100000000ull))
+        return e.set(GBSDF_ECSR, "supercell CSR has %llu entries (reference guard: 1..1e8)",
+                     (unsigned long long)w.hs->csr_entries);
+    const long long brick_pairs = (long long)w.hs->brick_pairs;
+    const long long strip_pairs = (long long)w.hs->strip_pairs;
+    const long long n_active = (long long)w.hs->active_bricks;
+    GB_CK(ensure(w.blist, (size_t)std::max<long long>(brick_pairs, 1) * 4));
+    GB_CK(ensure(w.slist, (size_t)std::max<long long>(strip_pairs, 1) * 4));
+    GB_CK(cudaMemsetAsync(w.bcur.p, 0, (size_t)L.nbricks * 4, st));
+    GB_CK(cudaMemsetAsync(w.scur.p, 0, (size_t)L.nstrips * 4, st));
+    launch_bin_fill(P<SplatTri>(w.stt), P<ParTri>(w.ptt), T, L, P<unsigned long long>(w.boff), P<unsigned>(w.bcur),
+                    P<unsigned>(w.blist), P<unsigned long long>(w.soff), P<unsigned>(w.scur), P<unsigned>(w.slist),
+                    st);
+    GB_CK(cudaEventRecord(w.ev[2], st));
+    // ---- [init] + [A]
+    launch_fill(P<float>(w.A), N, kFarSentinel, st);
+    launch_splat(P<SplatTri>(w.stt), P<unsigned long long>(w.boff), P<unsigned>(w.bcount), P<unsigned>(w.blist),
+                 P<unsigned>(w.active), n_active, L, P<float>(w.A), w.ds, st);
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaEventRecord(w.ev[3], st));
+    // ---- [B]
+    launch_parity(P<ParTri>(w.ptt), P<unsigned long long>(w.soff), P<unsigned>(w.scount), P<unsigned>(w.slist), L,
+                  P<uint32_t>(w.S), P<uint32_t>(w.U), w.ds, st);
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaEventRecord(w.ev[4], st));
+    // ---- [C]
+    int rc = fixup_unknown(w, L, T, e);
+    if (rc != GBSDF_OK) return rc;
+    GB_CK(cudaEventRecord(w.ev[5], st));
+    // ---- [D]
+    const int rule = ref_mode ? 0 : 1;
+    float* src = P<float>(w.A);
+    float* dst = P<float>(w.B);
+    if (ref_mode) {
+        for (int r = 0; r < kMaxRounds; ++r) {
+            for (int axis = 0; axis < 3; ++axis)
+                for (int dir = 1; dir >= -1; dir -= 2) {
+                    launch_sweep(rule, axis, dir, r, src, dst, L, w.ds, st);
+                    std::swap(src, dst);
+                }
+            launch_end_round(r, r, kMaxRounds, w.ds, st);
+        }
+    } else {
+        const int cap = o.max_rounds > 0 ? o.max_rounds : 4096;
+        const int batch = 4;
+        for (int r0 = 0; r0 < cap; r0 += batch) {
+            for (int r = r0; r < std::min(cap, r0 + batch); ++r) {
+                GB_CK(cudaMemsetAsync(&w.ds->changed[r % 64], 0, sizeof(int), st));
+                for (int axis = 0; axis < 3; ++axis)
+                    for (int dir = 1; dir >= -1; dir -= 2) {
+                        launch_sweep(rule, axis, dir, r % 64, src, dst, L, w.ds, st);
+                        std::swap(src, dst);
+                    }
+                launch_end_round(r % 64, r, cap, w.ds, st);
+            }
+            GB_CK(cudaMemcpyAsync(&w.hs->stop, &w.ds->stop, sizeof(int), cudaMemcpyDeviceToHost, st));
+            GB_CK(cudaStreamSynchronize(st));
+            if (w.hs->stop) break;
+        }
+    }
+    // rounds are whole (6 sweeps, an even number), so the field is back in A
+    launch_audit(P<float>(w.A), L, w.ds, st);
+    launch_clamp(P<float>(w.A), P<uint32_t>(w.S), L, w.ds, st);
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaEventRecord(w.ev[6], st));
+    // ---- [E]
+    for (int gen = 0; gen < kProbeGens; ++gen) {
+        launch_verify_prepare(L, gen, P<uint32_t>(w.U), P<long long>(w.list), w.ds, st);
+        launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnVerify, 0, P<uint32_t>(w.S),
+                   P<long long>(w.recheck), kListCap, w.ds, w.num_sms, st);
+        launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnVerify, P<uint32_t>(w.S),
+                           w.ds, w.num_sms, st);
+        launch_verify_plan(gen, w.ds, st);
+        if (gen == kProbeGens - 1) break;  // the last generation never patches
+        launch_patch_mark(L, P<uint32_t>(w.U), w.ds, st);
+        launch_list_unknown(P<uint32_t>(w.U), P<uint32_t>(w.S), L, P<long long>(w.list), kListCap, w.ds, 1, st);
+        launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 1, P<uint32_t>(w.S),
+                   P<long long>(w.recheck), kListCap, w.ds, w.num_sms, st);
+        launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
+                           w.ds, w.num_sms, st);
+    }
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaEventRecord(w.ev[7], st));
+    // ---- [F]
+    float* final_dst = out_dev ? out : P<float>(w.B);
+    launch_apply(P<float>(w.A), P<uint32_t>(w.S), L, final_dst, w.ds, st);
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaEventRecord(w.ev[8], st));
+    GB_CK(cudaMemcpyAsync(w.hs, w.ds, sizeof(DevState), cudaMemcpyDeviceToHost, st));
+    GB_CK(cudaStreamSynchronize(st));
+    const DevState& h = *w.hs;
+    int status = GBSDF_OK;
+    if (h.verify_state != 1) status = e.set(GBSDF_EVERIFY, "sign verification diverged: %d mismatches in probe %d",
+                                            h.probe_m, h.probes - 1);
+    if (status == GBSDF_OK && !out_dev) {
+        GB_CK(cudaMemcpyAsync(out, w.B.p, (size_t)N * 4, cudaMemcpyDeviceToHost, st));
+    }
+    GB_CK(cudaEventRecord(w.ev[9], st));
+    GB_CK(cudaStreamSynchronize(st));
+    if (stats) {
+        stats->ms_prep = ev_ms(w.ev[1], w.ev[2]);
+        stats->ms_splat = ev_ms(w.ev[2], w.ev[3]);
+        stats->ms_parity = ev_ms(w.ev[3], w.ev[4]);
+        stats->ms_fixup = ev_ms(w.ev[4], w.ev[5]);
+        stats->ms_eikonal = ev_ms(w.ev[5], w.ev[6]);
+        stats->ms_verify = ev_ms(w.ev[6], w.ev[7]);
+        stats->ms_apply = ev_ms(w.ev[7], w.ev[8]);
+        stats->ms_d2h = ev_ms(w.ev[8], w.ev[9]);
+        stats->eikonal_rounds = h.rounds;
+        stats->far_residual = (long long)h.far_residual;
+        stats->safe_clamped = (long long)h.far_residual;
+        // the reference runs up to 16 audit-gated extra rounds while a residual remains
+        // (cuda_rasterizer.cu:1028-1037); a residual after a full round means no voxel is
+        // reachable (empty band), so those rounds cannot change anything and are counted,
+        // not run.
+        stats->extra_rounds = (ref_mode && h.far_residual > 0) ? kMaxExtraRounds : 0;
+        if (ref_mode) stats->eikonal_rounds += stats->extra_rounds;
+        stats->far_residual = 0;
+        stats->probes = h.probes;
+        stats->sites = h.total_sites;
+        stats->patch_rounds = h.patch_rounds;
+        stats->unknown_columns = (long long)h.unknown_columns;
+        stats->fixup_voxels = (long long)h.fixup_voxels;
+        stats->patched_voxels = (long long)h.patched_voxels;
+        stats->fp64_rechecks = (long long)h.fp64_rechecks;
+        stats->band_voxels = (long long)h.band_voxels;
+        stats->splat_evals = (long long)h.splat_evals;
+        stats->gwn_pairs = (long long)h.gwn_pairs;
+        stats->brick_pairs = (long long)h.brick_pairs;
+        stats->csr_entries = (long long)h.csr_entries;
+        stats->path_taken = GBSDF_PATH_FAST;
+    }
+    return status;
+}
+
+int run_legacy(Workspace& w, long long T, const Lattice& L, float* out, bool out_dev, gbsdf_stats* stats, Err& e) {
+    cudaStream_t st = w.st;
+    const long long N = L.N;
+    const long long ntiles = (T + 127) / 128;
+    GB_CK(ensure(w.A, (size_t)N * 4));
+    GB_CK(ensure(w.B, (size_t)N * 4));
+    GB_CK(ensure(w.S, (size_t)L.nwords * 4));
+    GB_CK(ensure(w.t9, (size_t)T * 36));
+    GB_CK(ensure(w.hb, (size_t)ntiles * 24));
+    GB_CK(ensure(w.list, (size_t)kListCap * 8));
+    GB_CK(ensure(w.recheck, (size_t)kListCap * 8));
+    GB_CK(cudaMemsetAsync(w.ds, 0, sizeof(DevState), st));
+    GB_CK(cudaMemsetAsync(w.S.p, 0, (size_t)L.nwords * 4, st));
+    launch_pack_tri9(P<float>(w.t12), T, P<float>(w.t9), st);
+    launch_tile_bounds(P<float>(w.t12), T, P<float>(w.hb), st);
+    GB_CK(cudaEventRecord(w.ev[2], st));
+    launch_legacy_dist(P<float>(w.t9), T, P<float>(w.hb), L, P<float>(w.A), st);
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaEventRecord(w.ev[3], st));
+    // exact winding sign of every voxel, in list-sized chunks
+    for (long long v0 = 0; v0 < N; v0 += kListCap) {
+        long long n = std::min(kListCap, N - v0);
+        launch_iota(P<long long>(w.list), n, v0, st);
+        unsigned long long nn = (unsigned long long)n;
+        GB_CK(cudaMemcpyAsync(&w.ds->listed, &nn, sizeof(nn), cudaMemcpyHostToDevice, st));
+        GB_CK(cudaMemsetAsync(&w.ds->recheck_n, 0, sizeof(unsigned long long), st));
+        launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 0, P<uint32_t>(w.S),
+                   P<long long>(w.recheck), kListCap, w.ds, w.num_sms, st);
+        launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
+                           w.ds, w.num_sms, st);
+        GB_CK(cudaStreamSynchronize(st));  // `nn` lives on the host stack
+    }
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaEventRecord(w.ev[4], st));
+    float* final_dst = out_dev ? out : P<float>(w.B);
+    launch_legacy_combine(P<float>(w.A), P<uint32_t>(w.S), L, final_dst, st);
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaEventRecord(w.ev[8], st));
+    if (!out_dev) GB_CK(cudaMemcpyAsync(out, w.B.p, (size_t)N * 4, cudaMemcpyDeviceToHost, st));
+    GB_CK(cudaEventRecord(w.ev[9], st));
+    GB_CK(cudaMemcpyAsync(w.hs, w.ds, sizeof(DevState), cudaMemcpyDeviceToHost, st));
+    GB_CK(cudaStreamSynchronize(st));
+    if (stats) {
+        stats->ms_prep = ev_ms(w.ev[1], w.ev[2]);
+        stats->ms_splat = ev_ms(w.ev[2], w.ev[3]);
+        stats->ms_fixup = ev_ms(w.ev[3], w.ev[4]);
+        stats->ms_apply = ev_ms(w.ev[4], w.ev[8]);
+        stats->ms_d2h = ev_ms(w.ev[8], w.ev[9]);
+        stats->gwn_pairs = (long long)w.hs->gwn_pairs;
+        stats->fp64_rechecks = (long long)w.hs->fp64_rechecks;
+        stats->path_taken = GBSDF_PATH_LEGACY;
+    }
+    return GBSDF_OK;
+}
+
+int compute(const float* tris12, long long T, bool tris_dev, float h, const int32_t mn[3], const int32_t mx[3],
+            float* out, bool out_dev, const gbsdf_options& o, gbsdf_stats* stats, Err& e) {
+    auto t0 = std::chrono::steady_clock::now();
+    const unsigned long long launches0 = launch_counter();
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->status = GBSDF_EINVAL;
+    }
+    if (!mn || !mx || !out) return e.set(GBSDF_EINVAL, "null lattice or output pointer");
+    if (!(h > 0.0f) || !std::isfinite(h)) return e.set(GBSDF_EINVAL, "voxel size must be positive and finite");
+    long long dims[3];
+    for (int k = 0; k < 3; ++k) dims[k] = (long long)mx[k] - mn[k] + 1;
+    if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return e.set(GBSDF_EINVAL, "empty lattice");
+    if (T <= 0 || !tris12) return e.set(GBSDF_EINVAL, "no triangles");
+    if (dims[0] > (1 << 30) || dims[1] > (1 << 30) || dims[2] > (1 << 30))
+        return e.set(GBSDF_EINVAL, "lattice dimension out of range");
+    const long long N = dims[0] * dims[1] * dims[2];
+    int path = o.path;
+    if (path == GBSDF_PATH_AUTO) path = ((unsigned long long)N >= kFastMinVoxels) ? GBSDF_PATH_FAST : GBSDF_PATH_LEGACY;
+    // the reference's int-range guards (cuda_rasterizer.cu:816-820), reference mode only
+    if (path == GBSDF_PATH_FAST && o.mode == GBSDF_MODE_REFERENCE) {
+        const long long G = 2000000000LL;
+        if (N > G || T * dims[2] > G || dims[0] * dims[1] > G || dims[0] * dims[2] > G || dims[1] * dims[2] > G) {
+            if (o.path != GBSDF_PATH_AUTO)
+                return e.set(GBSDF_EGUARD, "reference int-range guard declines the fast path");
+            path = GBSDF_PATH_LEGACY;
+        }
+    }
+    if (T > 0x7fffffffLL) return e.set(GBSDF_EINVAL, "too many triangles");
+    Workspace* wp;
+    {
+        std::lock_guard<std::mutex> g(g_ws_mu);
+        if (o.device < 0 || o.device >= 64) return e.set(GBSDF_ENODEV, "device %d out of range", o.device);
+        wp = &g_ws[o.device];
+    }
+    Workspace& w = *wp;
+    std::lock_guard<std::mutex> lk(w.mu);
+    int rc = init_ws(w, o.device, e);
+    if (rc != GBSDF_OK) return rc;
+    GB_CK(cudaSetDevice(o.device));
+    Lattice L = make_lattice(mn, mx, h);
+    GB_CK(cudaEventRecord(w.ev[0], w.st));
+    if (tris_dev) {
+        GB_CK(ensure(w.t12, (size_t)T * 48));
+        GB_CK(cudaMemcpyAsync(w.t12.p, tris12, (size_t)T * 48, cudaMemcpyDeviceToDevice, w.st));
+    } else {
+        GB_CK(ensure(w.t12, (size_t)T * 48));
+        GB_CK(cudaMemcpyAsync(w.t12.p, tris12, (size_t)T * 48, cudaMemcpyHostToDevice, w.st));
+    }
+    GB_CK(cudaEventRecord(w.ev[1], w.st));
+    if (path == GBSDF_PATH_FAST) {
+        rc = run_fast(w, T, L, o, out, out_dev, stats, e);
+        if (rc == GBSDF_EVERIFY || rc == GBSDF_ECSR) {
+            if (o.path == GBSDF_PATH_AUTO) rc = run_legacy(w, T, L, out, out_dev, stats, e);  // reference fall-through
+        }
+    } else {
+        rc = run_legacy(w, T, L, out, out_dev, stats, e);
+    }
+    if (stats) {
+        stats->ms_h2d = ev_ms(w.ev[0], w.ev[1]);
+        stats->status = rc;
+        stats->kernel_launches = (long long)(launch_counter() - launches0);
+        stats->ms_total =
+            std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (rc != GBSDF_OK) {
+        // leave the stream clean for the next call
+        cudaStreamSynchronize(w.st);
+        cudaGetLastError();
+    }
+    return rc;
+}
+
+}  // namespace
+}  // namespace gbsdf
+
+using namespace gbsdf;
+
+extern "C" {
+
+void gbsdf_default_options(gbsdf_options* opt) {
+    if (!opt) return;
+    std::memset(opt, 0, sizeof(*opt));
+    opt->mode = GBSDF_MODE_REFERENCE;
+    opt->path = GBSDF_PATH_AUTO;
+}
+
+int gbsdf_compute_mesh_sdf(const gbsdf_tri* tris, int64_t n_tris, float voxel_size, const int32_t min_coord[3],
+                           const int32_t max_coord[3], float* out, int32_t out_on_device, const gbsdf_options* opt,
+                           gbsdf_stats* stats, char* err, size_t errlen) {
+    Err e{err, errlen};
+    if (err && errlen) err[0] = 0;
+    gbsdf_options o;
+    gbsdf_default_options(&o);
+    if (opt) o = *opt;
+    return compute(reinterpret_cast<const float*>(tris), n_tris, o.tris_on_device != 0, voxel_size, min_coord,
+                   max_coord, out, out_on_device != 0, o, stats, e);
+}
+
+int gbsdf_mesh_lattice(const float* verts, int64_t n_verts, float voxel_size, int32_t min_coord[3],
+                       int32_t max_coord[3], char* err, size_t errlen) {
+    Err e{err, errlen};
+    if (err && errlen) err[0] = 0;
+    if (!verts || n_verts <= 0) return e.set(GBSDF_EINVAL, "no vertices");
+    if (!(voxel_size > 0.0f) || !std::isfinite(voxel_size)) return e.set(GBSDF_EINVAL, "bad voxel size");
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+    for (int64_t i = 0; i < n_verts; ++i)
+        for (int k = 0; k < 3; ++k) {
+            float v = verts[3 * i + k];
+            if (!std::isfinite(v)) return e.set(GBSDF_EINVAL, "non-finite vertex %lld", (long long)i);
+            lo[k] = std::fmin(lo[k], v);
+            hi[k] = std::fmax(hi[k], v);
+        }
+    // cuda_rasterizer.cu:1358-1372, with the integer range validated in FP64 first
+    float pad = voxel_size * 10.0f;
+    for (int k = 0; k < 3; ++k) {
+        double a = std::floor((double)((lo[k] - pad) / voxel_size));
+        double b = std::ceil((double)((hi[k] + pad) / voxel_size));
+        if (!(a > -1.0e9 && b < 1.0e9)) return e.set(GBSDF_EINVAL, "lattice out of integer range");
+        min_coord[k] = (int32_t)std::floor((lo[k] - pad) / voxel_size);
+        max_coord[k] = (int32_t)std::ceil((hi[k] + pad) / voxel_size);
+    }
+    return GBSDF_OK;
+}
+
+int gbsdf_build_from_mesh(const float* verts, int64_t n_verts, const uint32_t* indices, int64_t n_indices,
+                          float voxel_size, const int32_t min_coord[3], const int32_t max_coord[3], float* out,
+                          int32_t out_on_device, const gbsdf_options* opt, gbsdf_stats* stats, char* err,
+                          size_t errlen) {
+    Err e{err, errlen};
+    if (err && errlen) err[0] = 0;
+    gbsdf_options o;
+    gbsdf_default_options(&o);
+    if (opt) o = *opt;
+    if (!verts || n_verts <= 0 || !indices || n_indices < 3) return e.set(GBSDF_EINVAL, "empty mesh");
+    const long long nt = n_indices / 3;
+    Workspace* wp;
+    {
+        std::lock_guard<std::mutex> g(g_ws_mu);
+        if (o.device < 0 || o.device >= 64) return e.set(GBSDF_ENODEV, "device %d out of range", o.device);
+        wp = &g_ws[o.device];
+    }
+    Workspace& w = *wp;
+    long long kept = 0;
+    float* tris_dev = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(w.mu);
+        int rc = init_ws(w, o.device, e);
+        if (rc != GBSDF_OK) return rc;
+        GB_CK(cudaSetDevice(o.device));
+        cudaStream_t st = w.st;
+        GB_CK(ensure(w.verts, (size_t)n_verts * 12));
+        GB_CK(ensure(w.idx, (size_t)nt * 12));
+        GB_CK(ensure(w.flags, (size_t)nt * 4));
+        GB_CK(ensure(w.fpos, (size_t)nt * 8));
+        GB_CK(ensure(w.scan, (size_t)scan_tmp_elems(nt) * 8));
+        GB_CK(cudaMemcpyAsync(w.verts.p, verts, (size_t)n_verts * 12, cudaMemcpyHostToDevice, st));
+        GB_CK(cudaMemcpyAsync(w.idx.p, indices, (size_t)nt * 12, cudaMemcpyHostToDevice, st));
+        launch_tri_flags(P<float>(w.verts), n_verts, P<uint32_t>(w.idx), nt, P<unsigned>(w.flags), st);
+        launch_exclusive_scan(P<unsigned>(w.flags), P<unsigned long long>(w.fpos), nt,
+                              P<unsigned long long>(w.scan), 0, st);
+        unsigned long long last_pos = 0;
+        unsigned last_flag = 0;
+        GB_CK(cudaMemcpyAsync(&last_pos, P<unsigned long long>(w.fpos) + (nt - 1), 8, cudaMemcpyDeviceToHost, st));
+        GB_CK(cudaMemcpyAsync(&last_flag, P<unsigned>(w.flags) + (nt - 1), 4, cudaMemcpyDeviceToHost, st));
+        GB_CK(cudaStreamSynchronize(st));
+        kept = (long long)last_pos + last_flag;
+        if (kept <= 0) return e.set(GBSDF_EINVAL, "mesh has no non-degenerate triangle");
+        GB_CK(cudaMalloc(&tris_dev, (size_t)kept * 48));
+        launch_tri_scatter(P<float>(w.verts), n_verts, P<uint32_t>(w.idx), nt, P<unsigned long long>(w.fpos),
+                           tris_dev, st);
+        GB_CK(cudaGetLastError());
+        GB_CK(cudaStreamSynchronize(st));
+    }
+    o.tris_on_device = 1;
+    int rc = compute(tris_dev, kept, true, voxel_size, min_coord, max_coord, out, out_on_device != 0, o, stats, e);
+    cudaFree(tris_dev);
+    return rc;
+}
+
+void gbsdf_release_workspace(int32_t device) {
+    if (device < 0 || device >= 64) return;
+    std::lock_guard<std::mutex> g(g_ws_mu);
+    std::lock_guard<std::mutex> lk(g_ws[device].mu);
+    free_ws(g_ws[device]);
+}
+
+const char* gbsdf_version(void) { return "gbsdf 0.1 (sm_103a)"; }
+
+}  // extern "C"

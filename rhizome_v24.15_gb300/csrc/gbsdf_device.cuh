@@ -1,0 +1,180 @@
+// gbsdf_device.cuh — device-side geometry and eikonal arithmetic for the GB300
+// mesh-to-SDF engine.
+//
+// Every translation unit of the engine is compiled with -fmad=false: products
+// and sums round separately, in the operation order of the reference's
+// expressions (native/src/core/math_utils.cuh, native/src/engine/sdf/
+// cuda_rasterizer.cu), so band distances, parity hits and eikonal updates are
+// bit-identical to a contraction-free CPU evaluation of the same formulas.
+// Where speed matters more than bit-identity (the FP32 winding sum, whose
+// sign decisions are re-checked in FP64 near the threshold), fused
+// multiply-adds are written explicitly with __fmaf_rn.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbsdf {
+
+// ---- constants of the reference path (cuda_rasterizer.cu:74-82, :298-299, :825, :1010, :1027)
+constexpr int kBandVoxels = 8;
+constexpr int kParityMaxHits = 128;
+constexpr float kFarSentinel = 1e30f;
+constexpr int kVerifySamples = 4096;
+constexpr int kProbeGens = 3;
+constexpr int kMaxSitesPerProbe = 64;
+constexpr int kPatchRadius = 24;
+constexpr int kSup = 4;
+constexpr int kMaxRounds = 8;
+constexpr int kMaxExtraRounds = 16;
+constexpr float kJX = 0.037f;
+constexpr float kJY = 0.051f;
+constexpr float kInv4Pi = 0.07957747154594767f;
+constexpr float kRecheckBand = 0.05f;  // FP64 re-evaluation when | |w| - 0.5 | < this
+constexpr unsigned long long kFastMinVoxels = 32ull * 1024ull * 1024ull;
+
+// Brick edge of the band splat and lattice strip width of the parity pass.
+constexpr int kBrick = 8;
+constexpr int kStrip = 32;
+
+struct f3 {
+    float x, y, z;
+};
+__host__ __device__ __forceinline__ f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+__host__ __device__ __forceinline__ f3 sub(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__host__ __device__ __forceinline__ f3 add(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__host__ __device__ __forceinline__ f3 mul(f3 a, float s) { return f3{a.x * s, a.y * s, a.z * s}; }
+// glm::dot on vec3: (x*x' + y*y') + z*z'
+__host__ __device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// Exact point-triangle squared distance, point_triangle_distance_sq
+// (math_utils.cuh:43-106): Ericson's seven Voronoi regions, same branch order.
+__device__ __forceinline__ float ptd_sq(f3 p, f3 a, f3 b, f3 c) {
+    f3 ab = sub(b, a), ac = sub(c, a), ap = sub(p, a);
+    float d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= 0.0f && d2 <= 0.0f) return dot(ap, ap);
+    f3 bp = sub(p, b);
+    float d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= 0.0f && d4 <= d3) return dot(bp, bp);
+    float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) {
+        float v = d1 / (d1 - d3);
+        f3 df = sub(p, add(a, mul(ab, v)));
+        return dot(df, df);
+    }
+    f3 cp = sub(p, c);
+    float d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= 0.0f && d5 <= d6) return dot(cp, cp);
+    float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) {
+        float w = d2 / (d2 - d6);
+        f3 df = sub(p, add(a, mul(ac, w)));
+        return dot(df, df);
+    }
+    float va = d3 * d6 - d5 * d4;
+    if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f) {
+        float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        f3 df = sub(p, add(b, mul(sub(c, b), w)));
+        return dot(df, df);
+    }
+    float denom = 1.0f / (va + vb + vc);
+    float v = vb * denom, w = vc * denom;
+    f3 df = sub(p, add(add(a, mul(ab, v)), mul(ac, w)));
+    return dot(df, df);
+}
+
+// Triangle solid angle (Van Oosterom-Strackee), triangle_solid_angle
+// (math_utils.cuh:109-132), FP32 with explicit FMAs: the winding sum's sign is
+// decided exactly by re-evaluating in FP64 near the threshold, so this form is
+// free to be fast.
+__device__ __forceinline__ float solid_angle_fast(f3 p, f3 v0, f3 v1, f3 v2) {
+    float ax = v0.x - p.x, ay = v0.y - p.y, az = v0.z - p.z;
+    float bx = v1.x - p.x, by = v1.y - p.y, bz = v1.z - p.z;
+    float cx = v2.x - p.x, cy = v2.y - p.y, cz = v2.z - p.z;
+    float la = sqrtf(__fmaf_rn(az, az, __fmaf_rn(ay, ay, ax * ax)));
+    float lb = sqrtf(__fmaf_rn(bz, bz, __fmaf_rn(by, by, bx * bx)));
+    float lc = sqrtf(__fmaf_rn(cz, cz, __fmaf_rn(cy, cy, cx * cx)));
+    if (la <= 1e-6f || lb <= 1e-6f || lc <= 1e-6f) return 0.0f;
+    float det = __fmaf_rn(az, __fmaf_rn(bx, cy, -(by * cx)),
+                          __fmaf_rn(-ay, __fmaf_rn(bx, cz, -(bz * cx)), ax * __fmaf_rn(by, cz, -(bz * cy))));
+    float ab = __fmaf_rn(az, bz, __fmaf_rn(ay, by, ax * bx));
+    float bc = __fmaf_rn(bz, cz, __fmaf_rn(by, cy, bx * cx));
+    float ca = __fmaf_rn(cz, az, __fmaf_rn(cy, ay, cx * ax));
+    float denom = __fmaf_rn(ca, lb, __fmaf_rn(bc, la, __fmaf_rn(ab, lc, la * lb * lc)));
+    return 2.0f * atan2f(det, denom);
+}
+
+// The same formula in FP64 from the FP32 inputs (used only for re-checks).
+__device__ __forceinline__ double solid_angle_f64(f3 pf, f3 v0, f3 v1, f3 v2) {
+    double px = pf.x, py = pf.y, pz = pf.z;
+    double ax = v0.x - px, ay = v0.y - py, az = v0.z - pz;
+    double bx = v1.x - px, by = v1.y - py, bz = v1.z - pz;
+    double cx = v2.x - px, cy = v2.y - py, cz = v2.z - pz;
+    double la = sqrt(ax * ax + ay * ay + az * az);
+    double lb = sqrt(bx * bx + by * by + bz * bz);
+    double lc = sqrt(cx * cx + cy * cy + cz * cz);
+    if (la <= 1e-6 || lb <= 1e-6 || lc <= 1e-6) return 0.0;
+    double det = ax * (by * cz - bz * cy) - ay * (bx * cz - bz * cx) + az * (bx * cy - by * cx);
+    double denom = la * lb * lc + (ax * bx + ay * by + az * bz) * lc + (bx * cx + by * cy + bz * cz) * la +
+                   (cx * ax + cy * ay + cz * az) * lb;
+    return 2.0 * atan2(det, denom);
+}
+
+// The reference's Godunov update, rhi_eikonal_godunov (cuda_rasterizer.cu:405-425),
+// operation for operation (including its halved 3D pairwise sum).
+__device__ __forceinline__ float godunov_ref(float ax, float ay, float az, float h) {
+    float s0 = fminf(ax, fminf(ay, az));
+    float s2 = fmaxf(ax, fmaxf(ay, az));
+    float s1 = ax + ay + az - s0 - s2;
+    float updated = s0 + h;
+    if (updated > s1) {
+        float disc = 2.0f * h * h - (s1 - s0) * (s1 - s0);
+        if (disc >= 0.0f) {
+            updated = (s0 + s1 + sqrtf(disc)) * 0.5f;
+            if (updated > s2) {
+                float disc3 = 3.0f * h * h -
+                              ((s1 - s0) * (s1 - s0) + (s2 - s1) * (s2 - s1) + (s2 - s0) * (s2 - s0)) * 0.5f;
+                if (disc3 >= 0.0f) updated = (s0 + s1 + s2 + sqrtf(disc3)) / 3.0f;
+            }
+        }
+    }
+    return updated;
+}
+
+// Corrected, monotone Godunov update (the engine's exact mode): sorted minima,
+// true 3D discriminant 3h^2 - sum_{i<j}(s_i - s_j)^2, increments formed from
+// differences and added to the smallest neighbour once.
+__device__ __forceinline__ float godunov_exact(float a, float b, float c, float h) {
+    float lo = fminf(a, b), hi = fmaxf(a, b);
+    float s0 = fminf(lo, c);
+    float m = fmaxf(lo, c);
+    float s1 = fminf(m, hi);
+    float s2 = fmaxf(m, hi);
+    float u = s0 + h;
+    if (u > s1) {
+        float d1 = s1 - s0;
+        float disc = 2.0f * h * h - d1 * d1;
+        float inc = (d1 + sqrtf(fmaxf(disc, 0.0f))) * 0.5f;
+        u = s0 + inc;
+        if (u > s2) {
+            float d2 = s2 - s0;
+            float e = s2 - s1;
+            float disc3 = 3.0f * h * h - (d1 * d1 + e * e + d2 * d2);
+            float inc3 = (d1 + d2 + sqrtf(fmaxf(disc3, 0.0f))) / 3.0f;
+            u = s0 + inc3;
+        }
+    }
+    return u;
+}
+
+template <int RULE>
+__device__ __forceinline__ float godunov(float ax, float ay, float az, float h) {
+    if constexpr (RULE == 0) return godunov_ref(ax, ay, az, h);
+    else return godunov_exact(ax, ay, az, h);
+}
+
+// Voxel lattice point, as the reference forms it: (min + i) * h in FP32.
+__device__ __forceinline__ f3 lattice_point(int mnx, int mny, int mnz, int x, int y, int z, float h) {
+    return f3{(float)(mnx + x) * h, (float)(mny + y) * h, (float)(mnz + z) * h};
+}
+
+}  // namespace gbsdf

@@ -1,0 +1,322 @@
+// k_gwn.cu — exact generalized-winding-number signs: the fixup [C] of unknown
+// voxels and the stratified verify / patch loop [E] of the mesh-to-SDF path.
+//
+// Reference: gpu_exact_winding_fixup_kernel (cuda_rasterizer.cu:374-400) scans all
+// N voxels and sums every triangle's solid angle for each unknown one in plain FP32
+// index order; gpu_verify_sign_samples_kernel (:566-607), gpu_mark_patch_unknown_kernel
+// (:615-646) and the host loop (:1078-1132) probe 3 x 4096 stratified voxels and patch
+// (2*24+1)^3 boxes around mismatches.
+//
+// Here:
+//  * unknown voxels are first compacted from the 1-bit unknown mask into a dense
+//    list, so the O(voxels x triangles) kernel runs with every lane busy;
+//  * the winding sum is FP32 with Kahan compensation, the triangles staged through
+//    shared memory in chunks shared by the whole CTA; one voxel per thread for long
+//    lists, one voxel per warp (triangles split over lanes) for short ones;
+//  * every voxel whose FP32 |w| lies within 0.05 of 0.5 is re-evaluated in FP64 by a
+//    CTA (deterministic tree reduction), so each inside/outside decision is the
+//    exact-arithmetic one: inside iff |w| >= 0.5, the reference's rule;
+//  * the probe / patch control runs on the device (state in DevState), so the loop
+//    needs no host round trip per probe.
+#include "gbsdf_device.cuh"
+#include "gbsdf_internal.h"
+
+namespace gbsdf {
+
+namespace {
+
+constexpr int kGwnThreads = 256;
+constexpr int kGwnChunk = 256;  // triangles staged per chunk (9 floats each)
+
+__device__ __forceinline__ void voxel_coords(const Lattice& L, long long v, int& x, int& y, int& z) {
+    long long dx = L.dims[0], dy = L.dims[1];
+    x = (int)(v % dx);
+    long long r = v / dx;
+    y = (int)(r % dy);
+    z = (int)(r / dy);
+}
+
+__device__ __forceinline__ size_t word_of(const Lattice& L, int x, int y, int z) {
+    return ((size_t)z * L.dims[1] + y) * L.wx + (x >> 5);
+}
+
+__device__ __forceinline__ void consume(const Lattice& L, long long v, bool inside, int consumer,
+                                        uint32_t* sbits, DevState* ds) {
+    int x, y, z;
+    voxel_coords(L, v, x, y, z);
+    size_t w = word_of(L, x, y, z);
+    uint32_t bit = 1u << (x & 31);
+    if (consumer == kGwnFixup) {
+        if (inside) atomicOr(&sbits[w], bit);
+    } else {
+        bool s = (sbits[w] & bit) != 0u;
+        if (s != inside) {
+            int m = atomicAdd(&ds->probe_m, 1);
+            if (m < kVerifySamples) ds->sites[m] = v;
+        }
+    }
+}
+
+__global__ void list_unknown_kernel(uint32_t* __restrict__ ubits, uint32_t* __restrict__ sbits, Lattice L,
+                                    long long* __restrict__ list, long long cap, DevState* ds, int only_if_patching) {
+    if (only_if_patching && !ds->patching) return;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < L.nwords; w += stride) {
+        uint32_t u = ubits[w];
+        if (u == 0u) continue;
+        int n = __popc(u);
+        unsigned long long pos = atomicAdd(&ds->listed, (unsigned long long)n);
+        if ((long long)(pos + n) > cap) {
+            for (long long k = (long long)pos; k < cap && k < (long long)pos + n; ++k) list[k] = -1;
+            atomicAdd(&ds->list_overflow, 1ull);
+            continue;
+        }
+        long long row = w / L.wx;
+        int xw = (int)(w % L.wx);
+        long long base = row * L.dims[0] + (long long)xw * 32;
+        uint32_t m = u;
+        while (m) {
+            int b = __ffs(m) - 1;
+            m &= m - 1u;
+            list[pos++] = base + b;
+        }
+        ubits[w] = 0u;
+        sbits[w] &= ~u;
+        if (only_if_patching) atomicAdd(&ds->patched_voxels, (unsigned long long)n);
+        else atomicAdd(&ds->fixup_voxels, (unsigned long long)n);
+    }
+}
+
+// Kahan step
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+template <int TEAM>
+__global__ void __launch_bounds__(kGwnThreads) gwn_kernel(const float* __restrict__ tri9, long long T, Lattice L,
+                                                          const long long* __restrict__ list, long long cap,
+                                                          int consumer, int only_if, uint32_t* __restrict__ sbits,
+                                                          long long* __restrict__ recheck, long long recheck_cap,
+                                                          DevState* ds) {
+    if (only_if && !ds->patching) return;
+    constexpr int VPB = kGwnThreads / TEAM;
+    __shared__ float s_tri[kGwnChunk * 9];
+    const long long n = min((long long)ds->listed, cap);
+    const int member = threadIdx.x % TEAM;
+    const int slot = threadIdx.x / TEAM;
+    unsigned long long pairs = 0;
+    for (long long base = (long long)blockIdx.x * VPB; base < n; base += (long long)gridDim.x * VPB) {
+        const long long j = base + slot;
+        long long v = (j < n) ? list[j] : -1;
+        f3 p = mk(0.f, 0.f, 0.f);
+        if (v >= 0) {
+            int x, y, z;
+            voxel_coords(L, v, x, y, z);
+            p = lattice_point(L.mn[0], L.mn[1], L.mn[2], x, y, z, L.h);
+        }
+        float s = 0.0f, c = 0.0f;
+        for (long long c0 = 0; c0 < T; c0 += kGwnChunk) {
+            int m = (int)min((long long)kGwnChunk, T - c0);
+            __syncthreads();
+            for (int k = threadIdx.x; k < m * 9; k += kGwnThreads) s_tri[k] = __ldg(tri9 + c0 * 9 + k);
+            __syncthreads();
+            if (v >= 0) {
+                for (int i = member; i < m; i += TEAM) {
+                    const float* t = s_tri + i * 9;
+                    kahan_add(s, c, solid_angle_fast(p, mk(t[0], t[1], t[2]), mk(t[3], t[4], t[5]),
+                                                     mk(t[6], t[7], t[8])));
+                }
+            }
+        }
+        if constexpr (TEAM > 1) {
+            // combine the lanes' compensated partials in a fixed order
+            float tot = s - c;
+#pragma unroll
+            for (int o = TEAM / 2; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o, TEAM);
+            s = tot;
+            c = 0.0f;
+        }
+        if (v >= 0 && member == 0) {
+            pairs += (unsigned long long)T;
+            float w = (s - c) * kInv4Pi;
+            float aw = fabsf(w);
+            if (fabsf(aw - 0.5f) < kRecheckBand) {
+                unsigned long long r = atomicAdd(&ds->recheck_n, 1ull);
+                if ((long long)r < recheck_cap) recheck[r] = v;
+            } else {
+                consume(L, v, aw >= 0.5f, consumer, sbits, ds);
+            }
+        }
+    }
+    if (pairs) atomicAdd(&ds->gwn_pairs, pairs);
+}
+
+constexpr int kRecheckThreads = 256;
+
+__global__ void __launch_bounds__(kRecheckThreads) gwn_recheck_kernel(const float* __restrict__ tri9, long long T,
+                                                                      Lattice L,
+                                                                      const long long* __restrict__ recheck,
+                                                                      long long cap, int consumer,
+                                                                      uint32_t* __restrict__ sbits, DevState* ds) {
+    __shared__ double red[kRecheckThreads];
+    const long long n = min((long long)ds->recheck_n, cap);
+    for (long long e = blockIdx.x; e < n; e += gridDim.x) {
+        long long v = recheck[e];
+        int x, y, z;
+        voxel_coords(L, v, x, y, z);
+        f3 p = lattice_point(L.mn[0], L.mn[1], L.mn[2], x, y, z, L.h);
+        double s = 0.0;
+        for (long long t = threadIdx.x; t < T; t += kRecheckThreads) {
+            const float* q = tri9 + t * 9;
+            s += solid_angle_f64(p, mk(q[0], q[1], q[2]), mk(q[3], q[4], q[5]), mk(q[6], q[7], q[8]));
+        }
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int o = kRecheckThreads / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            double w = red[0] / (4.0 * 3.14159265358979323846);
+            consume(L, v, fabs(w) >= 0.5, consumer, sbits, ds);
+            atomicAdd(&ds->fp64_rechecks, 1ull);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void verify_prepare_kernel(Lattice L, int gen, const uint32_t* __restrict__ ubits,
+                                      long long* __restrict__ list, DevState* ds) {
+    __shared__ int state;
+    if (threadIdx.x == 0) state = ds->verify_state;
+    __syncthreads();
+    if (state != 0) {
+        if (threadIdx.x == 0) ds->listed = 0;
+        return;
+    }
+    const double off = (gen == 0) ? 0.5 : (gen == 1) ? (1.0 / 6.0) : (5.0 / 6.0);
+    const unsigned long long N = (unsigned long long)L.N;
+    for (int i = threadIdx.x; i < kVerifySamples; i += blockDim.x) {
+        // cuda_rasterizer.cu:582-585
+        unsigned long long v = (unsigned long long)(((double)i + off) * (double)N / (double)kVerifySamples);
+        if (v >= N) v = N - 1;
+        int x, y, z;
+        voxel_coords(L, (long long)v, x, y, z);
+        bool unknown = (ubits[word_of(L, x, y, z)] >> (x & 31)) & 1u;  // sign == 2 -> skipped (:588)
+        list[i] = unknown ? -1 : (long long)v;
+    }
+    if (threadIdx.x == 0) {
+        ds->patching = 0;
+        ds->probe_m = 0;
+        ds->recheck_n = 0;
+        ds->listed = kVerifySamples;
+    }
+}
+
+__global__ void verify_plan_kernel(int gen, DevState* ds) {
+    if (ds->verify_state != 0) return;
+    int m = ds->probe_m;
+    ds->probes += 1;
+    if (m == 0) {
+        ds->verify_state = 1;
+        return;
+    }
+    if (m > kVerifySamples) m = kVerifySamples;
+    if (m > kMaxSitesPerProbe || gen == kProbeGens - 1) {
+        ds->verify_state = 2;
+        return;
+    }
+    ds->patching = 1;
+    ds->total_sites += m;
+    ds->patch_rounds += 1;
+    ds->listed = 0;
+    ds->recheck_n = 0;
+    ds->list_overflow = 0;
+}
+
+__global__ void patch_mark_kernel(Lattice L, uint32_t* __restrict__ ubits, DevState* ds) {
+    if (!ds->patching) return;
+    const int s = blockIdx.x;
+    if (s >= ds->probe_m) return;
+    const long long v = ds->sites[s];
+    int cx, cy, cz;
+    voxel_coords(L, v, cx, cy, cz);
+    const int r = kPatchRadius;
+    int x0 = max(cx - r, 0), y0 = max(cy - r, 0), z0 = max(cz - r, 0);
+    int x1 = min(cx + r, L.dims[0] - 1), y1 = min(cy + r, L.dims[1] - 1), z1 = min(cz + r, L.dims[2] - 1);
+    const int ny = y1 - y0 + 1, nz = z1 - z0 + 1;
+    // one row (y, z) per thread iteration; set the row's x range bit by bit per word
+    for (int k = threadIdx.x; k < ny * nz; k += blockDim.x) {
+        int y = y0 + k % ny, z = z0 + k / ny;
+        for (int xw = x0 >> 5; xw <= (x1 >> 5); ++xw) {
+            int lo = max(x0, xw * 32) - xw * 32, hi = min(x1, xw * 32 + 31) - xw * 32;
+            uint32_t mask = (hi == 31 ? 0xffffffffu : ((1u << (hi + 1)) - 1u)) & ~((1u << lo) - 1u);
+            atomicOr(&ubits[((size_t)z * L.dims[1] + y) * L.wx + xw], mask);
+        }
+    }
+}
+
+}  // namespace
+
+void launch_list_unknown(uint32_t* ubits, uint32_t* sbits, const Lattice& L, long long* list, long long cap,
+                         DevState* ds, int only_if_patching, cudaStream_t st) {
+    long long blocks = std::min<long long>((L.nwords + 255) / 256, 152LL * 16);
+    if (blocks < 1) blocks = 1;
+    GBSDF_COUNT_LAUNCH();
+    list_unknown_kernel<<<(unsigned)blocks, 256, 0, st>>>(ubits, sbits, L, list, cap, ds, only_if_patching);
+}
+
+void launch_gwn(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
+                int consumer, int only_if, uint32_t* sbits, long long* recheck, long long recheck_cap,
+                DevState* ds, int num_sms, cudaStream_t st) {
+    // consumer kGwnVerify lists are short (<= 4096): one voxel per warp.
+    if (consumer == kGwnVerify) {
+        long long blocks = (kVerifySamples + 7) / 8;
+        GBSDF_COUNT_LAUNCH();
+        gwn_kernel<32><<<(unsigned)blocks, kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, only_if,
+                                                                 sbits, recheck, recheck_cap, ds);
+    } else {
+        long long blocks = (long long)num_sms * 8;
+        GBSDF_COUNT_LAUNCH();
+        gwn_kernel<1><<<(unsigned)blocks, kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, only_if,
+                                                                sbits, recheck, recheck_cap, ds);
+    }
+}
+
+void launch_gwn_small(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
+                      int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, DevState* ds,
+                      long long n_hint, cudaStream_t st) {
+    long long blocks = std::max<long long>(1, (n_hint + 7) / 8);
+    GBSDF_COUNT_LAUNCH();
+    gwn_kernel<32><<<(unsigned)blocks, kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, 0, sbits,
+                                                             recheck, recheck_cap, ds);
+}
+
+void launch_gwn_recheck(const float* tri9, long long T, const Lattice& L, const long long* recheck,
+                        long long recheck_cap, int consumer, uint32_t* sbits, DevState* ds, int num_sms,
+                        cudaStream_t st) {
+    GBSDF_COUNT_LAUNCH();
+    gwn_recheck_kernel<<<(unsigned)(num_sms * 4), kRecheckThreads, 0, st>>>(tri9, T, L, recheck, recheck_cap,
+                                                                          consumer, sbits, ds);
+}
+
+void launch_verify_prepare(const Lattice& L, int gen, const uint32_t* ubits, long long* list, DevState* ds,
+                           cudaStream_t st) {
+    GBSDF_COUNT_LAUNCH();
+    verify_prepare_kernel<<<1, 1024, 0, st>>>(L, gen, ubits, list, ds);
+}
+
+void launch_verify_plan(int gen, DevState* ds, cudaStream_t st) {
+    GBSDF_COUNT_LAUNCH();
+    verify_plan_kernel<<<1, 1, 0, st>>>(gen, ds);
+}
+
+void launch_patch_mark(const Lattice& L, uint32_t* ubits, DevState* ds, cudaStream_t st) {
+    GBSDF_COUNT_LAUNCH();
+    patch_mark_kernel<<<kMaxSitesPerProbe, 256, 0, st>>>(L, ubits, ds);
+}
+
+}  // namespace gbsdf

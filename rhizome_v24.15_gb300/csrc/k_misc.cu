@@ -1,0 +1,190 @@
+// k_misc.cu — front-end and legacy-path kernels of the mesh-to-SDF engine:
+//   * deterministic triangle build from an indexed mesh (build_from_mesh front-end),
+//   * the legacy exact kernel's distance pass (mesh_to_sdf_kernel),
+//   * small packing / combine helpers.
+#include <algorithm>
+
+#include "gbsdf_device.cuh"
+#include "gbsdf_internal.h"
+
+namespace gbsdf {
+
+namespace {
+
+// dev_try_build_cuda_triangle (math_utils.cuh:484-514): indices in range and
+// |cross(v1-v0, v2-v0)|^2 > 1e-12.
+__device__ __forceinline__ bool build_one(const float* __restrict__ verts, long long nv,
+                                          const uint32_t* __restrict__ idx, long long t, float* out12) {
+    uint32_t i0 = idx[3 * t], i1 = idx[3 * t + 1], i2 = idx[3 * t + 2];
+    if ((long long)i0 >= nv || (long long)i1 >= nv || (long long)i2 >= nv) return false;
+    f3 v0 = mk(verts[3ll * i0], verts[3ll * i0 + 1], verts[3ll * i0 + 2]);
+    f3 v1 = mk(verts[3ll * i1], verts[3ll * i1 + 1], verts[3ll * i1 + 2]);
+    f3 v2 = mk(verts[3ll * i2], verts[3ll * i2 + 1], verts[3ll * i2 + 2]);
+    f3 a = sub(v1, v0), b = sub(v2, v0);
+    f3 n = mk(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+    float len2 = dot(n, n);
+    if (!(len2 > 1e-12f)) return false;
+    if (out12) {
+        float inv = rsqrtf(len2);
+        out12[0] = v0.x; out12[1] = v0.y; out12[2] = v0.z;
+        out12[3] = v1.x; out12[4] = v1.y; out12[5] = v1.z;
+        out12[6] = v2.x; out12[7] = v2.y; out12[8] = v2.z;
+        out12[9] = n.x * inv; out12[10] = n.y * inv; out12[11] = n.z * inv;
+    }
+    return true;
+}
+
+__global__ void tri_flags_kernel(const float* __restrict__ verts, long long nv, const uint32_t* __restrict__ idx,
+                                 long long nt, unsigned* __restrict__ flags) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nt) flags[t] = build_one(verts, nv, idx, t, nullptr) ? 1u : 0u;
+}
+
+// Scatter kept faces to their prefix-sum slot: index order is preserved (the
+// reference's atomicAdd compaction, cuda_rasterizer.cu:1321-1337, is not).
+__global__ void tri_scatter_kernel(const float* __restrict__ verts, long long nv, const uint32_t* __restrict__ idx,
+                                   long long nt, const unsigned long long* __restrict__ pos,
+                                   float* __restrict__ out) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    float r[12];
+    if (build_one(verts, nv, idx, t, r)) {
+        float* o = out + 12 * pos[t];
+        for (int k = 0; k < 12; ++k) o[k] = r[k];
+    }
+}
+
+__global__ void pack_tri9_kernel(const float* __restrict__ t12, long long T, float* __restrict__ t9) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    for (int k = 0; k < 9; ++k) t9[9 * t + k] = t12[12 * t + k];
+}
+
+// Legacy tile headers: per 128-triangle tile the min / max of its vertices
+// (cuda_rasterizer.cu:1200-1213; only the bounds are used by the active branch).
+__global__ void tile_bounds_kernel(const float* __restrict__ t12, long long T, int tile, float* __restrict__ hb) {
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long ntiles = (T + tile - 1) / tile;
+    if (k >= ntiles) return;
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+    for (long long i = k * tile; i < min(T, (k + 1) * tile); ++i)
+        for (int a = 0; a < 3; ++a) {
+            float v0 = t12[12 * i + a], v1 = t12[12 * i + 3 + a], v2 = t12[12 * i + 6 + a];
+            lo[a] = fminf(lo[a], fminf(v0, fminf(v1, v2)));
+            hi[a] = fmaxf(hi[a], fmaxf(v0, fmaxf(v1, v2)));
+        }
+    for (int a = 0; a < 3; ++a) {
+        hb[6 * k + a] = lo[a];
+        hb[6 * k + 3 + a] = hi[a];
+    }
+}
+
+constexpr int kLegTile = 128;  // RASTER_TILE_SIZE (math_utils.cuh:35)
+
+// Legacy distance pass (cuda_rasterizer.cu:97-185): per voxel, exact squared
+// distance minimised over 128-triangle tiles, a tile skipped when its box distance
+// is not below the running minimum (the reference's can_contain_closer test).
+// Writes min d^2; the winding sign comes from the exact winding kernels.
+__global__ void __launch_bounds__(256) legacy_dist_kernel(const float* __restrict__ t9, long long T,
+                                                          const float* __restrict__ hb, Lattice L,
+                                                          float* __restrict__ d2out) {
+    __shared__ float s[kLegTile * 9];
+    const long long ntiles = (T + kLegTile - 1) / kLegTile;
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool ok = v < L.N;
+    int x = 0, y = 0, z = 0;
+    if (ok) {
+        x = (int)(v % L.dims[0]);
+        long long r = v / L.dims[0];
+        y = (int)(r % L.dims[1]);
+        z = (int)(r / L.dims[1]);
+    }
+    const f3 p = lattice_point(L.mn[0], L.mn[1], L.mn[2], x, y, z, L.h);
+    float mind = 1e12f;
+    for (long long t = 0; t < ntiles; ++t) {
+        const long long t0 = t * kLegTile;
+        const int m = (int)min((long long)kLegTile, T - t0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < m * 9; k += blockDim.x) s[k] = t9[t0 * 9 + k];
+        __syncthreads();
+        if (!ok) continue;
+        const float* hh = hb + 6 * t;
+        float bdx = (p.x < hh[0]) ? (hh[0] - p.x) : ((p.x > hh[3]) ? (p.x - hh[3]) : 0.0f);
+        float bdy = (p.y < hh[1]) ? (hh[1] - p.y) : ((p.y > hh[4]) ? (p.y - hh[4]) : 0.0f);
+        float bdz = (p.z < hh[2]) ? (hh[2] - p.z) : ((p.z > hh[5]) ? (p.z - hh[5]) : 0.0f);
+        float box = bdx * bdx + bdy * bdy + bdz * bdz;
+        if (!(box < mind)) continue;
+        for (int i = 0; i < m; ++i) {
+            const float* q = s + 9 * i;
+            float d2 = ptd_sq(p, mk(q[0], q[1], q[2]), mk(q[3], q[4], q[5]), mk(q[6], q[7], q[8]));
+            if (d2 < mind) mind = d2;
+        }
+    }
+    if (ok) d2out[v] = mind;
+}
+
+// out = (inside ? -1 : 1) * sqrt(min d^2)  (cuda_rasterizer.cu:181-184)
+__global__ void legacy_combine_kernel(const float* __restrict__ d2, const uint32_t* __restrict__ sbits, Lattice L,
+                                      float* __restrict__ out) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L.N; i += stride) {
+        long long row = i / L.dims[0];
+        int x = (int)(i - row * L.dims[0]);
+        bool in = (sbits[(size_t)row * L.wx + (x >> 5)] >> (x & 31)) & 1u;
+        float sg = in ? -1.0f : 1.0f;
+        out[i] = sg * sqrtf(d2[i]);
+    }
+}
+
+__global__ void iota_kernel(long long* __restrict__ list, long long n, long long from) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) list[i] = from + i;
+}
+
+}  // namespace
+
+void launch_pack_tri9(const float* tris12, long long T, float* tri9, cudaStream_t st) {
+    if (T <= 0) return;
+    GBSDF_COUNT_LAUNCH();
+    pack_tri9_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(tris12, T, tri9);
+}
+
+void launch_tri_flags(const float* verts, long long nv, const uint32_t* idx, long long nt, unsigned* flags,
+                      cudaStream_t st) {
+    if (nt <= 0) return;
+    GBSDF_COUNT_LAUNCH();
+    tri_flags_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(verts, nv, idx, nt, flags);
+}
+
+void launch_tri_scatter(const float* verts, long long nv, const uint32_t* idx, long long nt,
+                        const unsigned long long* pos, float* out, cudaStream_t st) {
+    if (nt <= 0) return;
+    GBSDF_COUNT_LAUNCH();
+    tri_scatter_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(verts, nv, idx, nt, pos, out);
+}
+
+void launch_tile_bounds(const float* t12, long long T, float* hb, cudaStream_t st) {
+    long long ntiles = (T + kLegTile - 1) / kLegTile;
+    GBSDF_COUNT_LAUNCH();
+    tile_bounds_kernel<<<(unsigned)((ntiles + 127) / 128), 128, 0, st>>>(t12, T, kLegTile, hb);
+}
+
+void launch_legacy_dist(const float* t9, long long T, const float* hb, const Lattice& L, float* d2,
+                        cudaStream_t st) {
+    GBSDF_COUNT_LAUNCH();
+    legacy_dist_kernel<<<(unsigned)((L.N + 255) / 256), 256, 0, st>>>(t9, T, hb, L, d2);
+}
+
+void launch_legacy_combine(const float* d2, const uint32_t* sbits, const Lattice& L, float* out, cudaStream_t st) {
+    long long blocks = std::min<long long>((L.N + 255) / 256, 152LL * 32);
+    GBSDF_COUNT_LAUNCH();
+    legacy_combine_kernel<<<(unsigned)blocks, 256, 0, st>>>(d2, sbits, L, out);
+}
+
+void launch_iota(long long* list, long long n, long long from, cudaStream_t st) {
+    if (n <= 0) return;
+    GBSDF_COUNT_LAUNCH();
+    iota_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(list, n, from);
+}
+
+}  // namespace gbsdf

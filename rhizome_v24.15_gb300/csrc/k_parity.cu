@@ -1,0 +1,118 @@
+// k_parity.cu — scanline parity signs [B] with warp ballots.
+//
+// The reference runs one thread per (x, y) column, gathers up to 128 z-crossings
+// of the jittered column ray from a host-built 4x4-supercell CSR, sorts them and
+// writes one byte per voxel with column-strided stores (cuda_rasterizer.cu:279-368,
+// CSR :824-882). Here one warp owns a strip of 32 adjacent columns of one row: the
+// strip's candidate list is walked uniformly by the warp, each lane keeps its own
+// crossings in shared memory, and the inside/outside state of the 32 lanes at each
+// z is packed into one 32-bit sign word with __ballot_sync -- one store per warp
+// per z, bit-packed signs (1 bit per voxel) instead of bytes.
+//
+// Candidate predicate per (column, triangle), identical to the reference: the
+// column's supercell lies in the triangle's CSR supercell range and the jittered
+// ray passes the triangle's XY AABB; then the 2D edge functions, the |area2| >=
+// 1e-12 test and the barycentric hit height. An odd or overflowing (> 128) hit
+// count marks the whole column unknown (exact winding later).
+#include "gbsdf_device.cuh"
+#include "gbsdf_internal.h"
+
+namespace gbsdf {
+
+namespace {
+
+constexpr int kParWarps = 4;
+
+__global__ void __launch_bounds__(kParWarps * 32) parity_kernel(const ParTri* __restrict__ ptt,
+                                                                const unsigned long long* __restrict__ off,
+                                                                const unsigned* __restrict__ cnt,
+                                                                const unsigned* __restrict__ list, Lattice L,
+                                                                uint32_t* __restrict__ sbits,
+                                                                uint32_t* __restrict__ ubits, DevState* ds) {
+    extern __shared__ float s_hits[];  // [kParWarps][kParityMaxHits][32]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long strip = (long long)blockIdx.x * kParWarps + warp;
+    if (strip >= L.nstrips) return;  // whole warp leaves; no block barrier below
+    float* hits = s_hits + (size_t)warp * kParityMaxHits * 32;
+    const int y = (int)(strip / L.nsx), sx = (int)(strip % L.nsx);
+    const int x = sx * kStrip + lane;
+    const bool col = x < L.dims[0];
+    const float h = L.h;
+    const float rx = ((float)(L.mn[0] + x) + kJX) * h;
+    const float ry = ((float)(L.mn[1] + y) + kJY) * h;
+    const int supx = x >> 2, supy = y >> 2;
+    int nh = 0;
+    bool bad = false;
+    const unsigned long long o = off[strip];
+    const unsigned n = cnt[strip];
+    for (unsigned e = 0; e < n; ++e) {
+        const ParTri& p = ptt[list[o + e]];
+        if (!col || bad) continue;
+        if (supx < p.sx0 || supx > p.sx1 || supy < p.sy0 || supy > p.sy1) continue;
+        const float4 ab = *reinterpret_cast<const float4*>(p.xyab);
+        if (rx < ab.x || rx > ab.z || ry < ab.y || ry > ab.w) continue;
+        const float* v = p.v;
+        float d0 = (v[3] - v[0]) * (ry - v[1]) - (v[4] - v[1]) * (rx - v[0]);
+        float d1 = (v[6] - v[3]) * (ry - v[4]) - (v[7] - v[4]) * (rx - v[3]);
+        float d2 = (v[0] - v[6]) * (ry - v[7]) - (v[1] - v[7]) * (rx - v[6]);
+        bool pos = (d0 > 0.0f && d1 > 0.0f && d2 > 0.0f);
+        bool neg = (d0 < 0.0f && d1 < 0.0f && d2 < 0.0f);
+        if (!pos && !neg) continue;
+        float area2 = d0 + d1 + d2;
+        if (fabsf(area2) < 1e-12f) continue;
+        float zh = (d1 * v[2] + d2 * v[5] + d0 * v[8]) / area2;
+        if (nh < kParityMaxHits) {
+            hits[nh * 32 + lane] = zh;
+            ++nh;
+        } else {
+            bad = true;
+        }
+    }
+    // insertion sort of this lane's crossings
+    for (int i = 1; i < nh; ++i) {
+        float key = hits[i * 32 + lane];
+        int j = i - 1;
+        while (j >= 0 && hits[j * 32 + lane] > key) {
+            hits[(j + 1) * 32 + lane] = hits[j * 32 + lane];
+            --j;
+        }
+        hits[(j + 1) * 32 + lane] = key;
+    }
+    const bool unknown = col && (bad || (nh & 1));
+    const uint32_t uword = __ballot_sync(0xffffffffu, unknown);
+    if (lane == 0 && uword) atomicAdd(&ds->unknown_columns, (unsigned long long)__popc(uword));
+    const bool track = col && !unknown;
+    int k = 0;
+    bool inside = false;
+    const size_t zrow = (size_t)L.dims[1] * L.wx;
+    const size_t wbase = (size_t)y * L.wx + sx;
+    for (int z = 0; z < L.dims[2]; ++z) {
+        const float zc = (float)(L.mn[2] + z) * h;
+        if (track) {
+            while (k < nh && hits[k * 32 + lane] < zc) {
+                inside = !inside;
+                ++k;
+            }
+        }
+        const uint32_t sword = __ballot_sync(0xffffffffu, track && inside);
+        if (lane == 0) {
+            sbits[(size_t)z * zrow + wbase] = sword;
+            ubits[(size_t)z * zrow + wbase] = uword;
+        }
+    }
+}
+
+}  // namespace
+
+void launch_parity(const ParTri* ptt, const unsigned long long* strip_off, const unsigned* strip_count,
+                   const unsigned* strip_list, const Lattice& L, uint32_t* sbits, uint32_t* ubits, DevState* ds,
+                   cudaStream_t st) {
+    const int smem = kParWarps * kParityMaxHits * 32 * (int)sizeof(float);
+    cudaFuncSetAttribute(parity_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    long long blocks = (L.nstrips + kParWarps - 1) / kParWarps;
+    GBSDF_COUNT_LAUNCH();
+    parity_kernel<<<(unsigned)blocks, kParWarps * 32, smem, st>>>(ptt, strip_off, strip_count, strip_list, L, sbits,
+                                                                  ubits, ds);
+}
+
+}  // namespace gbsdf

@@ -1,0 +1,78 @@
+"""ctypes binding of libgbsdf.so (the C ABI declared in include/gbsdf.h).
+
+Loading fails loudly when the CUDA library has not been built: there is no CPU
+fallback anywhere in this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libgbsdf.so"
+
+# gbsdf_status
+OK, EINVAL, EGUARD, ECSR, EVERIFY, ENOMEM, ECUDA, ENODEV = range(8)
+STATUS_NAMES = {OK: "OK", EINVAL: "EINVAL", EGUARD: "EGUARD", ECSR: "ECSR", EVERIFY: "EVERIFY",
+                ENOMEM: "ENOMEM", ECUDA: "ECUDA", ENODEV: "ENODEV"}
+# gbsdf_mode / gbsdf_path
+MODE_REFERENCE, MODE_EXACT = 0, 1
+PATH_AUTO, PATH_FAST, PATH_LEGACY = 0, 1, 2
+
+
+class Options(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("path", C.c_int32), ("device", C.c_int32), ("tris_on_device", C.c_int32),
+                ("max_rounds", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("path_taken", C.c_int32), ("ms_total", C.c_float),
+                ("ms_h2d", C.c_float), ("ms_prep", C.c_float), ("ms_splat", C.c_float), ("ms_parity", C.c_float),
+                ("ms_fixup", C.c_float), ("ms_eikonal", C.c_float), ("ms_verify", C.c_float),
+                ("ms_apply", C.c_float), ("ms_d2h", C.c_float),
+                ("eikonal_rounds", C.c_int32), ("extra_rounds", C.c_int32), ("probes", C.c_int32),
+                ("sites", C.c_int32), ("patch_rounds", C.c_int32), ("pad0", C.c_int32),
+                ("unknown_columns", C.c_int64), ("fixup_voxels", C.c_int64), ("far_residual", C.c_int64),
+                ("safe_clamped", C.c_int64), ("patched_voxels", C.c_int64), ("fp64_rechecks", C.c_int64),
+                ("band_voxels", C.c_int64), ("splat_evals", C.c_int64), ("gwn_pairs", C.c_int64),
+                ("brick_pairs", C.c_int64), ("csr_entries", C.c_int64), ("kernel_launches", C.c_int64),
+                ("reserved", C.c_int64 * 7)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "pad0")}
+
+
+# every exported symbol of include/gbsdf.h
+EXPORTS = ("gbsdf_default_options", "gbsdf_compute_mesh_sdf", "gbsdf_mesh_lattice", "gbsdf_build_from_mesh",
+           "gbsdf_release_workspace", "gbsdf_version")
+
+_lib = None
+
+
+def load(path: Path | None = None):
+    """Load libgbsdf.so (raises if it is missing: build it with __graft_entry__.build())."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(f"{p} is missing: the CUDA engine has not been built (run __graft_entry__.build())")
+    L = C.CDLL(str(p))
+    i32p = C.POINTER(C.c_int32)
+    L.gbsdf_default_options.argtypes = [C.POINTER(Options)]
+    L.gbsdf_default_options.restype = None
+    L.gbsdf_compute_mesh_sdf.argtypes = [C.c_void_p, C.c_int64, C.c_float, i32p, i32p, C.c_void_p, C.c_int32,
+                                         C.POINTER(Options), C.POINTER(Stats), C.c_char_p, C.c_size_t]
+    L.gbsdf_compute_mesh_sdf.restype = C.c_int
+    L.gbsdf_mesh_lattice.argtypes = [C.c_void_p, C.c_int64, C.c_float, i32p, i32p, C.c_char_p, C.c_size_t]
+    L.gbsdf_mesh_lattice.restype = C.c_int
+    L.gbsdf_build_from_mesh.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_float, i32p, i32p,
+                                        C.c_void_p, C.c_int32, C.POINTER(Options), C.POINTER(Stats), C.c_char_p,
+                                        C.c_size_t]
+    L.gbsdf_build_from_mesh.restype = C.c_int
+    L.gbsdf_release_workspace.argtypes = [C.c_int32]
+    L.gbsdf_release_workspace.restype = None
+    L.gbsdf_version.argtypes = []
+    L.gbsdf_version.restype = C.c_char_p
+    if path is None:
+        _lib = L
+    return L

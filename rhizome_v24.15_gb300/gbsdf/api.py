@@ -1,0 +1,178 @@
+"""Host-side mirror of the reference's CudaRasterizer mesh-to-SDF interface.
+
+Reference (golemid/rhizome_v24.15):
+  * ``CudaRasterizer::compute_mesh_sdf`` -- native/src/engine/sdf/cuda_rasterizer.hpp:21-28,
+    cuda_rasterizer.cu:1163-1265: ``(triangles, voxel_size, min_coord, max_coord) ->
+    bool``, ``out_distances`` resized to N and filled, ``out_time_ms`` set; on failure
+    the output is left untouched and ``False`` is returned.
+  * ``CudaRasterizer::build_from_mesh`` -- cuda_rasterizer.hpp:31-35,
+    cuda_rasterizer.cu:1340-1435: ``(mesh, voxel_size) -> CudaVolumeGrid | nullptr``.
+  * ``CudaVolumeGrid`` -- native/src/engine/sdf/cuda_types.hpp:155-175.
+
+Everything runs through the C ABI (include/gbsdf.h) of libgbsdf.so; there is no CPU
+path. Triangles are ``(T, 12)`` float32 arrays in the reference's ``CudaTriangle``
+layout (v0, v1, v2, normal).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import MODE_EXACT, MODE_REFERENCE, PATH_AUTO, PATH_FAST, PATH_LEGACY, STATUS_NAMES
+
+__all__ = ["GbsdfError", "Result", "compute_mesh_sdf", "mesh_lattice", "build_from_mesh", "CudaRasterizer",
+           "CudaVolumeGrid", "MODE_REFERENCE", "MODE_EXACT", "PATH_AUTO", "PATH_FAST", "PATH_LEGACY"]
+
+
+class GbsdfError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"gbsdf {STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+@dataclass
+class Result:
+    status: int
+    stats: dict
+    message: str = ""
+
+    @property
+    def ok(self) -> bool:
+        return self.status == _lib.OK
+
+
+def _i3(v):
+    a = (C.c_int32 * 3)(*[int(x) for x in np.asarray(v).reshape(3)])
+    return a
+
+
+def _ptr_of(buf):
+    """(address, on_device) of a numpy array or a torch tensor."""
+    if isinstance(buf, np.ndarray):
+        if not buf.flags["C_CONTIGUOUS"]:
+            raise ValueError("buffer must be C-contiguous")
+        return buf.ctypes.data, False
+    # torch tensor (duck-typed: data_ptr / is_cuda)
+    if hasattr(buf, "data_ptr"):
+        if not buf.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return buf.data_ptr(), bool(buf.is_cuda)
+    raise TypeError(f"unsupported buffer type {type(buf)}")
+
+
+def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE_REFERENCE, path=PATH_AUTO,
+                     device=0, max_rounds=0, raise_on_error=True):
+    """Run the engine. ``tris``: (T,12) float32 numpy array (host) or CUDA tensor.
+    ``out``: float32 buffer of N voxels (numpy = host, CUDA tensor = device); allocated
+    on the host when None. Returns ``(out, Result)``."""
+    mn = np.asarray(min_coord, np.int64).reshape(3)
+    mx = np.asarray(max_coord, np.int64).reshape(3)
+    dims = mx - mn + 1
+    N = int(np.prod(dims)) if (dims > 0).all() else 0
+    if isinstance(tris, np.ndarray):
+        tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 12)
+    T = int(tris.shape[0])
+    tp, tdev = _ptr_of(tris)
+    if out is None:
+        out = np.empty(max(N, 1), np.float32)
+    op, odev = _ptr_of(out)
+    o = _lib.Options()
+    L = _lib.load()
+    L.gbsdf_default_options(C.byref(o))
+    o.mode, o.path, o.device, o.tris_on_device, o.max_rounds = int(mode), int(path), int(device), int(tdev), int(max_rounds)
+    st = _lib.Stats()
+    err = C.create_string_buffer(512)
+    rc = L.gbsdf_compute_mesh_sdf(tp, T, float(voxel_size), _i3(mn), _i3(mx), op, int(odev), C.byref(o),
+                                  C.byref(st), err, len(err))
+    res = Result(rc, st.as_dict(), err.value.decode(errors="replace"))
+    if rc != _lib.OK and raise_on_error:
+        raise GbsdfError(rc, res.message)
+    return out, res
+
+
+def mesh_lattice(vertices, voxel_size):
+    """Lattice of build_from_mesh (cuda_rasterizer.cu:1354-1372): returns (min, max)."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    mn = (C.c_int32 * 3)()
+    mx = (C.c_int32 * 3)()
+    err = C.create_string_buffer(256)
+    rc = _lib.load().gbsdf_mesh_lattice(v.ctypes.data, len(v), float(voxel_size), mn, mx, err, len(err))
+    if rc != _lib.OK:
+        raise GbsdfError(rc, err.value.decode())
+    return np.array(list(mn), np.int32), np.array(list(mx), np.int32)
+
+
+def build_from_mesh(vertices, indices, voxel_size, mode=MODE_REFERENCE, path=PATH_AUTO, device=0, out=None,
+                    raise_on_error=True):
+    """Indexed mesh -> SDF on the build_from_mesh lattice. Returns (out, min, max, Result)."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    idx = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+    mn, mx = mesh_lattice(v, voxel_size)
+    N = int(np.prod(mx.astype(np.int64) - mn + 1))
+    if out is None:
+        out = np.empty(N, np.float32)
+    op, odev = _ptr_of(out)
+    L = _lib.load()
+    o = _lib.Options()
+    L.gbsdf_default_options(C.byref(o))
+    o.mode, o.path, o.device = int(mode), int(path), int(device)
+    st = _lib.Stats()
+    err = C.create_string_buffer(512)
+    rc = L.gbsdf_build_from_mesh(v.ctypes.data, len(v), idx.ctypes.data, len(idx), float(voxel_size), _i3(mn),
+                                 _i3(mx), op, int(odev), C.byref(o), C.byref(st), err, len(err))
+    res = Result(rc, st.as_dict(), err.value.decode(errors="replace"))
+    if rc != _lib.OK and raise_on_error:
+        raise GbsdfError(rc, res.message)
+    return out, mn, mx, res
+
+
+@dataclass
+class CudaVolumeGrid:
+    """cuda_types.hpp:155-175: dense grid, x fastest, value at lattice point (min+i) h."""
+    data: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    min_coord: np.ndarray = field(default_factory=lambda: np.zeros(3, np.int32))
+    max_coord: np.ndarray = field(default_factory=lambda: np.zeros(3, np.int32))
+    dims: np.ndarray = field(default_factory=lambda: np.zeros(3, np.int32))
+    voxel_size: float = 0.5
+    version: int = 1
+
+    def is_valid(self) -> bool:
+        return self.data.size > 0 and bool((self.dims > 0).all())
+
+
+class CudaRasterizer:
+    """Static entry points with the reference's names, argument meaning and
+    error behaviour (bool / None on failure, output untouched)."""
+
+    _next_version = 2
+
+    @staticmethod
+    def compute_mesh_sdf(triangles, voxel_size, min_coord, max_coord, out_distances: list | None = None):
+        """Returns (ok, out_distances ndarray, out_time_ms). On failure returns
+        (False, out_distances unchanged, time)."""
+        mn = np.asarray(min_coord, np.int64)
+        mx = np.asarray(max_coord, np.int64)
+        dims = mx - mn + 1
+        if (dims <= 0).any():
+            return False, out_distances, 0.0
+        N = int(np.prod(dims))
+        buf = np.full(N, 1e6, np.float32)  # cuda_rasterizer.cu:1180
+        _, res = compute_mesh_sdf(triangles, voxel_size, mn, mx, out=buf, raise_on_error=False)
+        if not res.ok:
+            return False, out_distances, res.stats.get("ms_total", 0.0)
+        return True, buf, res.stats["ms_total"]
+
+    @staticmethod
+    def build_from_mesh(vertices, indices, voxel_size):
+        """Returns (CudaVolumeGrid | None, out_time_ms)."""
+        if len(vertices) == 0 or len(indices) == 0:
+            return None, 0.0
+        out, mn, mx, res = build_from_mesh(vertices, indices, voxel_size, raise_on_error=False)
+        if not res.ok:
+            return None, res.stats.get("ms_total", 0.0)
+        CudaRasterizer._next_version += 1
+        g = CudaVolumeGrid(out, mn, mx, (mx - mn + 1).astype(np.int32), float(voxel_size), CudaRasterizer._next_version)
+        return g, res.stats["ms_total"]

@@ -1,0 +1,180 @@
+"""GPU parity: the CUDA engine through its C ABI against the CPU oracle.
+
+Tolerances (the benchmark spec): signs bit-exact; band distances (|d| <= 8h) within 1e-5
+voxel; far field within 1e-4 voxel. In reference mode the engine and the oracle run
+the same arithmetic in the same (lockstep) schedule, so the grids are expected to be
+bit-identical; the tests assert the tolerances and report the bit-exact fraction.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+BAND_TOL = 1e-5  # voxel
+FAR_TOL = 1e-4   # voxel
+
+
+def compare(got, ref, h, what=""):
+    got = np.asarray(got, np.float32)
+    ref = np.asarray(ref, np.float32)
+    assert got.shape == ref.shape
+    nz = ref != 0
+    sign_mismatch = int(np.count_nonzero(np.signbit(got[nz]) != np.signbit(ref[nz])))
+    assert sign_mismatch == 0, f"{what}: {sign_mismatch} sign mismatches"
+    err = np.abs(got.astype(np.float64) - ref.astype(np.float64)) / h
+    band = np.abs(ref) <= 8 * h
+    assert err[band].max(initial=0) <= BAND_TOL, f"{what}: band error {err[band].max()} voxel"
+    assert err[~band].max(initial=0) <= FAR_TOL, f"{what}: far error {err[~band].max()} voxel"
+    return float(np.mean(got.view(np.uint32) == ref.view(np.uint32)))
+
+
+def small_mug(dims=(48, 48, 52), h=2.0, seg=96):
+    from gbsdf import meshgen
+
+    v, f = meshgen.mug(segments=seg, n_bottom=4, n_wall=8, n_rim=2, handle_path=20, handle_around=16)
+    vf, mn, mx = meshgen.fit_to_lattice(v, dims, h)
+    return meshgen.to_triangles(vf, f), mn, mx, h
+
+
+def test_fast_reference_mode_mug(engine, oracle):
+    tris, mn, mx, h = small_mug()
+    out, res = engine.compute_mesh_sdf(tris, h, mn, mx, mode=engine.MODE_REFERENCE, path=engine.PATH_FAST)
+    st, ref, _, ost = oracle.fast_sdf(tris, h, mn, mx, fsm_mode=0, gwn_mode=1)
+    assert st == oracle.OK and res.ok
+    exact = compare(out, ref, h, "mug")
+    assert res.stats["eikonal_rounds"] == ost["eikonal_rounds"]
+    assert res.stats["band_voxels"] == ost["band_voxels"]
+    assert res.stats["unknown_columns"] == ost["unknown_columns"]
+    assert exact == 1.0, f"bit-exact fraction {exact}"
+
+
+def test_fast_reference_mode_mug_c1_shape(engine, oracle):
+    from gbsdf import meshgen
+
+    tris, mn, mx, h = meshgen.workload("mug_c1_128", dims=(64, 64, 64), h=1.6)
+    out, res = engine.compute_mesh_sdf(tris, h, mn, mx, mode=engine.MODE_REFERENCE, path=engine.PATH_FAST)
+    st, ref, _, ost = oracle.fast_sdf(tris, h, mn, mx, fsm_mode=0, gwn_mode=1)
+    assert st == oracle.OK and res.ok
+    compare(out, ref, h, "mug64")
+    for k in ("probes", "sites", "patch_rounds", "patched_voxels"):
+        assert res.stats[k] == ost[k], (k, res.stats[k], ost[k])
+
+
+def test_fast_defective_vessel_matches_status_and_grid(engine, oracle):
+    from gbsdf import meshgen
+
+    v, f = meshgen.vessel_tree(seed=7, levels=3, around=16, n_len=8, n_cap=2, hole_frac=0.01, n_jitter=20,
+                               dup_frac=0.01)
+    vf, mn, mx = meshgen.fit_to_lattice(v, (56, 56, 56), 1.0)
+    tris = meshgen.to_triangles(vf, f)
+    buf = np.full(int(np.prod(mx.astype(np.int64) - mn + 1)), 7.0, np.float32)
+    out, res = engine.compute_mesh_sdf(tris, 1.0, mn, mx, out=buf, mode=engine.MODE_REFERENCE,
+                                       path=engine.PATH_FAST, raise_on_error=False)
+    st, ref, _, ost = oracle.fast_sdf(tris, 1.0, mn, mx, fsm_mode=0, gwn_mode=1)
+    assert res.status == st, (res.status, st, res.message)
+    assert res.stats["unknown_columns"] == ost["unknown_columns"] > 0
+    if st == oracle.OK:
+        compare(out, ref, 1.0, "vessel")
+    else:
+        assert np.all(buf == 7.0), "output must stay untouched on failure"
+
+
+def test_legacy_path_matches_oracle(engine, oracle):
+    tris, mn, mx, h = small_mug(dims=(24, 24, 26), h=4.0, seg=48)
+    out, res = engine.compute_mesh_sdf(tris, h, mn, mx, path=engine.PATH_LEGACY)
+    ref = oracle.legacy_sdf(tris, h, mn, mx, gwn_mode=1)
+    assert res.ok and res.stats["path_taken"] == engine.PATH_LEGACY
+    compare(out, ref, h, "legacy")
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+
+
+def test_auto_path_dispatch_below_gate_is_legacy(engine):
+    tris, mn, mx, h = small_mug(dims=(24, 24, 26), h=4.0, seg=48)
+    _, res = engine.compute_mesh_sdf(tris, h, mn, mx, path=engine.PATH_AUTO)
+    assert res.stats["path_taken"] == engine.PATH_LEGACY  # 32M-voxel gate, cuda_rasterizer.cu:1189
+
+
+def test_build_from_mesh_matches_oracle_front_end(engine, oracle):
+    from gbsdf import meshgen
+
+    v, f = meshgen.mug(segments=48, n_bottom=3, n_wall=6, n_rim=1, handle_path=12, handle_around=10)
+    v = (v * 0.5).astype(np.float32)
+    f = np.vstack([f, [[0, 0, 1]], [[len(v) + 5, 0, 1]]])  # one degenerate and one out-of-range face
+    h = 2.0
+    out, mn, mx, res = engine.build_from_mesh(v, f.astype(np.uint32), h, path=engine.PATH_FAST)
+    omn, omx = oracle.lattice(v, h)
+    assert list(mn) == list(omn) and list(mx) == list(omx)
+    tris = oracle.build_triangles(v, f.astype(np.uint32))
+    assert len(tris) == len(f) - 2
+    st, ref, _, _ = oracle.fast_sdf(tris, h, mn, mx, fsm_mode=0, gwn_mode=1)
+    assert st == oracle.OK and res.ok
+    compare(out, ref, h, "build_from_mesh")
+
+
+def test_exact_mode_against_fp64_fixed_point(engine, oracle):
+    import ctypes as C
+
+    tris, mn, mx, h = small_mug()
+    dims = (mx.astype(np.int64) - mn + 1).astype(np.int32)
+    out, res = engine.compute_mesh_sdf(tris, h, mn, mx, mode=engine.MODE_EXACT, path=engine.PATH_FAST)
+    band, _ = oracle.splat_band(tris, h, mn, dims)
+    ref64 = np.empty(band.size, np.float64)
+    L = oracle.lib()
+    L.orc_eikonal_exact_f64.restype = C.c_int
+    L.orc_eikonal_exact_f64(band.ctypes.data_as(C.c_void_p), dims.ctypes.data_as(C.c_void_p), C.c_double(h),
+                            ref64.ctypes.data_as(C.c_void_p), C.c_int(100000), C.c_int(oracle.default_threads()))
+    st, refr, sign, _ = oracle.fast_sdf(tris, h, mn, mx, fsm_mode=0, gwn_mode=1)
+    signed64 = np.where(np.signbit(refr), -ref64, ref64)
+    err = np.abs(np.abs(out.astype(np.float64)) - ref64) / h
+    assert err.max() <= FAR_TOL, err.max()
+    assert np.array_equal(np.signbit(out[refr != 0]), np.signbit(signed64[refr != 0]))
+
+
+def test_invalid_inputs_fail_loudly_and_leave_output(engine):
+    tris, mn, mx, h = small_mug(dims=(16, 16, 16), h=6.0, seg=24)
+    n = int(np.prod(mx.astype(np.int64) - mn + 1))
+    buf = np.full(n, 3.0, np.float32)
+    bad = tris.copy()
+    bad[3, 4] = np.nan
+    _, res = engine.compute_mesh_sdf(bad, h, mn, mx, out=buf, path=engine.PATH_FAST, raise_on_error=False)
+    assert res.status == 1 and np.all(buf == 3.0)
+    _, res = engine.compute_mesh_sdf(tris[:0], h, mn, mx, out=buf, raise_on_error=False)
+    assert res.status == 1
+    _, res = engine.compute_mesh_sdf(tris, h, mx, mn, out=buf, raise_on_error=False)
+    assert res.status == 1 and np.all(buf == 3.0)
+
+
+def test_mesh_outside_grid_clamp_semantics(engine, oracle):
+    # empty band: every voxel stays unreached and is clamped (cuda_rasterizer.cu:1052-1063)
+    tris, mn, mx, h = small_mug(dims=(16, 16, 16), h=6.0, seg=24)
+    tris = tris.copy()
+    tris[:, :9] += 5000.0
+    out, res = engine.compute_mesh_sdf(tris, h, mn, mx, path=engine.PATH_FAST, raise_on_error=False)
+    st, ref, _, ost = oracle.fast_sdf(tris, h, mn, mx, fsm_mode=0, gwn_mode=1)
+    assert res.status == st
+    if st == 0:
+        assert np.array_equal(out, ref)
+        assert res.stats["safe_clamped"] == ost["safe_clamped"] == out.size
+
+
+def test_device_output_and_determinism(engine):
+    import torch
+
+    tris, mn, mx, h = small_mug()
+    n = int(np.prod(mx.astype(np.int64) - mn + 1))
+    a = torch.empty(n, dtype=torch.float32, device="cuda")
+    b = torch.empty(n, dtype=torch.float32, device="cuda")
+    engine.compute_mesh_sdf(tris, h, mn, mx, out=a, path=engine.PATH_FAST)
+    engine.compute_mesh_sdf(torch.from_numpy(tris).cuda(), h, mn, mx, out=b, path=engine.PATH_FAST)
+    torch.cuda.synchronize()
+    assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+    host, _ = engine.compute_mesh_sdf(tris, h, mn, mx, path=engine.PATH_FAST)
+    assert np.array_equal(host, a.cpu().numpy())
+
+
+def test_cuda_rasterizer_mirror(engine):
+    tris, mn, mx, h = small_mug(dims=(24, 24, 26), h=4.0, seg=48)
+    ok, out, ms = engine.CudaRasterizer.compute_mesh_sdf(tris, h, mn, mx)
+    assert ok and out.size == int(np.prod(mx.astype(np.int64) - mn + 1)) and ms > 0
+    ok, out2, _ = engine.CudaRasterizer.compute_mesh_sdf(tris, h, mx, mn)
+    assert not ok and out2 is None
