@@ -140,6 +140,11 @@ int gbsdf_build_from_mesh(const float* verts, int64_t n_verts, const uint32_t* i
  * across calls on the same device). */
 void gbsdf_release_workspace(int32_t device);
 
+/* Engine self-tests (no counterpart in the reference). which = 0: the correctly rounded
+ * division by 3 used by the eikonal update is compared with the IEEE quotient for every
+ * non-NaN float input; *result = number of mismatches (0 expected). */
+int gbsdf_selftest(int32_t which, int32_t device, uint64_t* result, char* err, size_t errlen);
+
 /* Library version string. */
 const char* gbsdf_version(void);
 

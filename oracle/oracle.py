@@ -172,11 +172,13 @@ def parity_signs(tris, h, mn, dims, threads=None):
     return sign, n
 
 
-def fixup_unknown(tris, h, mn, dims, sign, gwn_mode=1, threads=None):
-    """[C]: exact winding for sign==2 voxels (RAST:374-400). In place; returns count."""
+def fixup_unknown(tris, h, mn, dims, sign, dist=None, gwn_mode=1, threads=None):
+    """[C]: exact winding for sign==2 voxels (RAST:374-400). In place; returns count.
+    ``dist``: the band field (on-surface voxels, |d| <= 1e-5 voxel, count as inside)."""
     t, T = _tris(tris)
     rech = C.c_longlong(0)
-    n = lib().orc_fixup_unknown(_p(t), C.c_int(T), C.c_float(h), _p(_ivec(mn)), _p(_ivec(dims)), _p(sign),
+    dp = _p(np.ascontiguousarray(dist, np.float32)) if dist is not None else None
+    n = lib().orc_fixup_unknown(_p(t), C.c_int(T), C.c_float(h), _p(_ivec(mn)), _p(_ivec(dims)), _p(sign), dp,
                                 C.c_int(gwn_mode), C.c_int(threads or default_threads()), C.byref(rech))
     return n
 

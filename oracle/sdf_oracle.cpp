@@ -173,26 +173,43 @@ static double solid_angle_d(V3 pf, V3 v0, V3 v1, V3 v2) {
 
 // Winding-number sign of one lattice point.
 //   mode 0: reference, FP32 naive sum in index order (RAST:392-397)
-//   mode 1: exact decision — FP32 Kahan sum, FP64 re-evaluation near the 0.5 threshold
+//   mode 1: exact decision. A point whose band distance is <= 1e-5 voxel lies on the
+//           surface, where the winding number is 0.5 in exact arithmetic: inside
+//           (|w| >= 0.5). Otherwise an FP32 compensated sum decides, unless |w| is
+//           within 0.05 of 0.5 or some triangle's term has an uncertain sign (the point
+//           nearly coplanar with it and projecting inside it); then FP64 decides.
 struct GwnCounters {
     std::atomic<long long> fp64_rechecks{0};
 };
-static bool gwn_inside(const OTri* tris, int T, V3 p, int mode, GwnCounters* ctr) {
+constexpr float kSurfaceTolVoxels = 1e-5f;
+constexpr float kCoplanarRel = 1e-4f;
+static bool gwn_inside(const OTri* tris, int T, V3 p, int mode, GwnCounters* ctr, float dvox, float h) {
     if (mode == 0) {
         float s = 0.0f;
         for (int t = 0; t < T; ++t) s += solid_angle_f(p, tris[t].v0, tris[t].v1, tris[t].v2);
         float w = s * kInv4Pi;
         return std::fabs(w) >= 0.5f;
     }
+    if (dvox <= kSurfaceTolVoxels * h) return true;
     float s = 0.0f, comp = 0.0f;
+    bool amb = false;
     for (int t = 0; t < T; ++t) {
-        float y = solid_angle_f(p, tris[t].v0, tris[t].v1, tris[t].v2) - comp;
+        V3 a = sub(tris[t].v0, p), b = sub(tris[t].v1, p), c = sub(tris[t].v2, p);
+        float la = std::sqrt(dot(a, a)), lb = std::sqrt(dot(b, b)), lc = std::sqrt(dot(c, c));
+        float om = 0.0f;
+        if (!(la <= 1e-6f || lb <= 1e-6f || lc <= 1e-6f)) {
+            float det = a.x * (b.y * c.z - b.z * c.y) - a.y * (b.x * c.z - b.z * c.x) + a.z * (b.x * c.y - b.y * c.x);
+            float denom = la * lb * lc + dot(a, b) * lc + dot(b, c) * la + dot(c, a) * lb;
+            if (std::fabs(det) < kCoplanarRel * (la * lb * lc) && denom < 0.0f) amb = true;
+            om = 2.0f * std::atan2(det, denom);
+        }
+        float y = om - comp;
         float u = s + y;
         comp = (u - s) - y;
         s = u;
     }
     float w = s * kInv4Pi;
-    if (std::fabs(std::fabs(w) - 0.5f) >= 0.05f) return std::fabs(w) >= 0.5f;
+    if (!amb && std::fabs(std::fabs(w) - 0.5f) >= 0.05f) return std::fabs(w) >= 0.5f;
     if (ctr) ctr->fp64_rechecks.fetch_add(1);
     double sd = 0.0;
     for (int t = 0; t < T; ++t) sd += solid_angle_d(p, tris[t].v0, tris[t].v1, tris[t].v2);
@@ -326,7 +343,7 @@ void orc_gwn_sign_voxels(const void* tris_, int T, float h, const int* mn, const
             long long v = vidx[i];
             int x = (int)(v % dx), y = (int)((v / dx) % dy), z = (int)(v / (dx * dy));
             V3 p{(float)(mn[0] + x) * h, (float)(mn[1] + y) * h, (float)(mn[2] + z) * h};
-            out_inside[i] = gwn_inside(tris, T, p, mode, nullptr) ? 1 : 0;
+            out_inside[i] = gwn_inside(tris, T, p, mode, nullptr, 1e30f, h) ? 1 : 0;
         }
     });
 }
@@ -498,7 +515,7 @@ long long orc_parity_signs(const void* tris_, int T, float h, const int* mn, con
 
 // ---- [C] exact winding fixup (RAST:374-400): every sign==2 voxel -----------------------
 long long orc_fixup_unknown(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
-                            int gwn_mode, int threads, long long* fp64_rechecks) {
+                            const float* dist, int gwn_mode, int threads, long long* fp64_rechecks) {
     const OTri* tris = static_cast<const OTri*>(tris_);
     const long long dx = dims[0], dy = dims[1], dz = dims[2];
     const long long N = dx * dy * dz;
@@ -511,7 +528,7 @@ long long orc_fixup_unknown(const void* tris_, int T, float h, const int* mn, co
             long long i = todo[(size_t)k];
             int x = (int)(i % dx), y = (int)((i / dx) % dy), z = (int)(i / (dx * dy));
             V3 p{(float)(mn[0] + x) * h, (float)(mn[1] + y) * h, (float)(mn[2] + z) * h};
-            sign[i] = gwn_inside(tris, T, p, gwn_mode, &ctr) ? 1 : 0;
+            sign[i] = gwn_inside(tris, T, p, gwn_mode, &ctr, dist ? dist[i] : 1e30f, h) ? 1 : 0;
         }
     });
     if (fp64_rechecks) *fp64_rechecks += ctr.fp64_rechecks.load();
@@ -701,8 +718,8 @@ float orc_godunov_exact(float ax, float ay, float az, float h) { return godunov_
 
 // ---- [E] stratified verify + patch (RAST:566-646, RAST:1078-1132) --------------------
 // Returns 1 when a probe came back clean, 0 on systematic divergence.
-int orc_verify_patch(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign, int gwn_mode,
-                     int threads, orc_fast_stats* st) {
+int orc_verify_patch(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
+                     const float* dist, int gwn_mode, int threads, orc_fast_stats* st) {
     const OTri* tris = static_cast<const OTri*>(tris_);
     const long long dx = dims[0], dy = dims[1], dz = dims[2];
     const size_t N = (size_t)(dx * dy * dz);
@@ -723,7 +740,7 @@ int orc_verify_patch(const void* tris_, int T, float h, const int* mn, const int
                 if (s == 2) continue;
                 int x = (int)(v % dx), y = (int)((v / dx) % dy), z = (int)(v / (dx * dy));
                 V3 p{(float)(mn[0] + x) * h, (float)(mn[1] + y) * h, (float)(mn[2] + z) * h};
-                bool inside = gwn_inside(tris, T, p, gwn_mode, &ctr);
+                bool inside = gwn_inside(tris, T, p, gwn_mode, &ctr, dist ? dist[v] : 1e30f, h);
                 if ((s == 1) != inside) ok[(size_t)i] = 0;
             }
         });
@@ -747,7 +764,8 @@ int orc_verify_patch(const void* tris_, int T, float h, const int* mn, const int
                 for (int y = y0; y <= y1; ++y)
                     for (int x = x0; x <= x1; ++x) sign[(size_t)z * dx * dy + (size_t)y * dx + x] = 2;
         }
-        long long fixed = orc_fixup_unknown(tris_, T, h, mn, dims, sign, gwn_mode, threads, &st->fp64_rechecks);
+        long long fixed =
+            orc_fixup_unknown(tris_, T, h, mn, dims, sign, dist, gwn_mode, threads, &st->fp64_rechecks);
         st->patched_voxels += fixed;
         st->sites += m;
         st->patch_rounds += 1;
@@ -792,13 +810,14 @@ int orc_fast_sdf(const void* tris_, int T, float h, const int* mn, const int* mx
     st->unknown_columns = (int)unk;
     if (unk > 0)
         st->fixup_voxels =
-            orc_fixup_unknown(tris_, T, h, mn, dims, out_sign, prm->gwn_mode, threads, &st->fp64_rechecks);
+            orc_fixup_unknown(tris_, T, h, mn, dims, out_sign, g.data(), prm->gwn_mode, threads, &st->fp64_rechecks);
     auto td = clk::now();
     st->eikonal_rounds = orc_eikonal(g.data(), out_sign, dims, h, prm->fsm_mode,
                                      prm->max_conv_rounds > 0 ? prm->max_conv_rounds : 100000, threads,
                                      &st->extra_rounds, &st->far_residual, &st->safe_clamped);
     auto te = clk::now();
-    int ok = prm->skip_verify ? 1 : orc_verify_patch(tris_, T, h, mn, dims, out_sign, prm->gwn_mode, threads, st);
+    int ok = prm->skip_verify ? 1
+                              : orc_verify_patch(tris_, T, h, mn, dims, out_sign, g.data(), prm->gwn_mode, threads, st);
     auto tf = clk::now();
     st->ms_splat = ms(ta, tb);
     st->ms_parity = ms(tb, tc);
@@ -861,7 +880,7 @@ void orc_legacy_sdf(const void* tris_, int T, float h, const int* mn, const int*
                     if (d2 < mind) mind = d2;
                 }
             }
-            bool inside = gwn_inside(tris, T, p, gwn_mode, nullptr);
+            bool inside = gwn_inside(tris, T, p, gwn_mode, nullptr, std::sqrt(mind), h);
             float sgn = inside ? -1.0f : 1.0f;
             out[i] = sgn * std::sqrt(mind);
         }

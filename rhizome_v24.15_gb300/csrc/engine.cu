@@ -180,10 +180,10 @@ int fixup_unknown(Workspace& w, const Lattice& L, long long T, Err& e) {
         if (n <= 0) return GBSDF_OK;
         if (n < 64 * 1024)
             launch_gwn_small(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, P<uint32_t>(w.S),
-                             P<long long>(w.recheck), kListCap, w.ds, n, st);
+                             P<long long>(w.recheck), kListCap, P<float>(w.A), 0, w.ds, n, st);
         else
             launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 0, P<uint32_t>(w.S),
-                       P<long long>(w.recheck), kListCap, w.ds, w.num_sms, st);
+                       P<long long>(w.recheck), kListCap, P<float>(w.A), 0, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
         GB_CK(cudaGetLastError());
@@ -303,7 +303,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     for (int gen = 0; gen < kProbeGens; ++gen) {
         launch_verify_prepare(L, gen, P<uint32_t>(w.U), P<long long>(w.list), w.ds, st);
         launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnVerify, 0, P<uint32_t>(w.S),
-                   P<long long>(w.recheck), kListCap, w.ds, w.num_sms, st);
+                   P<long long>(w.recheck), kListCap, P<float>(w.A), 0, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnVerify, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
         launch_verify_plan(gen, w.ds, st);
@@ -311,7 +311,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         launch_patch_mark(L, P<uint32_t>(w.U), w.ds, st);
         launch_list_unknown(P<uint32_t>(w.U), P<uint32_t>(w.S), L, P<long long>(w.list), kListCap, w.ds, 1, st);
         launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 1, P<uint32_t>(w.S),
-                   P<long long>(w.recheck), kListCap, w.ds, w.num_sms, st);
+                   P<long long>(w.recheck), kListCap, P<float>(w.A), 0, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
     }
@@ -396,7 +396,7 @@ int run_legacy(Workspace& w, long long T, const Lattice& L, float* out, bool out
         GB_CK(cudaMemcpyAsync(&w.ds->listed, &nn, sizeof(nn), cudaMemcpyHostToDevice, st));
         GB_CK(cudaMemsetAsync(&w.ds->recheck_n, 0, sizeof(unsigned long long), st));
         launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 0, P<uint32_t>(w.S),
-                   P<long long>(w.recheck), kListCap, w.ds, w.num_sms, st);
+                   P<long long>(w.recheck), kListCap, P<float>(w.A), 1, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
         GB_CK(cudaStreamSynchronize(st));  // `nn` lives on the host stack
@@ -609,6 +609,32 @@ void gbsdf_release_workspace(int32_t device) {
     std::lock_guard<std::mutex> g(g_ws_mu);
     std::lock_guard<std::mutex> lk(g_ws[device].mu);
     free_ws(g_ws[device]);
+}
+
+int gbsdf_selftest(int32_t which, int32_t device, uint64_t* result, char* err, size_t errlen) {
+    Err e{err, errlen};
+    if (err && errlen) err[0] = 0;
+    if (!result) return e.set(GBSDF_EINVAL, "null result");
+    if (which != 0) return e.set(GBSDF_EINVAL, "unknown self-test %d", which);
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) {
+        cudaGetLastError();
+        return e.set(GBSDF_ENODEV, "no CUDA device %d", device);
+    }
+    GB_CK(cudaSetDevice(device));
+    unsigned long long* d = nullptr;
+    GB_CK(cudaMalloc(&d, sizeof(unsigned long long)));
+    cudaError_t rc = cudaMemset(d, 0, sizeof(unsigned long long));
+    if (rc == cudaSuccess) {
+        launch_selftest_div3(d, 0);
+        rc = cudaGetLastError();
+    }
+    unsigned long long h = 0;
+    if (rc == cudaSuccess) rc = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (rc != cudaSuccess) return e.set(GBSDF_ECUDA, "self-test: %s", cudaGetErrorString(rc));
+    *result = h;
+    return GBSDF_OK;
 }
 
 const char* gbsdf_version(void) { return "gbsdf 0.1 (sm_103a)"; }

@@ -30,6 +30,12 @@ constexpr float kJX = 0.037f;
 constexpr float kJY = 0.051f;
 constexpr float kInv4Pi = 0.07957747154594767f;
 constexpr float kRecheckBand = 0.05f;  // FP64 re-evaluation when | |w| - 0.5 | < this
+// A voxel within this many voxels of the surface lies on it: its winding number is 0.5 in
+// exact arithmetic (inside by |w| >= 0.5), while any floating-point sum of it is noise.
+constexpr float kSurfaceTolVoxels = 1e-5f;
+// A triangle term's sign is uncertain when |det| < this * |a||b||c| and the point
+// projects inside the triangle (denominator < 0): such voxels are decided in FP64.
+constexpr float kCoplanarRel = 1e-4f;
 constexpr unsigned long long kFastMinVoxels = 32ull * 1024ull * 1024ull;
 
 // Brick edge of the band splat and lattice strip width of the parity pass.
@@ -86,7 +92,7 @@ __device__ __forceinline__ float ptd_sq(f3 p, f3 a, f3 b, f3 c) {
 // (math_utils.cuh:109-132), FP32 with explicit FMAs: the winding sum's sign is
 // decided exactly by re-evaluating in FP64 near the threshold, so this form is
 // free to be fast.
-__device__ __forceinline__ float solid_angle_fast(f3 p, f3 v0, f3 v1, f3 v2) {
+__device__ __forceinline__ float solid_angle_fast(f3 p, f3 v0, f3 v1, f3 v2, bool& amb) {
     float ax = v0.x - p.x, ay = v0.y - p.y, az = v0.z - p.z;
     float bx = v1.x - p.x, by = v1.y - p.y, bz = v1.z - p.z;
     float cx = v2.x - p.x, cy = v2.y - p.y, cz = v2.z - p.z;
@@ -99,7 +105,9 @@ __device__ __forceinline__ float solid_angle_fast(f3 p, f3 v0, f3 v1, f3 v2) {
     float ab = __fmaf_rn(az, bz, __fmaf_rn(ay, by, ax * bx));
     float bc = __fmaf_rn(bz, cz, __fmaf_rn(by, cy, bx * cx));
     float ca = __fmaf_rn(cz, az, __fmaf_rn(cy, ay, cx * ax));
-    float denom = __fmaf_rn(ca, lb, __fmaf_rn(bc, la, __fmaf_rn(ab, lc, la * lb * lc)));
+    float labc = la * lb * lc;
+    float denom = __fmaf_rn(ca, lb, __fmaf_rn(bc, la, __fmaf_rn(ab, lc, labc)));
+    amb |= (fabsf(det) < kCoplanarRel * labc) && (denom < 0.0f);
     return 2.0f * atan2f(det, denom);
 }
 
@@ -119,8 +127,21 @@ __device__ __forceinline__ double solid_angle_f64(f3 pf, f3 v0, f3 v1, f3 v2) {
     return 2.0 * atan2(det, denom);
 }
 
+// x / 3, correctly rounded, without a general division: q = RN(x * RN(1/3)), the exact
+// remainder r = x - 3q by one FMA, then RN(q + r * RN(1/3)) (Markstein's correction
+// step for division by a constant, IEEE Trans. Computers 1990). The engine checks it
+// against the IEEE quotient x / 3.0f for every float input (gbsdf_selftest).
+__device__ __forceinline__ float div3_rn(float x) {
+    const float r3 = 0.333333343267440796f;  // RN(1/3) = 0x3EAAAAAB
+    float q = x * r3;
+    float r = __fmaf_rn(-3.0f, q, x);
+    // r == 0: q is exact (keeps the sign of -0); q infinite: the quotient is q.
+    return (r == 0.0f || !(fabsf(q) < __int_as_float(0x7f800000))) ? q : __fmaf_rn(r, r3, q);
+}
+
 // The reference's Godunov update, rhi_eikonal_godunov (cuda_rasterizer.cu:405-425),
-// operation for operation (including its halved 3D pairwise sum).
+// operation for operation (including its halved 3D pairwise sum); the final division by
+// 3 uses div3_rn, which rounds identically.
 __device__ __forceinline__ float godunov_ref(float ax, float ay, float az, float h) {
     float s0 = fminf(ax, fminf(ay, az));
     float s2 = fmaxf(ax, fmaxf(ay, az));
@@ -133,7 +154,7 @@ __device__ __forceinline__ float godunov_ref(float ax, float ay, float az, float
             if (updated > s2) {
                 float disc3 = 3.0f * h * h -
                               ((s1 - s0) * (s1 - s0) + (s2 - s1) * (s2 - s1) + (s2 - s0) * (s2 - s0)) * 0.5f;
-                if (disc3 >= 0.0f) updated = (s0 + s1 + s2 + sqrtf(disc3)) / 3.0f;
+                if (disc3 >= 0.0f) updated = div3_rn(s0 + s1 + s2 + sqrtf(disc3));
             }
         }
     }
@@ -159,7 +180,7 @@ __device__ __forceinline__ float godunov_exact(float a, float b, float c, float 
             float d2 = s2 - s0;
             float e = s2 - s1;
             float disc3 = 3.0f * h * h - (d1 * d1 + e * e + d2 * d2);
-            float inc3 = (d1 + d2 + sqrtf(fmaxf(disc3, 0.0f))) / 3.0f;
+            float inc3 = div3_rn(d1 + d2 + sqrtf(fmaxf(disc3, 0.0f)));
             u = s0 + inc3;
         }
     }

@@ -102,9 +102,11 @@ void launch_parity(const ParTri* ptt, const unsigned long long* strip_off, const
                    cudaStream_t st);
 void launch_list_unknown(uint32_t* ubits, uint32_t* sbits, const Lattice& L, long long* list, long long cap,
                          DevState* ds, int only_if_patching, cudaStream_t st);
+// `dist`: the voxel distance field (squared when dist_sq): voxels within
+// kSurfaceTolVoxels of the surface are decided inside without a winding sum.
 void launch_gwn(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
                 int consumer, int only_if, uint32_t* sbits, long long* recheck, long long recheck_cap,
-                DevState* ds, int num_sms, cudaStream_t st);
+                const float* dist, int dist_sq, DevState* ds, int num_sms, cudaStream_t st);
 void launch_gwn_recheck(const float* tri9, long long T, const Lattice& L, const long long* recheck,
                         long long recheck_cap, int consumer, uint32_t* sbits, DevState* ds, int num_sms,
                         cudaStream_t st);
@@ -121,8 +123,8 @@ void launch_apply(const float* g, const uint32_t* sbits, const Lattice& L, float
                   cudaStream_t st);
 void launch_pack_tri9(const float* tris12, long long T, float* tri9, cudaStream_t st);
 void launch_gwn_small(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
-                      int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, DevState* ds,
-                      long long n_hint, cudaStream_t st);
+                      int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, const float* dist,
+                      int dist_sq, DevState* ds, long long n_hint, cudaStream_t st);
 void launch_tri_flags(const float* verts, long long nv, const uint32_t* idx, long long nt, unsigned* flags,
                       cudaStream_t st);
 void launch_tri_scatter(const float* verts, long long nv, const uint32_t* idx, long long nt,
@@ -132,5 +134,6 @@ void launch_legacy_dist(const float* t9, long long T, const float* hb, const Lat
                         cudaStream_t st);
 void launch_legacy_combine(const float* d2, const uint32_t* sbits, const Lattice& L, float* out, cudaStream_t st);
 void launch_iota(long long* list, long long n, long long from, cudaStream_t st);
+void launch_selftest_div3(unsigned long long* mism, cudaStream_t st);
 
 }  // namespace gbsdf

@@ -100,8 +100,10 @@ __global__ void __launch_bounds__(kGwnThreads) gwn_kernel(const float* __restric
                                                           const long long* __restrict__ list, long long cap,
                                                           int consumer, int only_if, uint32_t* __restrict__ sbits,
                                                           long long* __restrict__ recheck, long long recheck_cap,
+                                                          const float* __restrict__ dist, int dist_sq,
                                                           DevState* ds) {
     if (only_if && !ds->patching) return;
+    const float tau = kSurfaceTolVoxels * L.h;
     constexpr int VPB = kGwnThreads / TEAM;
     __shared__ float s_tri[kGwnChunk * 9];
     const long long n = min((long long)ds->listed, cap);
@@ -116,8 +118,16 @@ __global__ void __launch_bounds__(kGwnThreads) gwn_kernel(const float* __restric
             int x, y, z;
             voxel_coords(L, v, x, y, z);
             p = lattice_point(L.mn[0], L.mn[1], L.mn[2], x, y, z, L.h);
+            if (dist) {
+                const float d = dist[v];
+                if (dist_sq ? (d <= tau * tau) : (d <= tau)) {  // on the surface: inside
+                    if (member == 0) consume(L, v, true, consumer, sbits, ds);
+                    v = -2;
+                }
+            }
         }
         float s = 0.0f, c = 0.0f;
+        bool amb = false;
         for (long long c0 = 0; c0 < T; c0 += kGwnChunk) {
             int m = (int)min((long long)kGwnChunk, T - c0);
             __syncthreads();
@@ -127,7 +137,7 @@ __global__ void __launch_bounds__(kGwnThreads) gwn_kernel(const float* __restric
                 for (int i = member; i < m; i += TEAM) {
                     const float* t = s_tri + i * 9;
                     kahan_add(s, c, solid_angle_fast(p, mk(t[0], t[1], t[2]), mk(t[3], t[4], t[5]),
-                                                     mk(t[6], t[7], t[8])));
+                                                     mk(t[6], t[7], t[8]), amb));
                 }
             }
         }
@@ -138,12 +148,13 @@ __global__ void __launch_bounds__(kGwnThreads) gwn_kernel(const float* __restric
             for (int o = TEAM / 2; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o, TEAM);
             s = tot;
             c = 0.0f;
+            amb = __any_sync(0xffffffffu, amb);
         }
         if (v >= 0 && member == 0) {
             pairs += (unsigned long long)T;
             float w = (s - c) * kInv4Pi;
             float aw = fabsf(w);
-            if (fabsf(aw - 0.5f) < kRecheckBand) {
+            if (amb || fabsf(aw - 0.5f) < kRecheckBand) {
                 unsigned long long r = atomicAdd(&ds->recheck_n, 1ull);
                 if ((long long)r < recheck_cap) recheck[r] = v;
             } else {
@@ -271,28 +282,28 @@ void launch_list_unknown(uint32_t* ubits, uint32_t* sbits, const Lattice& L, lon
 
 void launch_gwn(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
                 int consumer, int only_if, uint32_t* sbits, long long* recheck, long long recheck_cap,
-                DevState* ds, int num_sms, cudaStream_t st) {
+                const float* dist, int dist_sq, DevState* ds, int num_sms, cudaStream_t st) {
     // consumer kGwnVerify lists are short (<= 4096): one voxel per warp.
     if (consumer == kGwnVerify) {
         long long blocks = (kVerifySamples + 7) / 8;
         GBSDF_COUNT_LAUNCH();
         gwn_kernel<32><<<(unsigned)blocks, kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, only_if,
-                                                                 sbits, recheck, recheck_cap, ds);
+                                                                 sbits, recheck, recheck_cap, dist, dist_sq, ds);
     } else {
         long long blocks = (long long)num_sms * 8;
         GBSDF_COUNT_LAUNCH();
         gwn_kernel<1><<<(unsigned)blocks, kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, only_if,
-                                                                sbits, recheck, recheck_cap, ds);
+                                                                sbits, recheck, recheck_cap, dist, dist_sq, ds);
     }
 }
 
 void launch_gwn_small(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
-                      int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, DevState* ds,
-                      long long n_hint, cudaStream_t st) {
+                      int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, const float* dist,
+                      int dist_sq, DevState* ds, long long n_hint, cudaStream_t st) {
     long long blocks = std::max<long long>(1, (n_hint + 7) / 8);
     GBSDF_COUNT_LAUNCH();
     gwn_kernel<32><<<(unsigned)blocks, kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, 0, sbits,
-                                                             recheck, recheck_cap, ds);
+                                                             recheck, recheck_cap, dist, dist_sq, ds);
 }
 
 void launch_gwn_recheck(const float* tri9, long long T, const Lattice& L, const long long* recheck,

@@ -136,6 +136,20 @@ __global__ void legacy_combine_kernel(const float* __restrict__ d2, const uint32
     }
 }
 
+// Self-test: div3_rn against the IEEE quotient x / 3.0f for every non-NaN float.
+__global__ void selftest_div3_kernel(unsigned long long* __restrict__ mism) {
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    unsigned long long bad = 0;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < (1ull << 32);
+         i += stride) {
+        const float x = __uint_as_float((unsigned)i);
+        if (isnan(x)) continue;
+        const float a = div3_rn(x), b = x / 3.0f;
+        bad += (__float_as_uint(a) != __float_as_uint(b)) ? 1ull : 0ull;
+    }
+    if (bad) atomicAdd(mism, bad);
+}
+
 __global__ void iota_kernel(long long* __restrict__ list, long long n, long long from) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) list[i] = from + i;
@@ -179,6 +193,11 @@ void launch_legacy_combine(const float* d2, const uint32_t* sbits, const Lattice
     long long blocks = std::min<long long>((L.N + 255) / 256, 152LL * 32);
     GBSDF_COUNT_LAUNCH();
     legacy_combine_kernel<<<(unsigned)blocks, 256, 0, st>>>(d2, sbits, L, out);
+}
+
+void launch_selftest_div3(unsigned long long* mism, cudaStream_t st) {
+    GBSDF_COUNT_LAUNCH();
+    selftest_div3_kernel<<<152 * 16, 256, 0, st>>>(mism);
 }
 
 void launch_iota(long long* list, long long n, long long from, cudaStream_t st) {

@@ -1,0 +1,18 @@
+"""Engine self-tests on the GPU: the correctly rounded division by 3 of the eikonal
+update equals the IEEE quotient x / 3.0f for all 2^32 - NaN float inputs."""
+import ctypes as C
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_div3_exhaustive(engine):
+    from gbsdf import _lib
+
+    L = _lib.load()
+    res = C.c_uint64(123)
+    err = C.create_string_buffer(256)
+    rc = L.gbsdf_selftest(0, 0, C.byref(res), err, len(err))
+    assert rc == 0, err.value
+    assert res.value == 0, f"{res.value} inputs round differently"
