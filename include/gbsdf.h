@@ -140,6 +140,25 @@ int gbsdf_build_from_mesh(const float* verts, int64_t n_verts, const uint32_t* i
  * across calls on the same device). */
 void gbsdf_release_workspace(int32_t device);
 
+/* The exact (legacy-kernel) SDF of gbsdf_compute_mesh_sdf with GBSDF_PATH_LEGACY, for
+ * callers that cannot allocate device memory: a step running under a device-memory
+ * budget fixed at start-up, a plugin whose host application owns all device allocations,
+ * or a latency-critical loop that cannot afford cudaMalloc's implicit synchronisation.
+ * No counterpart in the reference. It calls no cudaMalloc, cudaFree or allocating library
+ * routine: `tris_dev` (n_tris CudaTriangle records) and `out_dev` (dims.x*dims.y*dims.z
+ * floats) are caller-owned device buffers, and all scratch lives in one fixed array
+ * inside the library (about 12.6 MB per GPU, held from module load until process exit).
+ * Limits: at most 16,777,216 voxels, 1,048,576 sign words (ceil(dims.x/32)*dims.y*dims.z)
+ * and 1,048,576 triangles; larger inputs return GBSDF_EINVAL before any work.
+ * The first call on a device resolves the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture. Every call shares the array, so two
+ * calls whose GPU work overlapped would race; the entry point takes a process-wide lock
+ * and synchronises `stream` (a cudaStream_t, NULL = legacy default stream) before it
+ * returns. */
+int gbsdf_legacy_sdf_noalloc(const gbsdf_tri* tris_dev, int64_t n_tris, float voxel_size,
+                             const int32_t min_coord[3], const int32_t max_coord[3], float* out_dev,
+                             int32_t device, void* stream, gbsdf_stats* stats, char* err, size_t errlen);
+
 /* Engine self-tests (no counterpart in the reference). which = 0: the correctly rounded
  * division by 3 used by the eikonal update is compared with the IEEE quotient for every
  * non-NaN float input; *result = number of mismatches (0 expected). */

@@ -43,7 +43,7 @@ class Stats(C.Structure):
 
 # every exported symbol of include/gbsdf.h
 EXPORTS = ("gbsdf_default_options", "gbsdf_compute_mesh_sdf", "gbsdf_mesh_lattice", "gbsdf_build_from_mesh",
-           "gbsdf_release_workspace", "gbsdf_selftest", "gbsdf_version")
+           "gbsdf_release_workspace", "gbsdf_legacy_sdf_noalloc", "gbsdf_selftest", "gbsdf_version")
 
 _lib = None
 
@@ -71,6 +71,9 @@ def load(path: Path | None = None):
     L.gbsdf_build_from_mesh.restype = C.c_int
     L.gbsdf_release_workspace.argtypes = [C.c_int32]
     L.gbsdf_release_workspace.restype = None
+    L.gbsdf_legacy_sdf_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_float, i32p, i32p, C.c_void_p, C.c_int32,
+                                           C.c_void_p, C.POINTER(Stats), C.c_char_p, C.c_size_t]
+    L.gbsdf_legacy_sdf_noalloc.restype = C.c_int
     L.gbsdf_selftest.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_uint64), C.c_char_p, C.c_size_t]
     L.gbsdf_selftest.restype = C.c_int
     L.gbsdf_version.argtypes = []
