@@ -97,6 +97,23 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def max_over_ranks(dist, x: float) -> float:
+    """Max of a per-rank float over all ranks (identity without a process group)."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gvox(world: int, voxels_per_rank: int, ms_per_step: float) -> float:
+    """Whole-job throughput: every rank builds its own grid (replicas); the job's time
+    is the slowest rank's."""
+    return world * voxels_per_rank / (ms_per_step * 1e-3) / 1e9
+
+
 def make_workload():
     from gbsdf import meshgen
 
@@ -211,12 +228,8 @@ def main():
             stats.append(step_device().stats)
         e1.record()
         barrier()
-    dev_ms = e0.elapsed_time(e1) / args.steps
-    if dist:
-        t = torch.tensor([dev_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms = float(t.item())
-    value = world * N / (dev_ms * 1e-3) / 1e9
+    dev_ms = max_over_ranks(dist, e0.elapsed_time(e1) / args.steps)
+    value = whole_job_gvox(world, N, dev_ms)
 
     # ---- end to end through the public API with pinned host buffers
     tris_pin = torch.from_numpy(tris).pin_memory()
@@ -233,12 +246,8 @@ def main():
         gbsdf.compute_mesh_sdf(tris_np, h, mn, mx, out=out_np, mode=mode, path=gbsdf.PATH_FAST, device=local)
     e3.record()
     barrier()
-    e2e_ms = e2.elapsed_time(e3) / args.steps
-    if dist:
-        t = torch.tensor([e2e_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = world * N / (e2e_ms * 1e-3) / 1e9
+    e2e_ms = max_over_ranks(dist, e2.elapsed_time(e3) / args.steps)
+    e2e = whole_job_gvox(world, N, e2e_ms)
 
     # ---- roofline of the dominant kernel (eikonal sweeps), events on the engine's stream
     s0 = stats[-1]

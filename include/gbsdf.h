@@ -122,6 +122,26 @@ int gbsdf_compute_mesh_sdf(const gbsdf_tri* tris, int64_t n_tris, float voxel_si
                            const int32_t max_coord[3], float* out, int32_t out_on_device,
                            const gbsdf_options* opt, gbsdf_stats* stats, char* err, size_t errlen);
 
+/* One mesh of a batched call. */
+typedef struct gbsdf_mesh_desc {
+    const gbsdf_tri* tris;   /* host or device (opt->tris_on_device) */
+    int64_t n_tris;
+    float voxel_size;
+    int32_t min_coord[3];
+    int32_t max_coord[3];
+    float* out;              /* dims.x*dims.y*dims.z floats, host or device (out_on_device) */
+    int32_t status;          /* written: this mesh's gbsdf_status */
+    int32_t pad;
+} gbsdf_mesh_desc;
+
+/* Batched form of gbsdf_compute_mesh_sdf (the descriptor list of the reference-side
+ * C ABI plan): meshes of uneven size share one device workspace sized for the largest
+ * and run back to back on one stream. Returns GBSDF_OK when every mesh succeeded, else
+ * the first failing mesh's status; per-mesh statuses are written to meshes[i].status and
+ * per-mesh statistics to stats[i] (stats may be NULL). */
+int gbsdf_compute_mesh_sdf_batch(gbsdf_mesh_desc* meshes, int32_t n_meshes, int32_t out_on_device,
+                                 const gbsdf_options* opt, gbsdf_stats* stats, char* err, size_t errlen);
+
 /* Lattice of CudaRasterizer::build_from_mesh (cuda_rasterizer.cu:1354-1372): bounding box
  * of all vertices, padded by 10 voxels, floor/ceil onto the voxel lattice. */
 int gbsdf_mesh_lattice(const float* verts, int64_t n_verts, float voxel_size, int32_t min_coord[3],

@@ -523,6 +523,30 @@ int gbsdf_compute_mesh_sdf(const gbsdf_tri* tris, int64_t n_tris, float voxel_si
                    max_coord, out, out_on_device != 0, o, stats, e);
 }
 
+int gbsdf_compute_mesh_sdf_batch(gbsdf_mesh_desc* meshes, int32_t n_meshes, int32_t out_on_device,
+                                 const gbsdf_options* opt, gbsdf_stats* stats, char* err, size_t errlen) {
+    Err e{err, errlen};
+    if (err && errlen) err[0] = 0;
+    if (!meshes || n_meshes <= 0) return e.set(GBSDF_EINVAL, "empty batch");
+    gbsdf_options o;
+    gbsdf_default_options(&o);
+    if (opt) o = *opt;
+    int first_bad = GBSDF_OK;
+    char one[256];
+    for (int32_t i = 0; i < n_meshes; ++i) {
+        gbsdf_mesh_desc& m = meshes[i];
+        Err ei{one, sizeof(one)};
+        one[0] = 0;
+        m.status = compute(reinterpret_cast<const float*>(m.tris), m.n_tris, o.tris_on_device != 0, m.voxel_size,
+                           m.min_coord, m.max_coord, m.out, out_on_device != 0, o, stats ? &stats[i] : nullptr, ei);
+        if (m.status != GBSDF_OK && first_bad == GBSDF_OK) {
+            first_bad = m.status;
+            e.set(m.status, "mesh %d: %s", i, one);
+        }
+    }
+    return first_bad;
+}
+
 int gbsdf_mesh_lattice(const float* verts, int64_t n_verts, float voxel_size, int32_t min_coord[3],
                        int32_t max_coord[3], char* err, size_t errlen) {
     Err e{err, errlen};

@@ -140,20 +140,21 @@ __device__ __forceinline__ float div3_rn(float x) {
 }
 
 // The reference's Godunov update, rhi_eikonal_godunov (cuda_rasterizer.cu:405-425),
-// operation for operation (including its halved 3D pairwise sum); the final division by
-// 3 uses div3_rn, which rounds identically.
+// operation for operation (including its halved 3D pairwise sum). The final division by
+// 3 uses div3_rn, which rounds identically to the IEEE quotient. The branches are kept:
+// whole warps skip the 2D / 3D work where the 1D update applies.
 __device__ __forceinline__ float godunov_ref(float ax, float ay, float az, float h) {
-    float s0 = fminf(ax, fminf(ay, az));
-    float s2 = fmaxf(ax, fmaxf(ay, az));
-    float s1 = ax + ay + az - s0 - s2;
+    const float s0 = fminf(ax, fminf(ay, az));
+    const float s2 = fmaxf(ax, fmaxf(ay, az));
+    const float s1 = ax + ay + az - s0 - s2;
     float updated = s0 + h;
     if (updated > s1) {
-        float disc = 2.0f * h * h - (s1 - s0) * (s1 - s0);
+        const float disc = 2.0f * h * h - (s1 - s0) * (s1 - s0);
         if (disc >= 0.0f) {
             updated = (s0 + s1 + sqrtf(disc)) * 0.5f;
             if (updated > s2) {
-                float disc3 = 3.0f * h * h -
-                              ((s1 - s0) * (s1 - s0) + (s2 - s1) * (s2 - s1) + (s2 - s0) * (s2 - s0)) * 0.5f;
+                const float disc3 = 3.0f * h * h -
+                                    ((s1 - s0) * (s1 - s0) + (s2 - s1) * (s2 - s1) + (s2 - s0) * (s2 - s0)) * 0.5f;
                 if (disc3 >= 0.0f) updated = div3_rn(s0 + s1 + s2 + sqrtf(disc3));
             }
         }
@@ -165,23 +166,21 @@ __device__ __forceinline__ float godunov_ref(float ax, float ay, float az, float
 // true 3D discriminant 3h^2 - sum_{i<j}(s_i - s_j)^2, increments formed from
 // differences and added to the smallest neighbour once.
 __device__ __forceinline__ float godunov_exact(float a, float b, float c, float h) {
-    float lo = fminf(a, b), hi = fmaxf(a, b);
-    float s0 = fminf(lo, c);
-    float m = fmaxf(lo, c);
-    float s1 = fminf(m, hi);
-    float s2 = fmaxf(m, hi);
+    const float lo = fminf(a, b), hi = fmaxf(a, b);
+    const float s0 = fminf(lo, c);
+    const float m = fmaxf(lo, c);
+    const float s1 = fminf(m, hi);
+    const float s2 = fmaxf(m, hi);
     float u = s0 + h;
     if (u > s1) {
-        float d1 = s1 - s0;
-        float disc = 2.0f * h * h - d1 * d1;
-        float inc = (d1 + sqrtf(fmaxf(disc, 0.0f))) * 0.5f;
-        u = s0 + inc;
+        const float d1 = s1 - s0;
+        const float disc = 2.0f * h * h - d1 * d1;
+        u = s0 + (d1 + sqrtf(fmaxf(disc, 0.0f))) * 0.5f;
         if (u > s2) {
-            float d2 = s2 - s0;
-            float e = s2 - s1;
-            float disc3 = 3.0f * h * h - (d1 * d1 + e * e + d2 * d2);
-            float inc3 = div3_rn(d1 + d2 + sqrtf(fmaxf(disc3, 0.0f)));
-            u = s0 + inc3;
+            const float d2 = s2 - s0;
+            const float e = s2 - s1;
+            const float disc3 = 3.0f * h * h - (d1 * d1 + e * e + d2 * d2);
+            u = s0 + div3_rn(d1 + d2 + sqrtf(fmaxf(disc3, 0.0f)));
         }
     }
     return u;

@@ -265,29 +265,45 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_kernel(const float* __restr
             const float* cs = xring + (ci % kXS) * kXSlot;
             const float* ns = xring + ((ci + 1) % kXS) * kXSlot;  // next chunk in walk order
             float res[kXC];
+            const bool fast = (xc + kXC <= dx) && (ci + 1 < nchunks);
+            if (fast) {
 #pragma unroll
-            for (int jj = 0; jj < kXC; ++jj) {
-                const int j = (dir > 0) ? jj : (kXC - 1 - jj);
-                const int x = xc + j;
-                res[j] = 0.0f;
-                if (x >= dx) continue;
-                const float cur = cs[me * kXStride + j];
-                float down;
-                if (dir > 0) down = (j + 1 < kXC) ? cs[me * kXStride + j + 1]
-                                                 : ((ci + 1 < nchunks) ? ns[me * kXStride] : kFarSentinel);
-                else down = (j > 0) ? cs[me * kXStride + j - 1]
-                                    : ((ci + 1 < nchunks) ? ns[me * kXStride + kXC - 1] : kFarSentinel);
-                const float ax = fminf(prev, down);
-                const float ay = fminf(cs[n_ym * kXStride + j], cs[n_yp * kXStride + j]);
-                const float az = fminf(cs[n_zm * kXStride + j], cs[n_zp * kXStride + j]);
-                const float u = godunov<RULE>(ax, ay, az, h);
-                float out = cur;
-                if (u < cur) {
-                    out = u;
-                    ch = true;
+                for (int jj = 0; jj < kXC; ++jj) {
+                    const int j = (dir > 0) ? jj : (kXC - 1 - jj);
+                    const float cur = cs[me * kXStride + j];
+                    const float down = (dir > 0) ? ((j + 1 < kXC) ? cs[me * kXStride + j + 1] : ns[me * kXStride])
+                                                 : ((j > 0) ? cs[me * kXStride + j - 1] : ns[me * kXStride + kXC - 1]);
+                    const float ax = fminf(prev, down);
+                    const float ay = fminf(cs[n_ym * kXStride + j], cs[n_yp * kXStride + j]);
+                    const float az = fminf(cs[n_zm * kXStride + j], cs[n_zp * kXStride + j]);
+                    const float u = godunov<RULE>(ax, ay, az, h);
+                    const float out = (u < cur) ? u : cur;
+                    ch |= (u < cur);
+                    res[j] = out;
+                    prev = out;
                 }
-                res[j] = out;
-                prev = out;
+            } else {
+#pragma unroll
+                for (int jj = 0; jj < kXC; ++jj) {
+                    const int j = (dir > 0) ? jj : (kXC - 1 - jj);
+                    const int x = xc + j;
+                    res[j] = 0.0f;
+                    if (x >= dx) continue;
+                    const float cur = cs[me * kXStride + j];
+                    float down;
+                    if (dir > 0) down = (j + 1 < kXC) ? cs[me * kXStride + j + 1]
+                                                     : ((ci + 1 < nchunks) ? ns[me * kXStride] : kFarSentinel);
+                    else down = (j > 0) ? cs[me * kXStride + j - 1]
+                                        : ((ci + 1 < nchunks) ? ns[me * kXStride + kXC - 1] : kFarSentinel);
+                    const float ax = fminf(prev, down);
+                    const float ay = fminf(cs[n_ym * kXStride + j], cs[n_yp * kXStride + j]);
+                    const float az = fminf(cs[n_zm * kXStride + j], cs[n_zp * kXStride + j]);
+                    const float u = godunov<RULE>(ax, ay, az, h);
+                    const float out = (u < cur) ? u : cur;
+                    ch |= (u < cur);
+                    res[j] = out;
+                    prev = out;
+                }
             }
             float* drow = dst + (size_t)z * plane + (size_t)y * dx + xc;
             if (((dx & 3) == 0) && xc + kXC <= dx) {

@@ -41,8 +41,15 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "pad0")}
 
 
+class MeshDesc(C.Structure):
+    _fields_ = [("tris", C.c_void_p), ("n_tris", C.c_int64), ("voxel_size", C.c_float),
+                ("min_coord", C.c_int32 * 3), ("max_coord", C.c_int32 * 3), ("out", C.c_void_p),
+                ("status", C.c_int32), ("pad", C.c_int32)]
+
+
 # every exported symbol of include/gbsdf.h
-EXPORTS = ("gbsdf_default_options", "gbsdf_compute_mesh_sdf", "gbsdf_mesh_lattice", "gbsdf_build_from_mesh",
+EXPORTS = ("gbsdf_default_options", "gbsdf_compute_mesh_sdf", "gbsdf_compute_mesh_sdf_batch",
+           "gbsdf_mesh_lattice", "gbsdf_build_from_mesh",
            "gbsdf_release_workspace", "gbsdf_legacy_sdf_noalloc", "gbsdf_selftest", "gbsdf_version")
 
 _lib = None
@@ -63,6 +70,9 @@ def load(path: Path | None = None):
     L.gbsdf_compute_mesh_sdf.argtypes = [C.c_void_p, C.c_int64, C.c_float, i32p, i32p, C.c_void_p, C.c_int32,
                                          C.POINTER(Options), C.POINTER(Stats), C.c_char_p, C.c_size_t]
     L.gbsdf_compute_mesh_sdf.restype = C.c_int
+    L.gbsdf_compute_mesh_sdf_batch.argtypes = [C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.POINTER(Options),
+                                               C.POINTER(Stats), C.c_char_p, C.c_size_t]
+    L.gbsdf_compute_mesh_sdf_batch.restype = C.c_int
     L.gbsdf_mesh_lattice.argtypes = [C.c_void_p, C.c_int64, C.c_float, i32p, i32p, C.c_char_p, C.c_size_t]
     L.gbsdf_mesh_lattice.restype = C.c_int
     L.gbsdf_build_from_mesh.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_float, i32p, i32p,

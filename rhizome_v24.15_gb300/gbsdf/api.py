@@ -23,7 +23,7 @@ import numpy as np
 from . import _lib
 from ._lib import MODE_EXACT, MODE_REFERENCE, PATH_AUTO, PATH_FAST, PATH_LEGACY, STATUS_NAMES
 
-__all__ = ["GbsdfError", "Result", "compute_mesh_sdf", "mesh_lattice", "build_from_mesh", "CudaRasterizer",
+__all__ = ["GbsdfError", "Result", "compute_mesh_sdf", "compute_mesh_sdf_batch", "mesh_lattice", "build_from_mesh", "CudaRasterizer",
            "CudaVolumeGrid", "MODE_REFERENCE", "MODE_EXACT", "PATH_AUTO", "PATH_FAST", "PATH_LEGACY"]
 
 
@@ -91,6 +91,49 @@ def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE
     if rc != _lib.OK and raise_on_error:
         raise GbsdfError(rc, res.message)
     return out, res
+
+
+def compute_mesh_sdf_batch(meshes, outs=None, mode=MODE_REFERENCE, path=PATH_FAST, device=0,
+                           raise_on_error=True):
+    """Batched build. ``meshes``: list of (tris, voxel_size, min_coord, max_coord); all
+    triangles host arrays or all CUDA tensors; ``outs``: matching output buffers (host
+    arrays allocated when None). Returns (outs, statuses, stats list, message)."""
+    n = len(meshes)
+    descs = (_lib.MeshDesc * n)()
+    keep = []
+    tdev = None
+    if outs is None:
+        outs = []
+        for _, _, mn, mx in meshes:
+            d = np.asarray(mx, np.int64) - np.asarray(mn, np.int64) + 1
+            outs.append(np.empty(int(np.prod(d)), np.float32))
+    odev = None
+    for i, ((tris, h, mn, mx), out) in enumerate(zip(meshes, outs)):
+        if isinstance(tris, np.ndarray):
+            tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 12)
+        keep.append(tris)
+        tp, td = _ptr_of(tris)
+        op, od = _ptr_of(out)
+        if tdev is None:
+            tdev, odev = td, od
+        if td != tdev or od != odev:
+            raise ValueError("all triangles (and all outputs) must be on the same side")
+        descs[i].tris, descs[i].n_tris, descs[i].voxel_size = tp, int(tris.shape[0]), float(h)
+        for k in range(3):
+            descs[i].min_coord[k] = int(np.asarray(mn).reshape(3)[k])
+            descs[i].max_coord[k] = int(np.asarray(mx).reshape(3)[k])
+        descs[i].out = op
+    L = _lib.load()
+    o = _lib.Options()
+    L.gbsdf_default_options(C.byref(o))
+    o.mode, o.path, o.device, o.tris_on_device = int(mode), int(path), int(device), int(bool(tdev))
+    stats = (_lib.Stats * n)()
+    err = C.create_string_buffer(512)
+    rc = L.gbsdf_compute_mesh_sdf_batch(descs, n, int(bool(odev)), C.byref(o), stats, err, len(err))
+    statuses = [descs[i].status for i in range(n)]
+    if rc != _lib.OK and raise_on_error:
+        raise GbsdfError(rc, err.value.decode(errors="replace"))
+    return outs, statuses, [s.as_dict() for s in stats], err.value.decode(errors="replace")
 
 
 def mesh_lattice(vertices, voxel_size):

@@ -1,5 +1,5 @@
 """Engine self-tests on the GPU: the correctly rounded division by 3 of the eikonal
-update equals the IEEE quotient x / 3.0f for all 2^32 - NaN float inputs."""
+update equals the IEEE quotient x / 3.0f for every non-NaN float input."""
 import ctypes as C
 
 import pytest
@@ -16,3 +16,4 @@ def test_div3_exhaustive(engine):
     rc = L.gbsdf_selftest(0, 0, C.byref(res), err, len(err))
     assert rc == 0, err.value
     assert res.value == 0, f"{res.value} inputs round differently"
+
