@@ -2,9 +2,10 @@
 
 Workload (one step = one full mesh-to-SDF build): the procedural mug (cup of
 revolution + swept-torus handle) with ~180k triangles on an 860 x 860 x 880 lattice at
-0.1 mm (650,848,000 voxels, 2.6 GB of FP32), fast path, reference-compatible mode
-(the reference's Godunov update and 8-round loop, lockstep sweeps, parity signs,
-3 x 4096 stratified exact-winding probes with r = 24 patch boxes).
+0.1 mm (650,848,000 voxels, 2.6 GB of FP32), fast path. The headline mode is exact
+signs (signed crossings, exact winding number for columns through holes and for the
+3 x 4096 stratified probes, the reference's 8-round lockstep eikonal); `plain` reports
+the reference-compatible mode (parity signs, same eikonal) on the same lattice.
 
 * value   -- Gvoxels/s with the triangles resident in HBM and the grid written to
              HBM (device buffers), timed with CUDA events around K steps.
@@ -170,7 +171,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--mode", default="reference", choices=["reference", "exact"])
+    ap.add_argument("--mode", default="exact-signs", choices=["reference", "exact-signs", "exact"])
     ap.add_argument("--ref-slab", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -198,7 +199,8 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    mode = gbsdf.MODE_REFERENCE if args.mode == "reference" else gbsdf.MODE_EXACT
+    modes = {"reference": gbsdf.MODE_REFERENCE, "exact-signs": gbsdf.MODE_EXACT_SIGNS, "exact": gbsdf.MODE_EXACT}
+    mode = modes[args.mode]
     tris, mn, mx, h = make_workload()
     dims = mx.astype(np.int64) - mn + 1
     N = int(np.prod(dims))
@@ -206,8 +208,8 @@ def main():
     tris_dev = torch.from_numpy(tris).to(dev)
     out_dev = torch.empty(N, dtype=torch.float32, device=dev)
 
-    def step_device():
-        _, res = gbsdf.compute_mesh_sdf(tris_dev, h, mn, mx, out=out_dev, mode=mode, path=gbsdf.PATH_FAST,
+    def step_device(m=mode):
+        _, res = gbsdf.compute_mesh_sdf(tris_dev, h, mn, mx, out=out_dev, mode=m, path=gbsdf.PATH_FAST,
                                         device=local)
         return res
 
@@ -230,6 +232,22 @@ def main():
         barrier()
     dev_ms = max_over_ranks(dist, e0.elapsed_time(e1) / args.steps)
     value = whole_job_gvox(world, N, dev_ms)
+
+    # the plain (reference-compatible) mode on the same lattice, same protocol
+    plain = None
+    if args.mode != "reference":
+        for _ in range(args.warmup):
+            step_device(gbsdf.MODE_REFERENCE)
+        barrier()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record()
+        for _ in range(args.steps):
+            step_device(gbsdf.MODE_REFERENCE)
+        p1.record()
+        barrier()
+        pms = max_over_ranks(dist, p0.elapsed_time(p1) / args.steps)
+        plain = {"mode": "reference", "value": whole_job_gvox(world, N, pms), "ms_per_step": pms}
 
     # ---- end to end through the public API with pinned host buffers
     tris_pin = torch.from_numpy(tris).pin_memory()
@@ -285,6 +303,7 @@ def main():
             "pipeline": {k: s0[k] for k in ("eikonal_rounds", "probes", "sites", "patch_rounds", "patched_voxels",
                                              "unknown_columns", "band_voxels", "splat_evals", "gwn_pairs",
                                              "fp64_rechecks")},
+            "plain": plain,
             "clocks": clk.summary(),
             "gpu_launches": int(sum(s["kernel_launches"] for s in stats))}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -65,9 +65,16 @@ typedef enum gbsdf_mode {
      * probes and r = 24 patch boxes, its decline conditions. Sweeps are lockstep
      * (deterministic); winding signs are decided exactly. */
     GBSDF_MODE_REFERENCE = 0,
-    /* Corrected, monotone Godunov update run to its (unique) fixed point; no
-     * int-range / CSR guards. */
-    GBSDF_MODE_EXACT = 1
+    /* Exact signs and the corrected, monotone Godunov update run to its (unique) fixed
+     * point; no int-range / CSR guards. */
+    GBSDF_MODE_EXACT = 1,
+    /* Exact signs with the reference's distances: signed crossings (the winding number of
+     * a closed, consistently oriented mesh, overlapping shells included) along rays 1000x
+     * closer to the lattice points than the reference's jitter; columns through holes
+     * (nonzero signed total) and the stratified probes decided by the exact winding
+     * number; voxels within 1e-3 voxel of the surface are on it (inside). Reference
+     * eikonal and decline conditions. */
+    GBSDF_MODE_EXACT_SIGNS = 2
 } gbsdf_mode;
 
 typedef enum gbsdf_path {

@@ -43,7 +43,7 @@ def build_ref() -> Path | None:
 
 class FastParams(C.Structure):
     _fields_ = [("fsm_mode", C.c_int), ("gwn_mode", C.c_int), ("threads", C.c_int),
-                ("max_conv_rounds", C.c_int), ("skip_verify", C.c_int)]
+                ("max_conv_rounds", C.c_int), ("skip_verify", C.c_int), ("signed_parity", C.c_int)]
 
 
 class FastStats(C.Structure):
@@ -76,6 +76,7 @@ def lib():
         L.orc_godunov.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float]
         L.orc_splat_band.restype = C.c_longlong
         L.orc_parity_signs.restype = C.c_longlong
+        L.orc_parity_signs_mode.restype = C.c_longlong
         L.orc_fixup_unknown.restype = C.c_longlong
         L.orc_fsm_sweep.restype = C.c_int
         L.orc_eikonal.restype = C.c_int
@@ -162,13 +163,14 @@ def splat_band(tris, h, mn, dims, threads=None):
     return dist, n
 
 
-def parity_signs(tris, h, mn, dims, threads=None):
-    """[B]: scanline parity (RAST:279-368, CSR RAST:824-882). Returns (sign u8, unknown_columns)."""
+def parity_signs(tris, h, mn, dims, threads=None, signed=False):
+    """[B]: scanline parity (RAST:279-368, CSR RAST:824-882), or signed crossings
+    (winding number along the column) with ``signed``. Returns (sign u8, unknown_columns)."""
     t, T = _tris(tris)
     dims = _ivec(dims)
     sign = np.empty(int(np.prod(dims.astype(np.int64))), np.uint8)
-    n = lib().orc_parity_signs(_p(t), C.c_int(T), C.c_float(h), _p(_ivec(mn)), _p(dims), _p(sign),
-                               C.c_int(threads or default_threads()))
+    n = lib().orc_parity_signs_mode(_p(t), C.c_int(T), C.c_float(h), _p(_ivec(mn)), _p(dims), _p(sign),
+                                    C.c_int(threads or default_threads()), C.c_int(1 if signed else 0))
     return sign, n
 
 
@@ -200,15 +202,18 @@ def eikonal(g, sign, dims, h, fsm_mode=1, max_conv_rounds=100000, threads=None):
     return dict(rounds=r, extra_rounds=extra.value, far_residual=resid.value, safe_clamped=clamped.value)
 
 
-def fast_sdf(tris, h, mn, mx, fsm_mode=1, gwn_mode=1, threads=None, skip_verify=False, max_conv_rounds=100000):
-    """The whole fast path (RAST:796-1159). Returns (status, dist or None, sign, stats dict)."""
+def fast_sdf(tris, h, mn, mx, fsm_mode=1, gwn_mode=1, threads=None, skip_verify=False, max_conv_rounds=100000,
+             signed_parity=False):
+    """The whole fast path (RAST:796-1159). Returns (status, dist or None, sign, stats dict).
+    ``signed_parity``: signed crossings in stage [B] (the engine's exact-signs modes)."""
     t, T = _tris(tris)
     mn, mx = _ivec(mn), _ivec(mx)
     dims = mx.astype(np.int64) - mn + 1
     N = int(np.prod(dims)) if (dims > 0).all() else 0
     dist = np.empty(max(N, 1), np.float32)
     sign = np.empty(max(N, 1), np.uint8)
-    prm = FastParams(fsm_mode, gwn_mode, threads or default_threads(), max_conv_rounds, 1 if skip_verify else 0)
+    prm = FastParams(fsm_mode, gwn_mode, threads or default_threads(), max_conv_rounds, 1 if skip_verify else 0,
+                     1 if signed_parity else 0)
     st = FastStats()
     s = lib().orc_fast_sdf(_p(t), C.c_int(T), C.c_float(h), _p(mn), _p(mx), C.byref(prm), _p(dist), _p(sign),
                            C.byref(st))

@@ -183,14 +183,15 @@ struct GwnCounters {
 };
 constexpr float kSurfaceTolVoxels = 1e-5f;
 constexpr float kCoplanarRel = 1e-4f;
-static bool gwn_inside(const OTri* tris, int T, V3 p, int mode, GwnCounters* ctr, float dvox, float h) {
+static bool gwn_inside(const OTri* tris, int T, V3 p, int mode, GwnCounters* ctr, float dvox, float h,
+                       float surface_tol = kSurfaceTolVoxels) {
     if (mode == 0) {
         float s = 0.0f;
         for (int t = 0; t < T; ++t) s += solid_angle_f(p, tris[t].v0, tris[t].v1, tris[t].v2);
         float w = s * kInv4Pi;
         return std::fabs(w) >= 0.5f;
     }
-    if (dvox <= kSurfaceTolVoxels * h) return true;
+    if (dvox <= surface_tol * h) return true;
     float s = 0.0f, comp = 0.0f;
     bool amb = false;
     for (int t = 0; t < T; ++t) {
@@ -280,12 +281,15 @@ static double godunov_exact_d(double a, double b, double c, double h) { return g
 extern "C" {
 
 struct orc_fast_params {
-    int fsm_mode;        // 0: reference loop (<= 8 rounds, audit-gated <= 16 extra); 1: to convergence
+    int fsm_mode;        // 0: reference loop (<= 8 rounds, audit-gated <= 16 extra); 1/2: to convergence
     int gwn_mode;        // 0: reference FP32 naive sum; 1: exact decision
     int threads;         // host threads
     int max_conv_rounds; // cap for fsm_mode 1 (safety only)
     int skip_verify;     // 1: skip stage [E] (used to time/compare stages separately)
+    int signed_parity;   // 1: exact signs -- signed crossings, near-lattice rays, surface tolerance 1e-3 voxel
 };
+// Exact-signs mode: voxels within this many voxels of the surface are on it (inside).
+constexpr float kSurfaceTolExact = 1e-3f;
 
 struct orc_fast_stats {
     int status;  // 0 ok, 1 invalid input, 2 int-range guard, 3 CSR guard, 4 verify diverged
@@ -416,8 +420,26 @@ long long orc_splat_band(const void* tris_, int T, float h, const int* mn, const
 // ---- [B] parity signs (RAST:824-882 host CSR, RAST:279-368 kernel) ------------------
 // Returns the number of unknown columns, or -1 when the CSR guard declines
 // (total_entries <= 0 or > 1e8, RAST:867-869).
+// signed = 0: the reference's parity (odd or > 128 crossings -> unknown column).
+// signed = 1: signed crossings -- a crossing whose projected triangle is clockwise in xy
+// (normal pointing down: entering an outward-oriented solid going up) counts +1, a
+// counter-clockwise one -1; the running sum below a voxel is the winding number of a
+// closed, consistently oriented mesh (overlapping shells included) and the voxel is
+// inside iff it is nonzero. A column whose total is nonzero (a ray through a hole) or
+// that overflows is unknown.
+// The exact-signs mode casts its rays 1000x closer to the lattice point than the
+// reference's jitter (still several float ulps away for |coordinate index| < 4096).
+constexpr float kJXExact = 3.7e-4f;
+constexpr float kJYExact = 5.1e-4f;
+long long orc_parity_signs_mode(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
+                                int threads, int signed_mode);
 long long orc_parity_signs(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
                            int threads) {
+    return orc_parity_signs_mode(tris_, T, h, mn, dims, sign, threads, 0);
+}
+long long orc_parity_signs_mode(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
+                                int threads, int signed_mode) {
+    const float jx = signed_mode ? kJXExact : kJX, jy = signed_mode ? kJYExact : kJY;
     const OTri* tris = static_cast<const OTri*>(tris_);
     const int dx = dims[0], dy = dims[1], dz = dims[2];
     const int sdx = (dx + kSup - 1) / kSup, sdy = (dy + kSup - 1) / kSup;
@@ -461,11 +483,12 @@ long long orc_parity_signs(const void* tris_, int T, float h, const int* mn, con
     std::atomic<long long> unknown(0);
     parallel_dyn((long long)dx * dy, 256, threads, [&](long long cb, long long ce) {
         float hit[kParityMaxHits];
+        int hsg[kParityMaxHits];
         long long local_unknown = 0;
         for (long long col = cb; col < ce; ++col) {
             int cx = (int)(col % dx), cy = (int)(col / dx);
-            float rx = ((float)(mn[0] + cx) + kJX) * h;
-            float ry = ((float)(mn[1] + cy) + kJY) * h;
+            float rx = ((float)(mn[0] + cx) + jx) * h;
+            float ry = ((float)(mn[1] + cy) + jy) * h;
             int nh = 0;
             bool bad = false;
             size_t sup = (size_t)(cy >> 2) * sdx + (cx >> 2);
@@ -484,6 +507,7 @@ long long orc_parity_signs(const void* tris_, int T, float h, const int* mn, con
                 if (std::fabs(area2) < 1e-12f) continue;
                 float zh = (d1 * tr.v0.z + d2 * tr.v1.z + d0 * tr.v2.z) / area2;
                 if (nh < kParityMaxHits) {
+                    hsg[nh] = neg ? 1 : -1;
                     hit[nh++] = zh;
                 } else {
                     bad = true;
@@ -491,21 +515,37 @@ long long orc_parity_signs(const void* tris_, int T, float h, const int* mn, con
                 }
             }
             size_t base = (size_t)cy * dx + cx;
-            if (bad || (nh & 1)) {
+            int total = 0;
+            for (int i = 0; i < nh; ++i) total += hsg[i];
+            if (bad || (signed_mode ? (total != 0) : (nh & 1))) {
                 for (int z = 0; z < dz; ++z) sign[(size_t)z * zstride + base] = 2;
                 ++local_unknown;
                 continue;
             }
-            std::sort(hit, hit + nh);
+            // insertion sort of (height, sign) pairs by height
+            for (int i = 1; i < nh; ++i) {
+                float key = hit[i];
+                int ks = hsg[i];
+                int j = i - 1;
+                while (j >= 0 && hit[j] > key) {
+                    hit[j + 1] = hit[j];
+                    hsg[j + 1] = hsg[j];
+                    --j;
+                }
+                hit[j + 1] = key;
+                hsg[j + 1] = ks;
+            }
             int k = 0;
             bool inside = false;
+            int wnum = 0;
             for (int z = 0; z < dz; ++z) {
                 float zc = (float)(mn[2] + z) * h;
                 while (k < nh && hit[k] < zc) {
                     inside = !inside;
+                    wnum += hsg[k];
                     ++k;
                 }
-                sign[(size_t)z * zstride + base] = inside ? 1 : 0;
+                sign[(size_t)z * zstride + base] = (signed_mode ? (wnum != 0) : inside) ? 1 : 0;
             }
         }
         unknown.fetch_add(local_unknown);
@@ -514,8 +554,15 @@ long long orc_parity_signs(const void* tris_, int T, float h, const int* mn, con
 }
 
 // ---- [C] exact winding fixup (RAST:374-400): every sign==2 voxel -----------------------
+long long orc_fixup_unknown_tol(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
+                                const float* dist, int gwn_mode, int threads, long long* fp64_rechecks, float tol);
 long long orc_fixup_unknown(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
                             const float* dist, int gwn_mode, int threads, long long* fp64_rechecks) {
+    return orc_fixup_unknown_tol(tris_, T, h, mn, dims, sign, dist, gwn_mode, threads, fp64_rechecks,
+                                 kSurfaceTolVoxels);
+}
+long long orc_fixup_unknown_tol(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
+                                const float* dist, int gwn_mode, int threads, long long* fp64_rechecks, float tol) {
     const OTri* tris = static_cast<const OTri*>(tris_);
     const long long dx = dims[0], dy = dims[1], dz = dims[2];
     const long long N = dx * dy * dz;
@@ -528,7 +575,7 @@ long long orc_fixup_unknown(const void* tris_, int T, float h, const int* mn, co
             long long i = todo[(size_t)k];
             int x = (int)(i % dx), y = (int)((i / dx) % dy), z = (int)(i / (dx * dy));
             V3 p{(float)(mn[0] + x) * h, (float)(mn[1] + y) * h, (float)(mn[2] + z) * h};
-            sign[i] = gwn_inside(tris, T, p, gwn_mode, &ctr, dist ? dist[i] : 1e30f, h) ? 1 : 0;
+            sign[i] = gwn_inside(tris, T, p, gwn_mode, &ctr, dist ? dist[i] : 1e30f, h, tol) ? 1 : 0;
         }
     });
     if (fp64_rechecks) *fp64_rechecks += ctr.fp64_rechecks.load();
@@ -719,7 +766,7 @@ float orc_godunov_exact(float ax, float ay, float az, float h) { return godunov_
 // ---- [E] stratified verify + patch (RAST:566-646, RAST:1078-1132) --------------------
 // Returns 1 when a probe came back clean, 0 on systematic divergence.
 int orc_verify_patch(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
-                     const float* dist, int gwn_mode, int threads, orc_fast_stats* st) {
+                     const float* dist, int gwn_mode, int threads, orc_fast_stats* st, float tol) {
     const OTri* tris = static_cast<const OTri*>(tris_);
     const long long dx = dims[0], dy = dims[1], dz = dims[2];
     const size_t N = (size_t)(dx * dy * dz);
@@ -740,7 +787,7 @@ int orc_verify_patch(const void* tris_, int T, float h, const int* mn, const int
                 if (s == 2) continue;
                 int x = (int)(v % dx), y = (int)((v / dx) % dy), z = (int)(v / (dx * dy));
                 V3 p{(float)(mn[0] + x) * h, (float)(mn[1] + y) * h, (float)(mn[2] + z) * h};
-                bool inside = gwn_inside(tris, T, p, gwn_mode, &ctr, dist ? dist[v] : 1e30f, h);
+                bool inside = gwn_inside(tris, T, p, gwn_mode, &ctr, dist ? dist[v] : 1e30f, h, tol);
                 if ((s == 1) != inside) ok[(size_t)i] = 0;
             }
         });
@@ -765,7 +812,7 @@ int orc_verify_patch(const void* tris_, int T, float h, const int* mn, const int
                     for (int x = x0; x <= x1; ++x) sign[(size_t)z * dx * dy + (size_t)y * dx + x] = 2;
         }
         long long fixed =
-            orc_fixup_unknown(tris_, T, h, mn, dims, sign, dist, gwn_mode, threads, &st->fp64_rechecks);
+            orc_fixup_unknown_tol(tris_, T, h, mn, dims, sign, dist, gwn_mode, threads, &st->fp64_rechecks, tol);
         st->patched_voxels += fixed;
         st->sites += m;
         st->patch_rounds += 1;
@@ -804,20 +851,23 @@ int orc_fast_sdf(const void* tris_, int T, float h, const int* mn, const int* mx
     auto ta = clk::now();
     st->band_voxels = orc_splat_band(tris_, T, h, mn, dims, g.data(), threads);
     auto tb = clk::now();
-    long long unk = orc_parity_signs(tris_, T, h, mn, dims, out_sign, threads);
+    long long unk = orc_parity_signs_mode(tris_, T, h, mn, dims, out_sign, threads, prm->signed_parity);
+    const float tol = prm->signed_parity ? kSurfaceTolExact : kSurfaceTolVoxels;
     auto tc = clk::now();
     if (unk < 0) return st->status = 3;
     st->unknown_columns = (int)unk;
     if (unk > 0)
         st->fixup_voxels =
-            orc_fixup_unknown(tris_, T, h, mn, dims, out_sign, g.data(), prm->gwn_mode, threads, &st->fp64_rechecks);
+            orc_fixup_unknown_tol(tris_, T, h, mn, dims, out_sign, g.data(), prm->gwn_mode, threads,
+                                  &st->fp64_rechecks, tol);
     auto td = clk::now();
     st->eikonal_rounds = orc_eikonal(g.data(), out_sign, dims, h, prm->fsm_mode,
                                      prm->max_conv_rounds > 0 ? prm->max_conv_rounds : 100000, threads,
                                      &st->extra_rounds, &st->far_residual, &st->safe_clamped);
     auto te = clk::now();
     int ok = prm->skip_verify ? 1
-                              : orc_verify_patch(tris_, T, h, mn, dims, out_sign, g.data(), prm->gwn_mode, threads, st);
+                              : orc_verify_patch(tris_, T, h, mn, dims, out_sign, g.data(), prm->gwn_mode, threads, st,
+                                                 tol);
     auto tf = clk::now();
     st->ms_splat = ms(ta, tb);
     st->ms_parity = ms(tb, tc);
@@ -827,6 +877,10 @@ int orc_fast_sdf(const void* tris_, int T, float h, const int* mn, const int* mx
     if (!ok) {
         st->ms_total = ms(t0, clk::now());
         return st->status = 4;
+    }
+    if (prm->signed_parity) {  // on-surface voxels take the exact-arithmetic sign (inside)
+        for (long long i = 0; i < N; ++i)
+            if (g[(size_t)i] <= tol * h) out_sign[i] = 1;
     }
     orc_apply_signs(g.data(), out_sign, N);
     std::memcpy(out_dist, g.data(), (size_t)N * sizeof(float));

@@ -167,7 +167,7 @@ constexpr long long kListCap = 8ll * 1024 * 1024;  // >= 64 patch boxes of 49^3 
 
 // Exact winding of every voxel flagged in U (initial unknown columns): compaction
 // into the dense list, FP32 pass, FP64 re-checks; repeats while the list overflowed.
-int fixup_unknown(Workspace& w, const Lattice& L, long long T, Err& e) {
+int fixup_unknown(Workspace& w, const Lattice& L, long long T, float stol, Err& e) {
     cudaStream_t st = w.st;
     for (int pass = 0; pass < 1 << 20; ++pass) {
         GB_CK(cudaMemsetAsync(&w.ds->listed, 0, sizeof(unsigned long long), st));
@@ -180,10 +180,10 @@ int fixup_unknown(Workspace& w, const Lattice& L, long long T, Err& e) {
         if (n <= 0) return GBSDF_OK;
         if (n < 64 * 1024)
             launch_gwn_small(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, P<uint32_t>(w.S),
-                             P<long long>(w.recheck), kListCap, P<float>(w.A), 0, w.ds, n, st);
+                             P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, n, st);
         else
             launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 0, P<uint32_t>(w.S),
-                       P<long long>(w.recheck), kListCap, P<float>(w.A), 0, w.ds, w.num_sms, st);
+                       P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
         GB_CK(cudaGetLastError());
@@ -196,6 +196,9 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
              gbsdf_stats* stats, Err& e) {
     cudaStream_t st = w.st;
     const bool ref_mode = (o.mode == GBSDF_MODE_REFERENCE);
+    const bool exact_signs = (o.mode == GBSDF_MODE_EXACT || o.mode == GBSDF_MODE_EXACT_SIGNS);
+    const bool ref_eikonal = (o.mode != GBSDF_MODE_EXACT);
+    const float stol = exact_signs ? kSurfaceTolExactSigns : kSurfaceTolVoxels;
     const long long N = L.N;
     // ---- buffers
     GB_CK(ensure(w.A, (size_t)N * 4));
@@ -234,7 +237,8 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     if (w.hs->invalid_tris > 0)
         return e.set(GBSDF_EINVAL, "%llu triangles have non-finite or out-of-range coordinates",
                      (unsigned long long)w.hs->invalid_tris);
-    if (ref_mode && (w.hs->csr_entries == 0 || w.hs->csr_entries > 100000000ull))
+    if ((ref_mode || o.mode == GBSDF_MODE_EXACT_SIGNS) &&
+        (w.hs->csr_entries == 0 || w.hs->csr_entries > 100000000ull))
         return e.set(GBSDF_ECSR, "supercell CSR has %llu entries (reference guard: 1..1e8)",
                      (unsigned long long)w.hs->csr_entries);
     const long long brick_pairs = (long long)w.hs->brick_pairs;
@@ -256,18 +260,18 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     GB_CK(cudaEventRecord(w.ev[3], st));
     // ---- [B]
     launch_parity(P<ParTri>(w.ptt), P<unsigned long long>(w.soff), P<unsigned>(w.scount), P<unsigned>(w.slist), L,
-                  P<uint32_t>(w.S), P<uint32_t>(w.U), w.ds, st);
+                  P<uint32_t>(w.S), P<uint32_t>(w.U), w.ds, exact_signs ? 1 : 0, st);
     GB_CK(cudaGetLastError());
     GB_CK(cudaEventRecord(w.ev[4], st));
     // ---- [C]
-    int rc = fixup_unknown(w, L, T, e);
+    int rc = fixup_unknown(w, L, T, stol, e);
     if (rc != GBSDF_OK) return rc;
     GB_CK(cudaEventRecord(w.ev[5], st));
     // ---- [D]
-    const int rule = ref_mode ? 0 : 1;
+    const int rule = ref_eikonal ? 0 : 1;
     float* src = P<float>(w.A);
     float* dst = P<float>(w.B);
-    if (ref_mode) {
+    if (ref_eikonal) {
         for (int r = 0; r < kMaxRounds; ++r) {
             for (int axis = 0; axis < 3; ++axis)
                 for (int dir = 1; dir >= -1; dir -= 2) {
@@ -303,7 +307,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     for (int gen = 0; gen < kProbeGens; ++gen) {
         launch_verify_prepare(L, gen, P<uint32_t>(w.U), P<long long>(w.list), w.ds, st);
         launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnVerify, 0, P<uint32_t>(w.S),
-                   P<long long>(w.recheck), kListCap, P<float>(w.A), 0, w.ds, w.num_sms, st);
+                   P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnVerify, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
         launch_verify_plan(gen, w.ds, st);
@@ -311,7 +315,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         launch_patch_mark(L, P<uint32_t>(w.U), w.ds, st);
         launch_list_unknown(P<uint32_t>(w.U), P<uint32_t>(w.S), L, P<long long>(w.list), kListCap, w.ds, 1, st);
         launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 1, P<uint32_t>(w.S),
-                   P<long long>(w.recheck), kListCap, P<float>(w.A), 0, w.ds, w.num_sms, st);
+                   P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
     }
@@ -319,7 +323,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     GB_CK(cudaEventRecord(w.ev[7], st));
     // ---- [F]
     float* final_dst = out_dev ? out : P<float>(w.B);
-    launch_apply(P<float>(w.A), P<uint32_t>(w.S), L, final_dst, w.ds, st);
+    launch_apply(P<float>(w.A), P<uint32_t>(w.S), L, final_dst, w.ds, exact_signs ? stol * L.h : 0.0f, st);
     GB_CK(cudaGetLastError());
     GB_CK(cudaEventRecord(w.ev[8], st));
     GB_CK(cudaMemcpyAsync(w.hs, w.ds, sizeof(DevState), cudaMemcpyDeviceToHost, st));
@@ -349,8 +353,8 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         // (cuda_rasterizer.cu:1028-1037); a residual after a full round means no voxel is
         // reachable (empty band), so those rounds cannot change anything and are counted,
         // not run.
-        stats->extra_rounds = (ref_mode && h.far_residual > 0) ? kMaxExtraRounds : 0;
-        if (ref_mode) stats->eikonal_rounds += stats->extra_rounds;
+        stats->extra_rounds = (ref_eikonal && h.far_residual > 0) ? kMaxExtraRounds : 0;
+        if (ref_eikonal) stats->eikonal_rounds += stats->extra_rounds;
         stats->far_residual = 0;
         stats->probes = h.probes;
         stats->sites = h.total_sites;
@@ -396,7 +400,7 @@ int run_legacy(Workspace& w, long long T, const Lattice& L, float* out, bool out
         GB_CK(cudaMemcpyAsync(&w.ds->listed, &nn, sizeof(nn), cudaMemcpyHostToDevice, st));
         GB_CK(cudaMemsetAsync(&w.ds->recheck_n, 0, sizeof(unsigned long long), st));
         launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 0, P<uint32_t>(w.S),
-                   P<long long>(w.recheck), kListCap, P<float>(w.A), 1, w.ds, w.num_sms, st);
+                   P<long long>(w.recheck), kListCap, P<float>(w.A), 1, kSurfaceTolVoxels, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
         GB_CK(cudaStreamSynchronize(st));  // `nn` lives on the host stack
@@ -444,7 +448,7 @@ int compute(const float* tris12, long long T, bool tris_dev, float h, const int3
     int path = o.path;
     if (path == GBSDF_PATH_AUTO) path = ((unsigned long long)N >= kFastMinVoxels) ? GBSDF_PATH_FAST : GBSDF_PATH_LEGACY;
     // the reference's int-range guards (cuda_rasterizer.cu:816-820), reference mode only
-    if (path == GBSDF_PATH_FAST && o.mode == GBSDF_MODE_REFERENCE) {
+    if (path == GBSDF_PATH_FAST && o.mode != GBSDF_MODE_EXACT) {
         const long long G = 2000000000LL;
         if (N > G || T * dims[2] > G || dims[0] * dims[1] > G || dims[0] * dims[2] > G || dims[1] * dims[2] > G) {
             if (o.path != GBSDF_PATH_AUTO)

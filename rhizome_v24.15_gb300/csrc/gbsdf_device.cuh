@@ -33,6 +33,9 @@ constexpr float kRecheckBand = 0.05f;  // FP64 re-evaluation when | |w| - 0.5 | 
 // A voxel within this many voxels of the surface lies on it: its winding number is 0.5 in
 // exact arithmetic (inside by |w| >= 0.5), while any floating-point sum of it is noise.
 constexpr float kSurfaceTolVoxels = 1e-5f;
+// The exact-signs modes cast near-lattice rays (offset 3.7e-4 h, 5.1e-4 h) and treat
+// voxels within 1e-3 voxel of the surface as on it.
+constexpr float kSurfaceTolExactSigns = 1e-3f;
 // A triangle term's sign is uncertain when |det| < this * |a||b||c| and the point
 // projects inside the triangle (denominator < 0): such voxels are decided in FP64.
 constexpr float kCoplanarRel = 1e-4f;

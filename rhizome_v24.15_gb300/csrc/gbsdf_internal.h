@@ -99,14 +99,14 @@ void launch_splat(const SplatTri* stt, const unsigned long long* brick_off, cons
                   float* dist, DevState* ds, cudaStream_t st);
 void launch_parity(const ParTri* ptt, const unsigned long long* strip_off, const unsigned* strip_count,
                    const unsigned* strip_list, const Lattice& L, uint32_t* sbits, uint32_t* ubits, DevState* ds,
-                   cudaStream_t st);
+                   int signed_crossings, cudaStream_t st);
 void launch_list_unknown(uint32_t* ubits, uint32_t* sbits, const Lattice& L, long long* list, long long cap,
                          DevState* ds, int only_if_patching, cudaStream_t st);
 // `dist`: the voxel distance field (squared when dist_sq): voxels within
 // kSurfaceTolVoxels of the surface are decided inside without a winding sum.
 void launch_gwn(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
                 int consumer, int only_if, uint32_t* sbits, long long* recheck, long long recheck_cap,
-                const float* dist, int dist_sq, DevState* ds, int num_sms, cudaStream_t st);
+                const float* dist, int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st);
 void launch_gwn_recheck(const float* tri9, long long T, const Lattice& L, const long long* recheck,
                         long long recheck_cap, int consumer, uint32_t* sbits, DevState* ds, int num_sms,
                         cudaStream_t st);
@@ -120,11 +120,11 @@ void launch_end_round(int slot, int round, int cap, DevState* ds, cudaStream_t s
 void launch_audit(const float* g, const Lattice& L, DevState* ds, cudaStream_t st);
 void launch_clamp(float* g, const uint32_t* sbits, const Lattice& L, DevState* ds, cudaStream_t st);
 void launch_apply(const float* g, const uint32_t* sbits, const Lattice& L, float* out, const DevState* ds,
-                  cudaStream_t st);
+                  float surf_tol, cudaStream_t st);
 void launch_pack_tri9(const float* tris12, long long T, float* tri9, cudaStream_t st);
 void launch_gwn_small(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
                       int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, const float* dist,
-                      int dist_sq, DevState* ds, long long n_hint, cudaStream_t st);
+                      int dist_sq, float surf_tol_vox, DevState* ds, long long n_hint, cudaStream_t st);
 void launch_tri_flags(const float* verts, long long nv, const uint32_t* idx, long long nt, unsigned* flags,
                       cudaStream_t st);
 void launch_tri_scatter(const float* verts, long long nv, const uint32_t* idx, long long nt,

@@ -354,8 +354,11 @@ __global__ void clamp_kernel(float* __restrict__ g, const uint32_t* __restrict__
 // [F] cuda_rasterizer.cu:650-661, applied only when the verify loop came back clean
 // (on divergence the output stays untouched, cuda_rasterizer.cu:788-791). One CTA per
 // 4 rows; float4 loads and stores when the row length allows.
+// surf_tol (world units, 0 = off): voxels this close to the surface take the exact-
+// arithmetic sign of a point on it (inside) -- the exact-signs modes.
 __global__ void __launch_bounds__(256) apply_kernel(const float* __restrict__ g, const uint32_t* __restrict__ sbits,
-                                                    Lattice L, float* __restrict__ out, const DevState* ds) {
+                                                    Lattice L, float* __restrict__ out, const DevState* ds,
+                                                    float surf_tol) {
     if (ds->verify_state != 1) return;
     const int dx = L.dims[0];
     const long long nrows = (long long)L.dims[1] * L.dims[2];
@@ -376,7 +379,7 @@ __global__ void __launch_bounds__(256) apply_kernel(const float* __restrict__ g,
                 for (int j = 0; j < 4; ++j) {
                     float e = v[j];
                     if (e > 1e29f) e = 1e6f;
-                    v[j] = ((w >> j) & 1u) ? -e : e;
+                    v[j] = (((w >> j) & 1u) || e <= surf_tol) ? -e : e;
                 }
                 reinterpret_cast<float4*>(orow)[q] = make_float4(v[0], v[1], v[2], v[3]);
             }
@@ -384,7 +387,7 @@ __global__ void __launch_bounds__(256) apply_kernel(const float* __restrict__ g,
             for (int x = threadIdx.x; x < dx; x += blockDim.x) {
                 float e = gr[x];
                 if (e > 1e29f) e = 1e6f;
-                orow[x] = ((sr[x >> 5] >> (x & 31)) & 1u) ? -e : e;
+                orow[x] = (((sr[x >> 5] >> (x & 31)) & 1u) || e <= surf_tol) ? -e : e;
             }
         }
     }
@@ -443,10 +446,10 @@ void launch_clamp(float* g, const uint32_t* sbits, const Lattice& L, DevState* d
 }
 
 void launch_apply(const float* g, const uint32_t* sbits, const Lattice& L, float* out, const DevState* ds,
-                  cudaStream_t st) {
+                  float surf_tol, cudaStream_t st) {
     long long blocks = ((long long)L.dims[1] * L.dims[2] + kRowsPerCta - 1) / kRowsPerCta;
     GBSDF_COUNT_LAUNCH();
-    apply_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, sbits, L, out, ds);
+    apply_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, sbits, L, out, ds, surf_tol);
 }
 
 }  // namespace gbsdf

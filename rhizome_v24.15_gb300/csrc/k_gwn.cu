@@ -101,9 +101,9 @@ __global__ void __launch_bounds__(kGwnThreads) gwn_kernel(const float* __restric
                                                           int consumer, int only_if, uint32_t* __restrict__ sbits,
                                                           long long* __restrict__ recheck, long long recheck_cap,
                                                           const float* __restrict__ dist, int dist_sq,
-                                                          DevState* ds) {
+                                                          float surf_tol_vox, DevState* ds) {
     if (only_if && !ds->patching) return;
-    const float tau = kSurfaceTolVoxels * L.h;
+    const float tau = surf_tol_vox * L.h;
     constexpr int VPB = kGwnThreads / TEAM;
     __shared__ float s_tri[kGwnChunk * 9];
     const long long n = min((long long)ds->listed, cap);
@@ -282,28 +282,28 @@ void launch_list_unknown(uint32_t* ubits, uint32_t* sbits, const Lattice& L, lon
 
 void launch_gwn(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
                 int consumer, int only_if, uint32_t* sbits, long long* recheck, long long recheck_cap,
-                const float* dist, int dist_sq, DevState* ds, int num_sms, cudaStream_t st) {
+                const float* dist, int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st) {
     // consumer kGwnVerify lists are short (<= 4096): one voxel per warp.
     if (consumer == kGwnVerify) {
         long long blocks = (kVerifySamples + 7) / 8;
         GBSDF_COUNT_LAUNCH();
         gwn_kernel<32><<<(unsigned)blocks, kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, only_if,
-                                                                 sbits, recheck, recheck_cap, dist, dist_sq, ds);
+                                                                 sbits, recheck, recheck_cap, dist, dist_sq, surf_tol_vox, ds);
     } else {
         long long blocks = (long long)num_sms * 8;
         GBSDF_COUNT_LAUNCH();
         gwn_kernel<1><<<(unsigned)blocks, kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, only_if,
-                                                                sbits, recheck, recheck_cap, dist, dist_sq, ds);
+                                                                sbits, recheck, recheck_cap, dist, dist_sq, surf_tol_vox, ds);
     }
 }
 
 void launch_gwn_small(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
                       int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, const float* dist,
-                      int dist_sq, DevState* ds, long long n_hint, cudaStream_t st) {
+                      int dist_sq, float surf_tol_vox, DevState* ds, long long n_hint, cudaStream_t st) {
     long long blocks = std::max<long long>(1, (n_hint + 7) / 8);
     GBSDF_COUNT_LAUNCH();
     gwn_kernel<32><<<(unsigned)blocks, kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, 0, sbits,
-                                                             recheck, recheck_cap, dist, dist_sq, ds);
+                                                             recheck, recheck_cap, dist, dist_sq, surf_tol_vox, ds);
 }
 
 void launch_gwn_recheck(const float* tri9, long long T, const Lattice& L, const long long* recheck,

@@ -22,24 +22,36 @@ namespace gbsdf {
 namespace {
 
 constexpr int kParWarps = 4;
+// Exact-signs rays sit 1000x closer to the lattice point than the reference's jitter.
+constexpr float kJXExact = 3.7e-4f;
+constexpr float kJYExact = 5.1e-4f;
 
+// SIGNED = 0: the reference's parity. SIGNED = 1: signed crossings -- a crossing whose
+// projected triangle is clockwise in xy (entering an outward-oriented solid going up)
+// counts +1, a counter-clockwise one -1; the running sum below a voxel is the winding
+// number of a closed, consistently oriented mesh (overlapping shells included), inside
+// iff nonzero; a column whose total is nonzero (a ray through a hole) or that overflows
+// is unknown.
+template <int SIGNED>
 __global__ void __launch_bounds__(kParWarps * 32) parity_kernel(const ParTri* __restrict__ ptt,
                                                                 const unsigned long long* __restrict__ off,
                                                                 const unsigned* __restrict__ cnt,
                                                                 const unsigned* __restrict__ list, Lattice L,
                                                                 uint32_t* __restrict__ sbits,
                                                                 uint32_t* __restrict__ ubits, DevState* ds) {
-    extern __shared__ float s_hits[];  // [kParWarps][kParityMaxHits][32]
+    extern __shared__ float s_hits[];  // [kParWarps][kParityMaxHits][32] floats, then signs
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long strip = (long long)blockIdx.x * kParWarps + warp;
     if (strip >= L.nstrips) return;  // whole warp leaves; no block barrier below
     float* hits = s_hits + (size_t)warp * kParityMaxHits * 32;
+    signed char* hsg = reinterpret_cast<signed char*>(s_hits + (size_t)kParWarps * kParityMaxHits * 32) +
+                       (size_t)warp * kParityMaxHits * 32;
     const int y = (int)(strip / L.nsx), sx = (int)(strip % L.nsx);
     const int x = sx * kStrip + lane;
     const bool col = x < L.dims[0];
     const float h = L.h;
-    const float rx = ((float)(L.mn[0] + x) + kJX) * h;
-    const float ry = ((float)(L.mn[1] + y) + kJY) * h;
+    const float rx = ((float)(L.mn[0] + x) + (SIGNED ? kJXExact : kJX)) * h;
+    const float ry = ((float)(L.mn[1] + y) + (SIGNED ? kJYExact : kJY)) * h;
     const int supx = x >> 2, supy = y >> 2;
     int nh = 0;
     bool bad = false;
@@ -63,27 +75,35 @@ __global__ void __launch_bounds__(kParWarps * 32) parity_kernel(const ParTri* __
         float zh = (d1 * v[2] + d2 * v[5] + d0 * v[8]) / area2;
         if (nh < kParityMaxHits) {
             hits[nh * 32 + lane] = zh;
+            if (SIGNED) hsg[nh * 32 + lane] = neg ? 1 : -1;
             ++nh;
         } else {
             bad = true;
         }
     }
-    // insertion sort of this lane's crossings
+    // insertion sort of this lane's crossings (with their signs)
+    int total = 0;
     for (int i = 1; i < nh; ++i) {
         float key = hits[i * 32 + lane];
+        signed char ks = SIGNED ? hsg[i * 32 + lane] : 0;
         int j = i - 1;
         while (j >= 0 && hits[j * 32 + lane] > key) {
             hits[(j + 1) * 32 + lane] = hits[j * 32 + lane];
+            if (SIGNED) hsg[(j + 1) * 32 + lane] = hsg[j * 32 + lane];
             --j;
         }
         hits[(j + 1) * 32 + lane] = key;
+        if (SIGNED) hsg[(j + 1) * 32 + lane] = ks;
     }
-    const bool unknown = col && (bad || (nh & 1));
+    if (SIGNED)
+        for (int i = 0; i < nh; ++i) total += hsg[i * 32 + lane];
+    const bool unknown = col && (bad || (SIGNED ? (total != 0) : (nh & 1)));
     const uint32_t uword = __ballot_sync(0xffffffffu, unknown);
     if (lane == 0 && uword) atomicAdd(&ds->unknown_columns, (unsigned long long)__popc(uword));
     const bool track = col && !unknown;
     int k = 0;
     bool inside = false;
+    int wnum = 0;
     const size_t zrow = (size_t)L.dims[1] * L.wx;
     const size_t wbase = (size_t)y * L.wx + sx;
     for (int z = 0; z < L.dims[2]; ++z) {
@@ -91,10 +111,11 @@ __global__ void __launch_bounds__(kParWarps * 32) parity_kernel(const ParTri* __
         if (track) {
             while (k < nh && hits[k * 32 + lane] < zc) {
                 inside = !inside;
+                if (SIGNED) wnum += hsg[k * 32 + lane];
                 ++k;
             }
         }
-        const uint32_t sword = __ballot_sync(0xffffffffu, track && inside);
+        const uint32_t sword = __ballot_sync(0xffffffffu, track && (SIGNED ? (wnum != 0) : inside));
         if (lane == 0) {
             sbits[(size_t)z * zrow + wbase] = sword;
             ubits[(size_t)z * zrow + wbase] = uword;
@@ -106,13 +127,19 @@ __global__ void __launch_bounds__(kParWarps * 32) parity_kernel(const ParTri* __
 
 void launch_parity(const ParTri* ptt, const unsigned long long* strip_off, const unsigned* strip_count,
                    const unsigned* strip_list, const Lattice& L, uint32_t* sbits, uint32_t* ubits, DevState* ds,
-                   cudaStream_t st) {
-    const int smem = kParWarps * kParityMaxHits * 32 * (int)sizeof(float);
-    cudaFuncSetAttribute(parity_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+                   int signed_crossings, cudaStream_t st) {
+    const int smem = kParWarps * kParityMaxHits * 32 * (int)(sizeof(float) + (signed_crossings ? 1 : 0));
     long long blocks = (L.nstrips + kParWarps - 1) / kParWarps;
     GBSDF_COUNT_LAUNCH();
-    parity_kernel<<<(unsigned)blocks, kParWarps * 32, smem, st>>>(ptt, strip_off, strip_count, strip_list, L, sbits,
-                                                                  ubits, ds);
+    if (signed_crossings) {
+        cudaFuncSetAttribute(parity_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        parity_kernel<1><<<(unsigned)blocks, kParWarps * 32, smem, st>>>(ptt, strip_off, strip_count, strip_list, L,
+                                                                         sbits, ubits, ds);
+    } else {
+        cudaFuncSetAttribute(parity_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        parity_kernel<0><<<(unsigned)blocks, kParWarps * 32, smem, st>>>(ptt, strip_off, strip_count, strip_list, L,
+                                                                         sbits, ubits, ds);
+    }
 }
 
 }  // namespace gbsdf

@@ -15,7 +15,7 @@ OK, EINVAL, EGUARD, ECSR, EVERIFY, ENOMEM, ECUDA, ENODEV = range(8)
 STATUS_NAMES = {OK: "OK", EINVAL: "EINVAL", EGUARD: "EGUARD", ECSR: "ECSR", EVERIFY: "EVERIFY",
                 ENOMEM: "ENOMEM", ECUDA: "ECUDA", ENODEV: "ENODEV"}
 # gbsdf_mode / gbsdf_path
-MODE_REFERENCE, MODE_EXACT = 0, 1
+MODE_REFERENCE, MODE_EXACT, MODE_EXACT_SIGNS = 0, 1, 2
 PATH_AUTO, PATH_FAST, PATH_LEGACY = 0, 1, 2
 
 

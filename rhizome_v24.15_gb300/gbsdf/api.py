@@ -21,10 +21,10 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import MODE_EXACT, MODE_REFERENCE, PATH_AUTO, PATH_FAST, PATH_LEGACY, STATUS_NAMES
+from ._lib import MODE_EXACT, MODE_EXACT_SIGNS, MODE_REFERENCE, PATH_AUTO, PATH_FAST, PATH_LEGACY, STATUS_NAMES
 
 __all__ = ["GbsdfError", "Result", "compute_mesh_sdf", "compute_mesh_sdf_batch", "mesh_lattice", "build_from_mesh", "CudaRasterizer",
-           "CudaVolumeGrid", "MODE_REFERENCE", "MODE_EXACT", "PATH_AUTO", "PATH_FAST", "PATH_LEGACY"]
+           "CudaVolumeGrid", "MODE_REFERENCE", "MODE_EXACT", "MODE_EXACT_SIGNS", "PATH_AUTO", "PATH_FAST", "PATH_LEGACY"]
 
 
 class GbsdfError(RuntimeError):
