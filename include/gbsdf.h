@@ -74,7 +74,13 @@ typedef enum gbsdf_mode {
      * (nonzero signed total) and the stratified probes decided by the exact winding
      * number; voxels within 1e-3 voxel of the surface are on it (inside). Reference
      * eikonal and decline conditions. */
-    GBSDF_MODE_EXACT_SIGNS = 2
+    GBSDF_MODE_EXACT_SIGNS = 2,
+    /* Reference mode plus learned proposals: a small network (32 brick features -> 64 ->
+     * 64 -> 1, BF16 weights, FP32 accumulation) scores every 8^3 brick's sign-error risk
+     * and the riskiest bricks are re-decided by the exact winding kernel after the
+     * stratified probes and patch boxes (which therefore see the plain path's signs); the
+     * network never supplies a sign. Needs opt->mlp_params. */
+    GBSDF_MODE_LEARNED = 3
 } gbsdf_mode;
 
 typedef enum gbsdf_path {
@@ -90,8 +96,18 @@ typedef struct gbsdf_options {
     int32_t device;        /* CUDA device ordinal */
     int32_t tris_on_device;/* 1: `tris` is a device pointer */
     int32_t max_rounds;    /* exact mode: safety cap on sweep rounds (0 = default 4096) */
-    int32_t reserved[7];
+    int32_t mlp_budget;    /* learned mode: most bricks proposed (0 = 1/16 of the bricks) */
+    float mlp_threshold;   /* learned mode: risk probability above which a brick is proposed */
+    int32_t reserved0;
+    const float* mlp_params; /* learned mode: GBSDF_MLP_PARAMS FP32 parameters in device memory */
+    const float* brick_scores; /* learned mode, instead of the network: caller-supplied risk
+                                  logits, one per 8^3 brick (x fastest), in device memory */
+    int32_t reserved[2];
 } gbsdf_options;
+
+/* Learned sign-risk model: parameter count and brick feature count. */
+#define GBSDF_MLP_PARAMS 6337
+#define GBSDF_MLP_FEATURES 32
 
 typedef struct gbsdf_stats {
     int32_t status;
@@ -116,7 +132,8 @@ typedef struct gbsdf_stats {
     int64_t brick_pairs;   /* (triangle, brick) pairs binned for the splat */
     int64_t csr_entries;   /* entries of the reference's supercell CSR */
     int64_t kernel_launches; /* CUDA kernels this call launched */
-    int64_t reserved[7];
+    int64_t proposed;      /* learned mode: bricks the network proposed for the exact winding number */
+    int64_t reserved[6];
 } gbsdf_stats;
 
 /* Fill `opt` with defaults: reference mode, AUTO path, device 0, host triangles. */
@@ -162,6 +179,30 @@ int gbsdf_build_from_mesh(const float* verts, int64_t n_verts, const uint32_t* i
                           float voxel_size, const int32_t min_coord[3], const int32_t max_coord[3], float* out,
                           int32_t out_on_device, const gbsdf_options* opt, gbsdf_stats* stats, char* err,
                           size_t errlen);
+
+/* Brick features of the learned sign-risk model for one lattice (8^3 bricks, x fastest):
+ * GBSDF_MLP_FEATURES floats per brick written to `features_dev` (device memory,
+ * capacity_bricks bricks). n_bricks[3] receives the brick grid. No counterpart in the
+ * reference. */
+int gbsdf_brick_features(const gbsdf_tri* tris, int64_t n_tris, float voxel_size, const int32_t min_coord[3],
+                         const int32_t max_coord[3], int32_t tris_on_device, float* features_dev,
+                         int64_t capacity_bricks, int32_t n_bricks[3], char* err, size_t errlen);
+
+/* The model's forward pass: logits_dev[i] for the n feature rows of features_dev (device). */
+int gbsdf_mlp_forward(const float* params_dev, const float* features_dev, int64_t n, float* logits_dev,
+                      int32_t device, char* err, size_t errlen);
+
+/* Backward pass of the weighted binary cross-entropy with logits: grad_dev receives the
+ * gradient summed over the n rows (deterministic order), loss_dev[0] the summed loss.
+ * labels_dev: 0/1 floats; weights_dev: per-row weights or NULL. */
+int gbsdf_mlp_backward(const float* params_dev, const float* features_dev, const float* labels_dev,
+                       const float* weights_dev, int64_t n, float* grad_dev, float* loss_dev, int32_t device,
+                       char* err, size_t errlen);
+
+/* One Adam step on params_dev with moments m_dev, v_dev (all GBSDF_MLP_PARAMS floats on
+ * the device); the gradient is multiplied by grad_scale first; step counts from 1. */
+int gbsdf_mlp_adam(float* params_dev, const float* grad_dev, float* m_dev, float* v_dev, float lr, float beta1,
+                   float beta2, float eps, float grad_scale, int32_t step, int32_t device, char* err, size_t errlen);
 
 /* Releases the cached device workspace of `device` (buffers are otherwise reused
  * across calls on the same device). */

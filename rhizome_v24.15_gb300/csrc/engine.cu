@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "../../include/gbsdf.h"
 #include "gbsdf_device.cuh"
@@ -46,7 +47,7 @@ struct Workspace {
     cudaEvent_t ev[12] = {};
     std::mutex mu;
     Buf A, B, S, U, t12, t9, stt, ptt, bcount, bcur, boff, active, blist, scount, scur, soff, slist, scan, list,
-        recheck, hb, verts, idx, flags, fpos;
+        recheck, hb, verts, idx, flags, fpos, S2, U2, fbase, fX, logits, opencnt, ekeys, ecnt, mparts, mlossp, phist, E;
     DevState* ds = nullptr;
     DevState* hs = nullptr;  // pinned host mirror
 };
@@ -120,7 +121,8 @@ void free_ws(Workspace& w) {
     cudaSetDevice(w.device);
     Buf* bufs[] = {&w.A, &w.B, &w.S, &w.U, &w.t12, &w.t9, &w.stt, &w.ptt, &w.bcount, &w.bcur, &w.boff,
                    &w.active, &w.blist, &w.scount, &w.scur, &w.soff, &w.slist, &w.scan, &w.list, &w.recheck,
-                   &w.hb, &w.verts, &w.idx, &w.flags, &w.fpos};
+                   &w.hb, &w.verts, &w.idx, &w.flags, &w.fpos, &w.S2, &w.U2, &w.fbase, &w.fX, &w.logits,
+                   &w.opencnt, &w.ekeys, &w.ecnt, &w.mparts, &w.mlossp, &w.phist, &w.E};
     for (Buf* b : bufs) {
         if (b->p) cudaFree(b->p);
         *b = Buf{};
@@ -167,13 +169,14 @@ constexpr long long kListCap = 8ll * 1024 * 1024;  // >= 64 patch boxes of 49^3 
 
 // Exact winding of every voxel flagged in U (initial unknown columns): compaction
 // into the dense list, FP32 pass, FP64 re-checks; repeats while the list overflowed.
-int fixup_unknown(Workspace& w, const Lattice& L, long long T, float stol, Err& e) {
+int fixup_unknown(Workspace& w, const Lattice& L, long long T, float stol, Err& e, uint32_t* ebits = nullptr) {
     cudaStream_t st = w.st;
     for (int pass = 0; pass < 1 << 20; ++pass) {
         GB_CK(cudaMemsetAsync(&w.ds->listed, 0, sizeof(unsigned long long), st));
         GB_CK(cudaMemsetAsync(&w.ds->list_overflow, 0, sizeof(unsigned long long), st));
         GB_CK(cudaMemsetAsync(&w.ds->recheck_n, 0, sizeof(unsigned long long), st));
-        launch_list_unknown(P<uint32_t>(w.U), P<uint32_t>(w.S), L, P<long long>(w.list), kListCap, w.ds, 0, st);
+        launch_list_unknown(P<uint32_t>(w.U), P<uint32_t>(w.S), L, P<long long>(w.list), kListCap, w.ds, 0, st,
+                            ebits);
         GB_CK(cudaMemcpyAsync(w.hs, w.ds, sizeof(DevState), cudaMemcpyDeviceToHost, st));
         GB_CK(cudaStreamSynchronize(st));
         long long n = std::min<long long>((long long)w.hs->listed, kListCap);
@@ -192,8 +195,34 @@ int fixup_unknown(Workspace& w, const Lattice& L, long long T, float stol, Err& 
     return e.set(GBSDF_ECUDA, "unknown-voxel fixup did not drain");
 }
 
+// Learned-model brick features into w.fX, from the unsigned distance field (w.A), the
+// plain path's signs (w.S), the exact-decided mask (w.E) and a second, signed-crossing
+// parity pass (w.S2 / w.U2); runs after the verify / patch stage.
+int brick_features(Workspace& w, long long T, const Lattice& L, Err& e) {
+    cudaStream_t st = w.st;
+    GB_CK(ensure(w.S2, (size_t)L.nwords * 4));
+    GB_CK(ensure(w.U2, (size_t)L.nwords * 4));
+    GB_CK(ensure(w.fbase, (size_t)L.nbricks * kBrickBase * 4));
+    GB_CK(ensure(w.fX, (size_t)L.nbricks * kMlpIn * 4));
+    GB_CK(ensure(w.opencnt, (size_t)L.nbricks * 4));
+    const long long cap = edge_table_cap(T);
+    GB_CK(ensure(w.ekeys, (size_t)cap * 8));
+    GB_CK(ensure(w.ecnt, (size_t)cap * 4));
+    GB_CK(cudaMemsetAsync(w.ekeys.p, 0, (size_t)cap * 8, st));
+    GB_CK(cudaMemsetAsync(w.ecnt.p, 0, (size_t)cap * 4, st));
+    GB_CK(cudaMemsetAsync(w.opencnt.p, 0, (size_t)L.nbricks * 4, st));
+    launch_parity(P<ParTri>(w.ptt), P<unsigned long long>(w.soff), P<unsigned>(w.scount), P<unsigned>(w.slist), L,
+                  P<uint32_t>(w.S2), P<uint32_t>(w.U2), w.ds, 1, st);
+    launch_open_edges(P<float>(w.t12), T, L, P<unsigned long long>(w.ekeys), P<unsigned>(w.ecnt), cap,
+                      P<unsigned>(w.opencnt), st);
+    launch_brick_features(P<float>(w.A), P<uint32_t>(w.S), P<uint32_t>(w.E), P<uint32_t>(w.S2), P<uint32_t>(w.U2),
+                          P<unsigned>(w.bcount), P<unsigned>(w.opencnt), L, P<float>(w.fbase), P<float>(w.fX), st);
+    GB_CK(cudaGetLastError());
+    return GBSDF_OK;
+}
+
 int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o, float* out, bool out_dev,
-             gbsdf_stats* stats, Err& e) {
+             gbsdf_stats* stats, Err& e, float* features_out = nullptr) {
     cudaStream_t st = w.st;
     const bool ref_mode = (o.mode == GBSDF_MODE_REFERENCE);
     const bool exact_signs = (o.mode == GBSDF_MODE_EXACT || o.mode == GBSDF_MODE_EXACT_SIGNS);
@@ -262,9 +291,18 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     launch_parity(P<ParTri>(w.ptt), P<unsigned long long>(w.soff), P<unsigned>(w.scount), P<unsigned>(w.slist), L,
                   P<uint32_t>(w.S), P<uint32_t>(w.U), w.ds, exact_signs ? 1 : 0, st);
     GB_CK(cudaGetLastError());
+    // ---- learned mode: E records every voxel the exact winding number decides, so the
+    // brick features (after [E]) can tell the remaining risk apart
+    const bool learned = (o.mode == GBSDF_MODE_LEARNED);
+    uint32_t* ebits = nullptr;
+    if (learned || features_out) {
+        GB_CK(ensure(w.E, (size_t)L.nwords * 4));
+        GB_CK(cudaMemsetAsync(w.E.p, 0, (size_t)L.nwords * 4, st));
+        ebits = P<uint32_t>(w.E);
+    }
     GB_CK(cudaEventRecord(w.ev[4], st));
     // ---- [C]
-    int rc = fixup_unknown(w, L, T, stol, e);
+    int rc = fixup_unknown(w, L, T, stol, e, ebits);
     if (rc != GBSDF_OK) return rc;
     GB_CK(cudaEventRecord(w.ev[5], st));
     // ---- [D]
@@ -313,13 +351,52 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         launch_verify_plan(gen, w.ds, st);
         if (gen == kProbeGens - 1) break;  // the last generation never patches
         launch_patch_mark(L, P<uint32_t>(w.U), w.ds, st);
-        launch_list_unknown(P<uint32_t>(w.U), P<uint32_t>(w.S), L, P<long long>(w.list), kListCap, w.ds, 1, st);
+        launch_list_unknown(P<uint32_t>(w.U), P<uint32_t>(w.S), L, P<long long>(w.list), kListCap, w.ds, 1, st,
+                            ebits);
         launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 1, P<uint32_t>(w.S),
                    P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
     }
     GB_CK(cudaGetLastError());
+    // ---- learned proposals: the riskiest bricks re-decided by the exact winding number
+    // (after [E], so the probes and patch boxes ran exactly as in the plain path)
+    if (learned || features_out) {
+        // the signed pass counts unknown columns too; keep the reference pass's count
+        GB_CK(cudaMemcpyAsync(&w.hs->unknown_columns, &w.ds->unknown_columns, 8, cudaMemcpyDeviceToHost, st));
+        GB_CK(cudaStreamSynchronize(st));
+        const unsigned long long unk_ref = w.hs->unknown_columns;
+        int rcf = brick_features(w, T, L, e);
+        if (rcf != GBSDF_OK) return rcf;
+        GB_CK(cudaMemcpyAsync(&w.ds->unknown_columns, &unk_ref, 8, cudaMemcpyHostToDevice, st));
+        if (features_out) {
+            GB_CK(cudaMemcpyAsync(features_out, w.fX.p, (size_t)L.nbricks * kMlpIn * 4, cudaMemcpyDeviceToDevice, st));
+            GB_CK(cudaStreamSynchronize(st));
+            return GBSDF_OK;
+        }
+        if (!o.mlp_params && !o.brick_scores) return e.set(GBSDF_EINVAL, "learned mode needs mlp_params");
+        const float* logits = o.brick_scores;
+        if (!logits) {
+            GB_CK(ensure(w.logits, (size_t)L.nbricks * 4));
+            launch_mlp_forward(o.mlp_params, P<float>(w.fX), L.nbricks, P<float>(w.logits), st);
+            logits = P<float>(w.logits);
+        }
+        const float pthr = (o.mlp_threshold > 0.0f && o.mlp_threshold < 1.0f) ? o.mlp_threshold : 0.5f;
+        const float lthr = logf(pthr / (1.0f - pthr));
+        const unsigned budget =
+            o.mlp_budget > 0 ? (unsigned)o.mlp_budget : (unsigned)std::max<long long>(1, L.nbricks / 16);
+        GB_CK(ensure(w.phist, (size_t)kPropBins * 4));
+        GB_CK(cudaMemsetAsync(w.phist.p, 0, (size_t)kPropBins * 4, st));
+        launch_propose_hist(logits, L.nbricks, lthr, P<unsigned>(w.phist), st);
+        std::vector<unsigned> hist(kPropBins);
+        GB_CK(cudaMemcpyAsync(hist.data(), w.phist.p, (size_t)kPropBins * 4, cudaMemcpyDeviceToHost, st));
+        GB_CK(cudaStreamSynchronize(st));
+        const int cut = propose_cut_bin(hist.data(), budget);
+        launch_propose(logits, L, lthr, cut, &w.ds->proposed, P<uint32_t>(w.U), st);
+        GB_CK(cudaGetLastError());
+        int rcp = fixup_unknown(w, L, T, stol, e);
+        if (rcp != GBSDF_OK) return rcp;
+    }
     GB_CK(cudaEventRecord(w.ev[7], st));
     // ---- [F]
     float* final_dst = out_dev ? out : P<float>(w.B);
@@ -369,6 +446,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         stats->brick_pairs = (long long)h.brick_pairs;
         stats->csr_entries = (long long)h.csr_entries;
         stats->path_taken = GBSDF_PATH_FAST;
+        stats->proposed = (long long)h.proposed;
     }
     return status;
 }
@@ -630,6 +708,100 @@ int gbsdf_build_from_mesh(const float* verts, int64_t n_verts, const uint32_t* i
     int rc = compute(tris_dev, kept, true, voxel_size, min_coord, max_coord, out, out_on_device != 0, o, stats, e);
     cudaFree(tris_dev);
     return rc;
+}
+
+int gbsdf_brick_features(const gbsdf_tri* tris, int64_t n_tris, float voxel_size, const int32_t min_coord[3],
+                         const int32_t max_coord[3], int32_t tris_on_device, float* features_dev,
+                         int64_t capacity_bricks, int32_t n_bricks[3], char* err, size_t errlen) {
+    Err e{err, errlen};
+    if (err && errlen) err[0] = 0;
+    if (!tris || n_tris <= 0 || !min_coord || !max_coord || !features_dev)
+        return e.set(GBSDF_EINVAL, "bad arguments");
+    long long dims[3];
+    for (int k = 0; k < 3; ++k) dims[k] = (long long)max_coord[k] - min_coord[k] + 1;
+    if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return e.set(GBSDF_EINVAL, "empty lattice");
+    Lattice L = make_lattice(min_coord, max_coord, voxel_size);
+    if (n_bricks)
+        for (int k = 0; k < 3; ++k) n_bricks[k] = L.nb[k];
+    if (L.nbricks > capacity_bricks) return e.set(GBSDF_EINVAL, "feature buffer holds %lld bricks, need %lld",
+                                                  (long long)capacity_bricks, L.nbricks);
+    gbsdf_options o;
+    gbsdf_default_options(&o);
+    o.mode = GBSDF_MODE_REFERENCE;
+    o.tris_on_device = tris_on_device;
+    Workspace& w = g_ws[0];
+    std::lock_guard<std::mutex> lk(w.mu);
+    int rc = init_ws(w, 0, e);
+    if (rc != GBSDF_OK) return rc;
+    GB_CK(cudaSetDevice(0));
+    GB_CK(ensure(w.t12, (size_t)n_tris * 48));
+    GB_CK(cudaMemcpyAsync(w.t12.p, tris, (size_t)n_tris * 48,
+                          tris_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, w.st));
+    GB_CK(cudaEventRecord(w.ev[0], w.st));
+    GB_CK(cudaEventRecord(w.ev[1], w.st));
+    return run_fast(w, n_tris, L, o, nullptr, true, nullptr, e, features_dev);
+}
+
+static Workspace* mlp_ws(int32_t device, Err& e, int& rc) {
+    rc = GBSDF_OK;
+    if (device < 0 || device >= 64) {
+        rc = e.set(GBSDF_ENODEV, "device %d out of range", device);
+        return nullptr;
+    }
+    Workspace& w = g_ws[device];
+    rc = init_ws(w, device, e);
+    return rc == GBSDF_OK ? &w : nullptr;
+}
+
+int gbsdf_mlp_forward(const float* params_dev, const float* features_dev, int64_t n, float* logits_dev,
+                      int32_t device, char* err, size_t errlen) {
+    Err e{err, errlen};
+    if (!params_dev || !features_dev || !logits_dev || n < 0) return e.set(GBSDF_EINVAL, "bad arguments");
+    int rc;
+    Workspace* w = mlp_ws(device, e, rc);
+    if (!w) return rc;
+    std::lock_guard<std::mutex> lk(w->mu);
+    GB_CK(cudaSetDevice(device));
+    launch_mlp_forward(params_dev, features_dev, n, logits_dev, w->st);
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaStreamSynchronize(w->st));
+    return GBSDF_OK;
+}
+
+int gbsdf_mlp_backward(const float* params_dev, const float* features_dev, const float* labels_dev,
+                       const float* weights_dev, int64_t n, float* grad_dev, float* loss_dev, int32_t device,
+                       char* err, size_t errlen) {
+    Err e{err, errlen};
+    if (!params_dev || !features_dev || !labels_dev || !grad_dev || !loss_dev || n <= 0)
+        return e.set(GBSDF_EINVAL, "bad arguments");
+    int rc;
+    Workspace* w = mlp_ws(device, e, rc);
+    if (!w) return rc;
+    std::lock_guard<std::mutex> lk(w->mu);
+    GB_CK(cudaSetDevice(device));
+    const int parts = mlp_backward_parts(n);
+    GB_CK(ensure(w->mparts, (size_t)parts * kMlpParams * 4));
+    GB_CK(ensure(w->mlossp, (size_t)parts * 4));
+    launch_mlp_backward(params_dev, features_dev, labels_dev, weights_dev, n, P<float>(w->mparts), P<float>(w->mlossp),
+                        grad_dev, loss_dev, w->st);
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaStreamSynchronize(w->st));
+    return GBSDF_OK;
+}
+
+int gbsdf_mlp_adam(float* params_dev, const float* grad_dev, float* m_dev, float* v_dev, float lr, float beta1,
+                   float beta2, float eps, float grad_scale, int32_t step, int32_t device, char* err, size_t errlen) {
+    Err e{err, errlen};
+    if (!params_dev || !grad_dev || !m_dev || !v_dev || step < 1) return e.set(GBSDF_EINVAL, "bad arguments");
+    int rc;
+    Workspace* w = mlp_ws(device, e, rc);
+    if (!w) return rc;
+    std::lock_guard<std::mutex> lk(w->mu);
+    GB_CK(cudaSetDevice(device));
+    launch_adam(params_dev, grad_dev, m_dev, v_dev, kMlpParams, lr, beta1, beta2, eps, grad_scale, step, w->st);
+    GB_CK(cudaGetLastError());
+    GB_CK(cudaStreamSynchronize(w->st));
+    return GBSDF_OK;
 }
 
 void gbsdf_release_workspace(int32_t device) {

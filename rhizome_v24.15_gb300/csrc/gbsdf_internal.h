@@ -71,11 +71,19 @@ struct DevState {
     int probe_m;                       // mismatches of the current probe
     int total_sites;
     int patch_rounds;
+    unsigned proposed;                 // learned mode: bricks the network proposed
+    unsigned pad_;
     long long sites[4096];
 };
 
 // Consumers of an exact winding decision.
 enum GwnConsumer : int { kGwnFixup = 0, kGwnVerify = 1 };
+
+// Learned sign-risk model: 32 brick features -> 64 -> 64 -> 1.
+constexpr int kBrickBase = 8;                 // base quantities per brick
+constexpr int kMlpIn = 32, kMlpHidden = 64;
+constexpr int kMlpParams = kMlpHidden * kMlpIn + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;
+constexpr int kMlpBwdSamples = 64;            // samples per CTA of the backward pass
 
 // Kernel launches issued by this library (all launchers count themselves).
 unsigned long long& launch_counter();
@@ -100,8 +108,10 @@ void launch_splat(const SplatTri* stt, const unsigned long long* brick_off, cons
 void launch_parity(const ParTri* ptt, const unsigned long long* strip_off, const unsigned* strip_count,
                    const unsigned* strip_list, const Lattice& L, uint32_t* sbits, uint32_t* ubits, DevState* ds,
                    int signed_crossings, cudaStream_t st);
+// Lists the voxels whose U bit is set, clears their U and S bits and, when `ebits` is
+// given, records them there as decided by the exact winding number.
 void launch_list_unknown(uint32_t* ubits, uint32_t* sbits, const Lattice& L, long long* list, long long cap,
-                         DevState* ds, int only_if_patching, cudaStream_t st);
+                         DevState* ds, int only_if_patching, cudaStream_t st, uint32_t* ebits = nullptr);
 // `dist`: the voxel distance field (squared when dist_sq): voxels within
 // kSurfaceTolVoxels of the surface are decided inside without a winding sum.
 void launch_gwn(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
@@ -134,6 +144,26 @@ void launch_legacy_dist(const float* t9, long long T, const float* hb, const Lat
                         cudaStream_t st);
 void launch_legacy_combine(const float* d2, const uint32_t* sbits, const Lattice& L, float* out, cudaStream_t st);
 void launch_iota(long long* list, long long n, long long from, cudaStream_t st);
+long long edge_table_cap(long long T);
+void launch_open_edges(const float* t12, long long T, const Lattice& L, unsigned long long* keys, unsigned* counts,
+                       long long cap, unsigned* open_count, cudaStream_t st);
+void launch_brick_features(const float* dist, const uint32_t* S, const uint32_t* E, const uint32_t* S2,
+                           const uint32_t* U2, const unsigned* brick_tris, const unsigned* open_count,
+                           const Lattice& L, float* base, float* X, cudaStream_t st);
+void launch_mlp_forward(const float* P, const float* X, long long B, float* logits, cudaStream_t st);
+int mlp_backward_parts(long long B);
+void launch_mlp_backward(const float* P, const float* X, const float* y, const float* wt, long long B, float* partial,
+                         float* loss_partial, float* grad, float* loss, cudaStream_t st);
+void launch_adam(float* P, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps,
+                 float scale, int step, cudaStream_t st);
+// learned proposals: logit histogram (kPropBins bins above the threshold), the cut bin
+// that keeps the proposal count within the budget (host), then the marking pass
+constexpr int kPropBins = 4096;
+constexpr float kPropScale = 128.0f;
+void launch_propose_hist(const float* logits, long long nb, float logit_thr, unsigned* hist, cudaStream_t st);
+int propose_cut_bin(const unsigned* hist, unsigned budget);
+void launch_propose(const float* logits, const Lattice& L, float logit_thr, int cut_bin, unsigned* n_prop, uint32_t* U,
+                    cudaStream_t st);
 void launch_selftest_div3(unsigned long long* mism, cudaStream_t st);
 
 }  // namespace gbsdf

@@ -57,8 +57,9 @@ __device__ __forceinline__ void consume(const Lattice& L, long long v, bool insi
     }
 }
 
-__global__ void list_unknown_kernel(uint32_t* __restrict__ ubits, uint32_t* __restrict__ sbits, Lattice L,
-                                    long long* __restrict__ list, long long cap, DevState* ds, int only_if_patching) {
+__global__ void list_unknown_kernel(uint32_t* __restrict__ ubits, uint32_t* __restrict__ sbits,
+                                    uint32_t* __restrict__ ebits, Lattice L, long long* __restrict__ list,
+                                    long long cap, DevState* ds, int only_if_patching) {
     if (only_if_patching && !ds->patching) return;
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < L.nwords; w += stride) {
@@ -82,6 +83,7 @@ __global__ void list_unknown_kernel(uint32_t* __restrict__ ubits, uint32_t* __re
         }
         ubits[w] = 0u;
         sbits[w] &= ~u;
+        if (ebits) ebits[w] |= u;  // these voxels are now decided by the exact winding number
         if (only_if_patching) atomicAdd(&ds->patched_voxels, (unsigned long long)n);
         else atomicAdd(&ds->fixup_voxels, (unsigned long long)n);
     }
@@ -273,11 +275,11 @@ __global__ void patch_mark_kernel(Lattice L, uint32_t* __restrict__ ubits, DevSt
 }  // namespace
 
 void launch_list_unknown(uint32_t* ubits, uint32_t* sbits, const Lattice& L, long long* list, long long cap,
-                         DevState* ds, int only_if_patching, cudaStream_t st) {
+                         DevState* ds, int only_if_patching, cudaStream_t st, uint32_t* ebits) {
     long long blocks = std::min<long long>((L.nwords + 255) / 256, 152LL * 16);
     if (blocks < 1) blocks = 1;
     GBSDF_COUNT_LAUNCH();
-    list_unknown_kernel<<<(unsigned)blocks, 256, 0, st>>>(ubits, sbits, L, list, cap, ds, only_if_patching);
+    list_unknown_kernel<<<(unsigned)blocks, 256, 0, st>>>(ubits, sbits, ebits, L, list, cap, ds, only_if_patching);
 }
 
 void launch_gwn(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,

@@ -15,13 +15,18 @@ OK, EINVAL, EGUARD, ECSR, EVERIFY, ENOMEM, ECUDA, ENODEV = range(8)
 STATUS_NAMES = {OK: "OK", EINVAL: "EINVAL", EGUARD: "EGUARD", ECSR: "ECSR", EVERIFY: "EVERIFY",
                 ENOMEM: "ENOMEM", ECUDA: "ECUDA", ENODEV: "ENODEV"}
 # gbsdf_mode / gbsdf_path
-MODE_REFERENCE, MODE_EXACT, MODE_EXACT_SIGNS = 0, 1, 2
+MODE_REFERENCE, MODE_EXACT, MODE_EXACT_SIGNS, MODE_LEARNED = 0, 1, 2, 3
 PATH_AUTO, PATH_FAST, PATH_LEGACY = 0, 1, 2
 
 
 class Options(C.Structure):
     _fields_ = [("mode", C.c_int32), ("path", C.c_int32), ("device", C.c_int32), ("tris_on_device", C.c_int32),
-                ("max_rounds", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("max_rounds", C.c_int32), ("mlp_budget", C.c_int32), ("mlp_threshold", C.c_float),
+                ("reserved0", C.c_int32), ("mlp_params", C.c_void_p), ("brick_scores", C.c_void_p),
+                ("reserved", C.c_int32 * 2)]
+
+
+MLP_PARAMS, MLP_FEATURES = 6337, 32
 
 
 class Stats(C.Structure):
@@ -35,7 +40,7 @@ class Stats(C.Structure):
                 ("safe_clamped", C.c_int64), ("patched_voxels", C.c_int64), ("fp64_rechecks", C.c_int64),
                 ("band_voxels", C.c_int64), ("splat_evals", C.c_int64), ("gwn_pairs", C.c_int64),
                 ("brick_pairs", C.c_int64), ("csr_entries", C.c_int64), ("kernel_launches", C.c_int64),
-                ("reserved", C.c_int64 * 7)]
+                ("proposed", C.c_int64), ("reserved", C.c_int64 * 6)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "pad0")}
@@ -50,6 +55,7 @@ class MeshDesc(C.Structure):
 # every exported symbol of include/gbsdf.h
 EXPORTS = ("gbsdf_default_options", "gbsdf_compute_mesh_sdf", "gbsdf_compute_mesh_sdf_batch",
            "gbsdf_mesh_lattice", "gbsdf_build_from_mesh",
+           "gbsdf_brick_features", "gbsdf_mlp_forward", "gbsdf_mlp_backward", "gbsdf_mlp_adam",
            "gbsdf_release_workspace", "gbsdf_legacy_sdf_noalloc", "gbsdf_selftest", "gbsdf_version")
 
 _lib = None
@@ -79,6 +85,18 @@ def load(path: Path | None = None):
                                         C.c_void_p, C.c_int32, C.POINTER(Options), C.POINTER(Stats), C.c_char_p,
                                         C.c_size_t]
     L.gbsdf_build_from_mesh.restype = C.c_int
+    L.gbsdf_brick_features.argtypes = [C.c_void_p, C.c_int64, C.c_float, i32p, i32p, C.c_int32, C.c_void_p,
+                                       C.c_int64, i32p, C.c_char_p, C.c_size_t]
+    L.gbsdf_brick_features.restype = C.c_int
+    L.gbsdf_mlp_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.c_char_p,
+                                    C.c_size_t]
+    L.gbsdf_mlp_forward.restype = C.c_int
+    L.gbsdf_mlp_backward.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                     C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t]
+    L.gbsdf_mlp_backward.restype = C.c_int
+    L.gbsdf_mlp_adam.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_float,
+                                 C.c_float, C.c_float, C.c_int32, C.c_int32, C.c_char_p, C.c_size_t]
+    L.gbsdf_mlp_adam.restype = C.c_int
     L.gbsdf_release_workspace.argtypes = [C.c_int32]
     L.gbsdf_release_workspace.restype = None
     L.gbsdf_legacy_sdf_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_float, i32p, i32p, C.c_void_p, C.c_int32,

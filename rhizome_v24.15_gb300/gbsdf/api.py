@@ -21,10 +21,12 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import MODE_EXACT, MODE_EXACT_SIGNS, MODE_REFERENCE, PATH_AUTO, PATH_FAST, PATH_LEGACY, STATUS_NAMES
+from ._lib import (MODE_EXACT, MODE_EXACT_SIGNS, MODE_LEARNED, MODE_REFERENCE, PATH_AUTO, PATH_FAST, PATH_LEGACY,
+                   STATUS_NAMES)
 
 __all__ = ["GbsdfError", "Result", "compute_mesh_sdf", "compute_mesh_sdf_batch", "mesh_lattice", "build_from_mesh", "CudaRasterizer",
-           "CudaVolumeGrid", "MODE_REFERENCE", "MODE_EXACT", "MODE_EXACT_SIGNS", "PATH_AUTO", "PATH_FAST", "PATH_LEGACY"]
+           "CudaVolumeGrid", "MODE_REFERENCE", "MODE_EXACT", "MODE_EXACT_SIGNS", "MODE_LEARNED", "PATH_AUTO", "PATH_FAST",
+           "PATH_LEGACY"]
 
 
 class GbsdfError(RuntimeError):
@@ -63,11 +65,54 @@ def _ptr_of(buf):
     raise TypeError(f"unsupported buffer type {type(buf)}")
 
 
+def _mlp_device_params(mlp_params, device):
+    """Device pointer (and the owning tensor) of the learned model's parameters: a CUDA
+    tensor is used as is, a host array is copied to ``device``, None loads the model
+    shipped with the package."""
+    import torch
+
+    if mlp_params is None:
+        from .learn import MODEL_PATH
+        mlp_params = np.load(MODEL_PATH)["params"]
+    if not isinstance(mlp_params, torch.Tensor):
+        mlp_params = torch.from_numpy(np.ascontiguousarray(mlp_params, np.float32)).to(f"cuda:{device}")
+    if not mlp_params.is_cuda or mlp_params.dtype != torch.float32 or mlp_params.numel() != _lib.MLP_PARAMS:
+        raise ValueError(f"mlp_params must be {_lib.MLP_PARAMS} float32 values")
+    mlp_params = mlp_params.contiguous()
+    return mlp_params.data_ptr(), mlp_params
+
+
+def _set_learned(o, mode, device, mlp_params, mlp_budget, mlp_threshold, brick_scores=None):
+    if int(mode) != MODE_LEARNED:
+        return None
+    if brick_scores is not None:
+        import torch
+
+        if not isinstance(brick_scores, torch.Tensor):
+            brick_scores = torch.from_numpy(np.ascontiguousarray(brick_scores, np.float32)).to(f"cuda:{device}")
+        if not brick_scores.is_cuda or brick_scores.dtype != torch.float32:
+            raise ValueError("brick_scores must be float32")
+        keep = brick_scores.contiguous()
+        o.brick_scores = keep.data_ptr()
+    else:
+        ptr, keep = _mlp_device_params(mlp_params, device)
+        o.mlp_params = ptr
+    if mlp_budget is not None:
+        o.mlp_budget = int(mlp_budget)
+    if mlp_threshold is not None:
+        o.mlp_threshold = float(mlp_threshold)
+    return keep
+
+
 def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE_REFERENCE, path=PATH_AUTO,
-                     device=0, max_rounds=0, raise_on_error=True):
+                     device=0, max_rounds=0, raise_on_error=True, mlp_params=None, mlp_budget=None,
+                     mlp_threshold=None, brick_scores=None):
     """Run the engine. ``tris``: (T,12) float32 numpy array (host) or CUDA tensor.
     ``out``: float32 buffer of N voxels (numpy = host, CUDA tensor = device); allocated
-    on the host when None. Returns ``(out, Result)``."""
+    on the host when None. ``MODE_LEARNED`` takes the sign-risk model's parameters
+    (``mlp_params``; the shipped model when None), the most bricks it may propose and the
+    probability threshold; ``brick_scores`` (one logit per 8^3 brick, x fastest) replaces
+    the network's scores. Returns ``(out, Result)``."""
     mn = np.asarray(min_coord, np.int64).reshape(3)
     mx = np.asarray(max_coord, np.int64).reshape(3)
     dims = mx - mn + 1
@@ -83,6 +128,7 @@ def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE
     L = _lib.load()
     L.gbsdf_default_options(C.byref(o))
     o.mode, o.path, o.device, o.tris_on_device, o.max_rounds = int(mode), int(path), int(device), int(tdev), int(max_rounds)
+    keep = _set_learned(o, mode, device, mlp_params, mlp_budget, mlp_threshold, brick_scores)  # noqa: F841
     st = _lib.Stats()
     err = C.create_string_buffer(512)
     rc = L.gbsdf_compute_mesh_sdf(tp, T, float(voxel_size), _i3(mn), _i3(mx), op, int(odev), C.byref(o),
@@ -94,7 +140,7 @@ def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE
 
 
 def compute_mesh_sdf_batch(meshes, outs=None, mode=MODE_REFERENCE, path=PATH_FAST, device=0,
-                           raise_on_error=True):
+                           raise_on_error=True, mlp_params=None, mlp_budget=None, mlp_threshold=None):
     """Batched build. ``meshes``: list of (tris, voxel_size, min_coord, max_coord); all
     triangles host arrays or all CUDA tensors; ``outs``: matching output buffers (host
     arrays allocated when None). Returns (outs, statuses, stats list, message)."""
@@ -127,6 +173,7 @@ def compute_mesh_sdf_batch(meshes, outs=None, mode=MODE_REFERENCE, path=PATH_FAS
     o = _lib.Options()
     L.gbsdf_default_options(C.byref(o))
     o.mode, o.path, o.device, o.tris_on_device = int(mode), int(path), int(device), int(bool(tdev))
+    keep_p = _set_learned(o, mode, device, mlp_params, mlp_budget, mlp_threshold)  # noqa: F841
     stats = (_lib.Stats * n)()
     err = C.create_string_buffer(512)
     rc = L.gbsdf_compute_mesh_sdf_batch(descs, n, int(bool(odev)), C.byref(o), stats, err, len(err))
