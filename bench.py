@@ -115,11 +115,69 @@ def whole_job_gvox(world: int, voxels_per_rank: int, ms_per_step: float) -> floa
     return world * voxels_per_rank / (ms_per_step * 1e-3) / 1e9
 
 
-def make_workload():
+def make_workload(dims=None, h=None):
     from gbsdf import meshgen
 
-    tris, mn, mx, h = meshgen.workload(WORKLOAD)
+    tris, mn, mx, h = meshgen.workload(WORKLOAD, dims=dims, h=h)
     return tris, mn, mx, h
+
+
+def run_batched(gbsdf, torch, dev, mode, steps, warmup, local):
+    """The 64-mesh batched workload: one planned batch (one CUDA graph per run) against
+    64 sequential single-mesh calls, device-resident triangles and outputs, timed on the
+    host around whole runs (each run returns after its last kernel)."""
+    from gbsdf import meshgen
+
+    meshes = meshgen.batch_workload()
+    dmeshes = [(torch.from_numpy(t).to(dev), h, mn, mx) for t, h, mn, mx in meshes]
+    outs = [torch.empty(int(np.prod(mx.astype(np.int64) - mn + 1)), dtype=torch.float32, device=dev)
+            for _, _, mn, mx in meshes]
+    vox = sum(int(o.numel()) for o in outs)
+    tris = sum(len(t) for t, _, _, _ in meshes)
+
+    def timed(fn, slow=False):
+        # the plain mode's patch boxes make some of these meshes cost seconds: fewer
+        # repetitions for those passes
+        w, k = (1, max(1, steps // 2)) if slow else (warmup, steps)
+        for _ in range(w):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / k * 1e3
+
+    res = {"workload": f"64 meshes (mug / vessel tree / perturbed sphere), {tris} triangles, cubic lattices "
+                       f"64^3-384^3, {vox} voxels, fast path, device buffers",
+           "voxels": vox}
+    launches = 0
+    for name, m in (("batched", mode), ("batched_plain", gbsdf.MODE_REFERENCE)):
+        with gbsdf.Batch(dmeshes, outs=outs, mode=m, device=local) as b:
+            st, stats = b.run()
+            ms = timed(b.run, slow=(m == gbsdf.MODE_REFERENCE))
+            if name == "batched":
+                launches = stats[0]["kernel_launches"]
+        # a mesh whose verification diverges is declined (the reference's fall-back case);
+        # it still costs its full build and is counted in the throughput
+        res[name] = {"value": vox / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms,
+                     "declined": sum(1 for x in st if x != 0)}
+
+    declined = []
+
+    def sequential(m):
+        declined.clear()
+        for (t, h, mn, mx), o in zip(dmeshes, outs):
+            _, r = gbsdf.compute_mesh_sdf(t, h, mn, mx, out=o, mode=m, path=gbsdf.PATH_FAST, device=local,
+                                          raise_on_error=False)
+            declined.append(not r.ok)
+
+    for name, m in (("sequential", mode), ("sequential_plain", gbsdf.MODE_REFERENCE)):
+        ms = timed(lambda: sequential(m), slow=(m == gbsdf.MODE_REFERENCE))
+        res[name] = {"value": vox / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms,
+                     "declined": int(sum(declined))}
+    res["graph_kernel_launches"] = launches
+    return res
 
 
 def cpu_baseline(tris, mn, mx, h, z_slab=64, threads=None):
@@ -171,9 +229,15 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--mode", default="exact-signs", choices=["reference", "exact-signs", "exact"])
+    ap.add_argument("--mode", default="exact-signs", choices=["reference", "exact-signs", "exact", "learned"])
     ap.add_argument("--ref-slab", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # profiling of a smaller lattice of the same mesh (never the reported configuration)
+    ap.add_argument("--dims", default=None, help="lattice override nx,ny,nz (profiling runs)")
+    ap.add_argument("--h", type=float, default=None, help="voxel size override (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-mode pass (profiling runs)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-mesh batched workload")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -199,9 +263,16 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    modes = {"reference": gbsdf.MODE_REFERENCE, "exact-signs": gbsdf.MODE_EXACT_SIGNS, "exact": gbsdf.MODE_EXACT}
+    modes = {"reference": gbsdf.MODE_REFERENCE, "exact-signs": gbsdf.MODE_EXACT_SIGNS, "exact": gbsdf.MODE_EXACT,
+             "learned": gbsdf.MODE_LEARNED}
     mode = modes[args.mode]
-    tris, mn, mx, h = make_workload()
+    dims_override = tuple(int(x) for x in args.dims.split(",")) if args.dims else None
+    tris, mn, mx, h = make_workload(dims_override, args.h)
+    mlp = None
+    if mode == gbsdf.MODE_LEARNED:
+        from gbsdf import learn
+
+        mlp = torch.from_numpy(np.load(learn.MODEL_PATH)["params"]).to(dev)
     dims = mx.astype(np.int64) - mn + 1
     N = int(np.prod(dims))
     T = len(tris)
@@ -210,7 +281,7 @@ def main():
 
     def step_device(m=mode):
         _, res = gbsdf.compute_mesh_sdf(tris_dev, h, mn, mx, out=out_dev, mode=m, path=gbsdf.PATH_FAST,
-                                        device=local)
+                                        device=local, mlp_params=mlp)
         return res
 
     def barrier():
@@ -235,7 +306,7 @@ def main():
 
     # the plain (reference-compatible) mode on the same lattice, same protocol
     plain = None
-    if args.mode != "reference":
+    if args.mode != "reference" and not args.no_plain:
         for _ in range(args.warmup):
             step_device(gbsdf.MODE_REFERENCE)
         barrier()
@@ -250,22 +321,26 @@ def main():
         plain = {"mode": "reference", "value": whole_job_gvox(world, N, pms), "ms_per_step": pms}
 
     # ---- end to end through the public API with pinned host buffers
-    tris_pin = torch.from_numpy(tris).pin_memory()
-    out_pin = torch.empty(N, dtype=torch.float32).pin_memory()
-    tris_np = tris_pin.numpy()
-    out_np = out_pin.numpy()
-    for _ in range(max(1, args.warmup // 2)):
-        gbsdf.compute_mesh_sdf(tris_np, h, mn, mx, out=out_np, mode=mode, path=gbsdf.PATH_FAST, device=local)
-    barrier()
-    e2 = torch.cuda.Event(enable_timing=True)
-    e3 = torch.cuda.Event(enable_timing=True)
-    e2.record()
-    for _ in range(args.steps):
-        gbsdf.compute_mesh_sdf(tris_np, h, mn, mx, out=out_np, mode=mode, path=gbsdf.PATH_FAST, device=local)
-    e3.record()
-    barrier()
-    e2e_ms = max_over_ranks(dist, e2.elapsed_time(e3) / args.steps)
-    e2e = whole_job_gvox(world, N, e2e_ms)
+    e2e = e2e_ms = None
+    if not args.no_e2e:
+        tris_pin = torch.from_numpy(tris).pin_memory()
+        out_pin = torch.empty(N, dtype=torch.float32).pin_memory()
+        tris_np = tris_pin.numpy()
+        out_np = out_pin.numpy()
+        for _ in range(max(1, args.warmup // 2)):
+            gbsdf.compute_mesh_sdf(tris_np, h, mn, mx, out=out_np, mode=mode, path=gbsdf.PATH_FAST, device=local,
+                                   mlp_params=mlp)
+        barrier()
+        e2 = torch.cuda.Event(enable_timing=True)
+        e3 = torch.cuda.Event(enable_timing=True)
+        e2.record()
+        for _ in range(args.steps):
+            gbsdf.compute_mesh_sdf(tris_np, h, mn, mx, out=out_np, mode=mode, path=gbsdf.PATH_FAST, device=local,
+                                   mlp_params=mlp)
+        e3.record()
+        barrier()
+        e2e_ms = max_over_ranks(dist, e2.elapsed_time(e3) / args.steps)
+        e2e = whole_job_gvox(world, N, e2e_ms)
 
     # ---- roofline of the dominant kernel (eikonal sweeps), events on the engine's stream
     s0 = stats[-1]
@@ -288,11 +363,12 @@ def main():
             "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{WORKLOAD}: procedural mug (cup of revolution + swept-torus handle), "
-                                   f"860x860x880 lattice at 0.1 mm, {T} triangles, fast path",
+                                   f"{'x'.join(str(int(d)) for d in dims)} lattice at {h:g} mm, {T} triangles, "
+                                   "fast path",
                        "mode": args.mode, "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (2.6 GB grid per step)"},
-            "e2e": {"value": e2e, "unit": UNIT, "ms_per_step": e2e_ms, "h2d_bytes_per_step": int(T * 48),
-                    "d2h_bytes_per_step": int(N * 4)},
+            "e2e": None if e2e is None else {"value": e2e, "unit": UNIT, "ms_per_step": e2e_ms,
+                                             "h2d_bytes_per_step": int(T * 48), "d2h_bytes_per_step": int(N * 4)},
             "roofline": {"kernel": "eikonal lockstep sweep (sweep_x/y/z)", "bound": "hbm", "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes,
@@ -306,6 +382,10 @@ def main():
             "plain": plain,
             "clocks": clk.summary(),
             "gpu_launches": int(sum(s["kernel_launches"] for s in stats))}
+    if mode == gbsdf.MODE_LEARNED:
+        line["pipeline"]["proposed_bricks"] = s0["proposed"]
+    if not args.no_batch and mode in (gbsdf.MODE_REFERENCE, gbsdf.MODE_EXACT_SIGNS):
+        line["batched"] = run_batched(gbsdf, torch, dev, mode, args.steps, args.warmup, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, dt, desc, threads = cpu_baseline(tris, mn, mx, h)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc,

@@ -159,12 +159,31 @@ typedef struct gbsdf_mesh_desc {
 } gbsdf_mesh_desc;
 
 /* Batched form of gbsdf_compute_mesh_sdf (the descriptor list of the reference-side
- * C ABI plan): meshes of uneven size share one device workspace sized for the largest
- * and run back to back on one stream. Returns GBSDF_OK when every mesh succeeded, else
+ * C ABI plan). With the fast path (opt->path == GBSDF_PATH_FAST) in reference or
+ * exact-signs mode the meshes run as one planned batch (gbsdf_batch_create / _run /
+ * _destroy below, one CUDA graph, every mesh its own branch); otherwise they run back to
+ * back through gbsdf_compute_mesh_sdf. Returns GBSDF_OK when every mesh succeeded, else
  * the first failing mesh's status; per-mesh statuses are written to meshes[i].status and
- * per-mesh statistics to stats[i] (stats may be NULL). */
+ * per-mesh statistics to stats[i] (stats may be NULL). A failing mesh's output is left
+ * untouched. No reference counterpart. */
 int gbsdf_compute_mesh_sdf_batch(gbsdf_mesh_desc* meshes, int32_t n_meshes, int32_t out_on_device,
                                  const gbsdf_options* opt, gbsdf_stats* stats, char* err, size_t errlen);
+
+/* A planned batch: the meshes' device buffers are sized from one counting pass, and the
+ * whole build of every mesh -- upload, binning, splat, parity, exact-winding fixup,
+ * eikonal rounds, verify / patch, sign apply, download -- is captured once as a CUDA
+ * graph with no host round trip inside, one independent branch per mesh. A run replays
+ * the graph: the descriptors' pointers and lattices are fixed at creation, their
+ * triangle contents may change between runs (a run whose counts outgrow the planned
+ * lists re-plans itself and runs again). Fast path only; opt->mode must be
+ * GBSDF_MODE_REFERENCE or GBSDF_MODE_EXACT_SIGNS. No reference counterpart. */
+typedef struct gbsdf_batch gbsdf_batch;
+int gbsdf_batch_create(const gbsdf_mesh_desc* meshes, int32_t n_meshes, int32_t out_on_device,
+                       const gbsdf_options* opt, gbsdf_batch** batch, char* err, size_t errlen);
+/* statuses[i] / stats[i] receive each mesh's gbsdf_status / statistics (either may be
+ * NULL); returns GBSDF_OK when every mesh succeeded, else the first failing status. */
+int gbsdf_batch_run(gbsdf_batch* batch, int32_t* statuses, gbsdf_stats* stats, char* err, size_t errlen);
+void gbsdf_batch_destroy(gbsdf_batch* batch);
 
 /* Lattice of CudaRasterizer::build_from_mesh (cuda_rasterizer.cu:1354-1372): bounding box
  * of all vertices, padded by 10 voxels, floor/ceil onto the voxel lattice. */

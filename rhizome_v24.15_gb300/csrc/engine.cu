@@ -33,6 +33,23 @@ unsigned long long& launch_counter() {
     return n;
 }
 
+Lattice make_lattice(const int32_t mn[3], const int32_t mx[3], float h) {
+    Lattice L{};
+    for (int k = 0; k < 3; ++k) {
+        L.mn[k] = mn[k];
+        L.dims[k] = mx[k] - mn[k] + 1;
+    }
+    L.h = h;
+    L.N = (long long)L.dims[0] * L.dims[1] * L.dims[2];
+    L.wx = (L.dims[0] + 31) / 32;
+    L.nwords = (long long)L.wx * L.dims[1] * L.dims[2];
+    for (int k = 0; k < 3; ++k) L.nb[k] = (L.dims[k] + kBrick - 1) / kBrick;
+    L.nbricks = (long long)L.nb[0] * L.nb[1] * L.nb[2];
+    L.nsx = (L.dims[0] + kStrip - 1) / kStrip;
+    L.nstrips = (long long)L.nsx * L.dims[1];
+    return L;
+}
+
 namespace {
 
 struct Buf {
@@ -137,23 +154,6 @@ void free_ws(Workspace& w) {
     w.st = nullptr;
     for (auto& ev : w.ev) ev = nullptr;
     w.device = -1;
-}
-
-Lattice make_lattice(const int32_t mn[3], const int32_t mx[3], float h) {
-    Lattice L{};
-    for (int k = 0; k < 3; ++k) {
-        L.mn[k] = mn[k];
-        L.dims[k] = mx[k] - mn[k] + 1;
-    }
-    L.h = h;
-    L.N = (long long)L.dims[0] * L.dims[1] * L.dims[2];
-    L.wx = (L.dims[0] + 31) / 32;
-    L.nwords = (long long)L.wx * L.dims[1] * L.dims[2];
-    for (int k = 0; k < 3; ++k) L.nb[k] = (L.dims[k] + kBrick - 1) / kBrick;
-    L.nbricks = (long long)L.nb[0] * L.nb[1] * L.nb[2];
-    L.nsx = (L.dims[0] + kStrip - 1) / kStrip;
-    L.nstrips = (long long)L.nsx * L.dims[1];
-    return L;
 }
 
 float ev_ms(cudaEvent_t a, cudaEvent_t b) {
@@ -613,6 +613,16 @@ int gbsdf_compute_mesh_sdf_batch(gbsdf_mesh_desc* meshes, int32_t n_meshes, int3
     gbsdf_options o;
     gbsdf_default_options(&o);
     if (opt) o = *opt;
+    if (o.path == GBSDF_PATH_FAST && (o.mode == GBSDF_MODE_REFERENCE || o.mode == GBSDF_MODE_EXACT_SIGNS)) {
+        gbsdf_batch* b = nullptr;
+        int rc = gbsdf_batch_create(meshes, n_meshes, out_on_device, &o, &b, err, errlen);
+        if (rc != GBSDF_OK) return rc;
+        std::vector<int32_t> st(n_meshes, GBSDF_ECUDA);
+        rc = gbsdf_batch_run(b, st.data(), stats, err, errlen);
+        gbsdf_batch_destroy(b);
+        for (int32_t i = 0; i < n_meshes; ++i) meshes[i].status = st[i];
+        return rc;
+    }
     int first_bad = GBSDF_OK;
     char one[256];
     for (int32_t i = 0; i < n_meshes; ++i) {

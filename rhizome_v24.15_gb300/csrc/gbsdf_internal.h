@@ -62,6 +62,7 @@ struct DevState {
     unsigned long long far_residual;
     unsigned long long safe_clamped;
     unsigned long long patched_voxels;
+    unsigned long long overflow;       // a list outgrew the capacity planned for it (batches)
     int changed[64];                   // per eikonal round
     int stop;                          // eikonal converged flag
     int rounds;
@@ -72,7 +73,7 @@ struct DevState {
     int total_sites;
     int patch_rounds;
     unsigned proposed;                 // learned mode: bricks the network proposed
-    unsigned pad_;
+    int abort_;                        // batches: the build failed a check, write no output
     long long sites[4096];
 };
 
@@ -85,6 +86,9 @@ constexpr int kMlpIn = 32, kMlpHidden = 64;
 constexpr int kMlpParams = kMlpHidden * kMlpIn + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;
 constexpr int kMlpBwdSamples = 64;            // samples per CTA of the backward pass
 
+// The lattice of [min, max] at voxel size h, with its sign-word, brick and strip counts.
+Lattice make_lattice(const int32_t mn[3], const int32_t mx[3], float h);
+
 // Kernel launches issued by this library (all launchers count themselves).
 unsigned long long& launch_counter();
 #define GBSDF_COUNT_LAUNCH() (++::gbsdf::launch_counter())
@@ -95,13 +99,19 @@ void launch_prep(const float* tris12, long long T, const Lattice& L, SplatTri* s
 void launch_exclusive_scan(const unsigned* in, unsigned long long* out, long long n, unsigned long long* tmp,
                            long long tmp_elems, cudaStream_t st);
 long long scan_tmp_elems(long long n);
+// With `ds`, the pair lists are known to hold `cap_b` / `cap_s` entries: when the counts
+// of this build exceed them the fill writes nothing and sets ds->overflow (the splat and
+// parity passes then skip the build).
 void launch_bin_fill(const SplatTri* stt, const ParTri* ptt, long long T, const Lattice& L,
                      const unsigned long long* brick_off, unsigned* brick_cur, unsigned* brick_list,
                      const unsigned long long* strip_off, unsigned* strip_cur, unsigned* strip_list,
-                     cudaStream_t st);
+                     cudaStream_t st, DevState* ds = nullptr, unsigned long long cap_b = ~0ull,
+                     unsigned long long cap_s = ~0ull);
 void launch_active_bricks(const unsigned* brick_count, long long nbricks, unsigned* active, DevState* ds,
                           cudaStream_t st);
 void launch_fill(float* g, long long n, float value, cudaStream_t st);
+// n_active < 0: the active-brick count is read on the device (one CTA per brick of the
+// lattice is launched and the surplus exits), so the launch needs no host round trip.
 void launch_splat(const SplatTri* stt, const unsigned long long* brick_off, const unsigned* brick_count,
                   const unsigned* brick_list, const unsigned* active, long long n_active, const Lattice& L,
                   float* dist, DevState* ds, cudaStream_t st);
@@ -117,6 +127,14 @@ void launch_list_unknown(uint32_t* ubits, uint32_t* sbits, const Lattice& L, lon
 void launch_gwn(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
                 int consumer, int only_if, uint32_t* sbits, long long* recheck, long long recheck_cap,
                 const float* dist, int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st);
+// Persistent exact-winding pass over a device-sized list, 32 threads per voxel (any list
+// length, no host round trip).
+void launch_gwn_team(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
+                     int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, const float* dist,
+                     int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st);
+// Batches: decides on the device whether the build passed its checks (valid triangles,
+// the reference's CSR guard when `csr_guard`, no list overflow); sets ds->abort_ if not.
+void launch_batch_finalize(DevState* ds, int csr_guard, cudaStream_t st);
 void launch_gwn_recheck(const float* tri9, long long T, const Lattice& L, const long long* recheck,
                         long long recheck_cap, int consumer, uint32_t* sbits, DevState* ds, int num_sms,
                         cudaStream_t st);

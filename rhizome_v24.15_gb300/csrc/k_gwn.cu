@@ -299,6 +299,15 @@ void launch_gwn(const float* tri9, long long T, const Lattice& L, const long lon
     }
 }
 
+void launch_gwn_team(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
+                     int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, const float* dist,
+                     int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st) {
+    GBSDF_COUNT_LAUNCH();
+    gwn_kernel<32><<<(unsigned)(num_sms * 8), kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, 0, sbits,
+                                                                     recheck, recheck_cap, dist, dist_sq,
+                                                                     surf_tol_vox, ds);
+}
+
 void launch_gwn_small(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
                       int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, const float* dist,
                       int dist_sq, float surf_tol_vox, DevState* ds, long long n_hint, cudaStream_t st) {

@@ -206,4 +206,16 @@ void launch_iota(long long* list, long long n, long long from, cudaStream_t st) 
     iota_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(list, n, from);
 }
 
+namespace {
+__global__ void batch_finalize_kernel(DevState* ds, int csr_guard) {
+    const bool csr_bad = csr_guard && (ds->csr_entries == 0ull || ds->csr_entries > 100000000ull);
+    if (ds->invalid_tris > 0ull || csr_bad || ds->overflow) ds->abort_ = 1;
+}
+}  // namespace
+
+void launch_batch_finalize(DevState* ds, int csr_guard, cudaStream_t st) {
+    GBSDF_COUNT_LAUNCH();
+    batch_finalize_kernel<<<1, 1, 0, st>>>(ds, csr_guard);
+}
+
 }  // namespace gbsdf

@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kParWarps * 32) parity_kernel(const ParTri* __
     extern __shared__ float s_hits[];  // [kParWarps][kParityMaxHits][32] floats, then signs
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long strip = (long long)blockIdx.x * kParWarps + warp;
-    if (strip >= L.nstrips) return;  // whole warp leaves; no block barrier below
+    if (strip >= L.nstrips || ds->overflow) return;  // whole warp leaves; no block barrier below
     float* hits = s_hits + (size_t)warp * kParityMaxHits * 32;
     signed char* hsg = reinterpret_cast<signed char*>(s_hits + (size_t)kParWarps * kParityMaxHits * 32) +
                        (size_t)warp * kParityMaxHits * 32;

@@ -171,9 +171,14 @@ __global__ void __launch_bounds__(kPrepThreads) bin_fill_kernel(
     const SplatTri* __restrict__ stt, const ParTri* __restrict__ ptt, long long T, Lattice L,
     const unsigned long long* __restrict__ brick_off, unsigned* __restrict__ brick_cur,
     unsigned* __restrict__ brick_list, const unsigned long long* __restrict__ strip_off,
-    unsigned* __restrict__ strip_cur, unsigned* __restrict__ strip_list) {
+    unsigned* __restrict__ strip_cur, unsigned* __restrict__ strip_list, DevState* ds, unsigned long long cap_b,
+    unsigned long long cap_s) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T) return;
+    if (ds && (ds->brick_pairs > cap_b || ds->strip_pairs > cap_s)) {  // planned lists too small
+        if (t == 0) ds->overflow = 1;
+        return;
+    }
     const float bw = (float)kBandVoxels * L.h;
     SplatTri s = stt[t];
     if (s.valid) {
@@ -295,6 +300,7 @@ __global__ void __launch_bounds__(kSplatThreads) splat_kernel(
     const unsigned* __restrict__ list, const unsigned* __restrict__ active, Lattice L, float* __restrict__ dist,
     DevState* ds) {
     __shared__ SplatTri s[kSplatChunk];
+    if (blockIdx.x >= ds->active_bricks || ds->overflow) return;
     const unsigned b = active[blockIdx.x];
     const int nbx = L.nb[0], nby = L.nb[1];
     const int bx = (int)(b % (unsigned)nbx), by = (int)((b / (unsigned)nbx) % (unsigned)nby),
@@ -399,11 +405,11 @@ void launch_exclusive_scan(const unsigned* in, unsigned long long* out, long lon
 void launch_bin_fill(const SplatTri* stt, const ParTri* ptt, long long T, const Lattice& L,
                      const unsigned long long* brick_off, unsigned* brick_cur, unsigned* brick_list,
                      const unsigned long long* strip_off, unsigned* strip_cur, unsigned* strip_list,
-                     cudaStream_t st) {
+                     cudaStream_t st, DevState* ds, unsigned long long cap_b, unsigned long long cap_s) {
     if (T <= 0) return;
     GBSDF_COUNT_LAUNCH();
     bin_fill_kernel<<<(unsigned)((T + kPrepThreads - 1) / kPrepThreads), kPrepThreads, 0, st>>>(
-        stt, ptt, T, L, brick_off, brick_cur, brick_list, strip_off, strip_cur, strip_list);
+        stt, ptt, T, L, brick_off, brick_cur, brick_list, strip_off, strip_cur, strip_list, ds, cap_b, cap_s);
 }
 
 void launch_active_bricks(const unsigned* brick_count, long long nbricks, unsigned* active, DevState* ds,
@@ -425,10 +431,11 @@ void launch_fill(float* g, long long n, float value, cudaStream_t st) {
 void launch_splat(const SplatTri* stt, const unsigned long long* brick_off, const unsigned* brick_count,
                   const unsigned* brick_list, const unsigned* active, long long n_active, const Lattice& L,
                   float* dist, DevState* ds, cudaStream_t st) {
-    if (n_active <= 0) return;
+    const long long blocks = n_active < 0 ? L.nbricks : n_active;
+    if (blocks <= 0) return;
     GBSDF_COUNT_LAUNCH();
-    splat_kernel<<<(unsigned)n_active, kSplatThreads, 0, st>>>(stt, brick_off, brick_count, brick_list, active, L,
-                                                               dist, ds);
+    splat_kernel<<<(unsigned)blocks, kSplatThreads, 0, st>>>(stt, brick_off, brick_count, brick_list, active, L,
+                                                             dist, ds);
 }
 
 }  // namespace gbsdf

@@ -56,6 +56,7 @@ class MeshDesc(C.Structure):
 EXPORTS = ("gbsdf_default_options", "gbsdf_compute_mesh_sdf", "gbsdf_compute_mesh_sdf_batch",
            "gbsdf_mesh_lattice", "gbsdf_build_from_mesh",
            "gbsdf_brick_features", "gbsdf_mlp_forward", "gbsdf_mlp_backward", "gbsdf_mlp_adam",
+           "gbsdf_batch_create", "gbsdf_batch_run", "gbsdf_batch_destroy",
            "gbsdf_release_workspace", "gbsdf_legacy_sdf_noalloc", "gbsdf_selftest", "gbsdf_version")
 
 _lib = None
@@ -97,6 +98,13 @@ def load(path: Path | None = None):
     L.gbsdf_mlp_adam.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_float,
                                  C.c_float, C.c_float, C.c_int32, C.c_int32, C.c_char_p, C.c_size_t]
     L.gbsdf_mlp_adam.restype = C.c_int
+    L.gbsdf_batch_create.argtypes = [C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.POINTER(Options),
+                                     C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]
+    L.gbsdf_batch_create.restype = C.c_int
+    L.gbsdf_batch_run.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(Stats), C.c_char_p, C.c_size_t]
+    L.gbsdf_batch_run.restype = C.c_int
+    L.gbsdf_batch_destroy.argtypes = [C.c_void_p]
+    L.gbsdf_batch_destroy.restype = None
     L.gbsdf_release_workspace.argtypes = [C.c_int32]
     L.gbsdf_release_workspace.restype = None
     L.gbsdf_legacy_sdf_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_float, i32p, i32p, C.c_void_p, C.c_int32,

@@ -24,7 +24,7 @@ from . import _lib
 from ._lib import (MODE_EXACT, MODE_EXACT_SIGNS, MODE_LEARNED, MODE_REFERENCE, PATH_AUTO, PATH_FAST, PATH_LEGACY,
                    STATUS_NAMES)
 
-__all__ = ["GbsdfError", "Result", "compute_mesh_sdf", "compute_mesh_sdf_batch", "mesh_lattice", "build_from_mesh", "CudaRasterizer",
+__all__ = ["GbsdfError", "Result", "Batch", "compute_mesh_sdf", "compute_mesh_sdf_batch", "mesh_lattice", "build_from_mesh", "CudaRasterizer",
            "CudaVolumeGrid", "MODE_REFERENCE", "MODE_EXACT", "MODE_EXACT_SIGNS", "MODE_LEARNED", "PATH_AUTO", "PATH_FAST",
            "PATH_LEGACY"]
 
@@ -181,6 +181,75 @@ def compute_mesh_sdf_batch(meshes, outs=None, mode=MODE_REFERENCE, path=PATH_FAS
     if rc != _lib.OK and raise_on_error:
         raise GbsdfError(rc, err.value.decode(errors="replace"))
     return outs, statuses, [s.as_dict() for s in stats], err.value.decode(errors="replace")
+
+
+class Batch:
+    """A planned batch (gbsdf_batch_create): the meshes' buffers are sized once and the
+    whole build of every mesh is one CUDA graph; ``run()`` replays it. ``meshes``: list
+    of (tris, voxel_size, min_coord, max_coord) with all triangles host arrays or all
+    CUDA tensors; ``outs``: matching float32 outputs (host arrays allocated when None).
+    The arrays are referenced, not copied: their contents may change between runs, their
+    sizes may not."""
+
+    def __init__(self, meshes, outs=None, mode=MODE_REFERENCE, device=0):
+        n = len(meshes)
+        self.n = n
+        self._descs = (_lib.MeshDesc * n)()
+        self._keep = []
+        if outs is None:
+            outs = [np.empty(int(np.prod(np.asarray(mx, np.int64) - np.asarray(mn, np.int64) + 1)), np.float32)
+                    for _, _, mn, mx in meshes]
+        self.outs = outs
+        tdev = odev = None
+        for i, ((tris, h, mn, mx), out) in enumerate(zip(meshes, outs)):
+            tp, td = _ptr_of(tris)
+            op, od = _ptr_of(out)
+            if tdev is None:
+                tdev, odev = td, od
+            if td != tdev or od != odev:
+                raise ValueError("all triangles (and all outputs) must be on the same side")
+            self._keep.append((tris, out))
+            d = self._descs[i]
+            d.tris, d.n_tris, d.voxel_size, d.out = tp, int(tris.shape[0]), float(h), op
+            for k in range(3):
+                d.min_coord[k] = int(np.asarray(mn).reshape(3)[k])
+                d.max_coord[k] = int(np.asarray(mx).reshape(3)[k])
+        L = _lib.load()
+        o = _lib.Options()
+        L.gbsdf_default_options(C.byref(o))
+        o.mode, o.path, o.device, o.tris_on_device = int(mode), int(PATH_FAST), int(device), int(bool(tdev))
+        self._h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        rc = L.gbsdf_batch_create(self._descs, n, int(bool(odev)), C.byref(o), C.byref(self._h), err, len(err))
+        if rc != _lib.OK:
+            raise GbsdfError(rc, err.value.decode(errors="replace"))
+
+    def run(self, raise_on_error=False):
+        """Replays the batch: returns (statuses, per-mesh stats dicts)."""
+        st = (C.c_int32 * self.n)()
+        stats = (_lib.Stats * self.n)()
+        err = C.create_string_buffer(512)
+        rc = _lib.load().gbsdf_batch_run(self._h, st, stats, err, len(err))
+        if rc != _lib.OK and raise_on_error:
+            raise GbsdfError(rc, err.value.decode(errors="replace"))
+        return list(st), [s.as_dict() for s in stats]
+
+    def close(self):
+        if self._h:
+            _lib.load().gbsdf_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def mesh_lattice(vertices, voxel_size):

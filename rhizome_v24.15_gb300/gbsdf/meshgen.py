@@ -39,6 +39,7 @@ __all__ = [
     "signed_volume",
     "to_triangles",
     "workload",
+    "batch_workload",
     "WORKLOADS",
 ]
 
@@ -429,6 +430,38 @@ WORKLOADS = {
     "vessel_c3_512": (dict(kind="vessel", seed=3), (512, 512, 512), 0.15),
     "blob_c5_1024": (dict(kind="blob", seed=5), (1024, 1024, 1024), 0.1),
 }
+
+
+def batch_workload(seed: int = 4, n: int = 64, t_lo: float = 2000.0, t_hi: float = 300000.0, g_lo: int = 64,
+                   g_hi: int = 384):
+    """Batched workload: ``n`` meshes cycling through the mug, vessel-tree and perturbed-
+    sphere generators, triangle counts log-uniform in [t_lo, t_hi], cubic lattices with
+    edges uniform in [g_lo, g_hi] and the mesh spanning 90% of its lattice (voxel size 1).
+    Returns a list of (tris, voxel_size, min_coord, max_coord)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        t = float(np.exp(rng.uniform(math.log(t_lo), math.log(t_hi))))
+        g = int(rng.integers(g_lo, g_hi + 1))
+        s = int(rng.integers(1 << 30))
+        kind = i % 3
+        if kind == 0:
+            f = math.sqrt(t / 23300.0)
+            v, fc = mug(segments=max(16, round(256 * f)), n_bottom=max(1, round(6 * f)), n_wall=max(2, round(14 * f)),
+                        n_rim=max(1, round(2 * f)), handle_path=max(8, round(28 * f)),
+                        handle_around=max(8, round(32 * f)))
+        elif kind == 1:
+            levels = int(np.clip(round(math.log2(max(t, 1.0) / 3000.0)), 1, 6))
+            per = t / (2 ** (levels + 1) - 1)
+            k = max(1.0, math.sqrt(per / 40.0))
+            v, fc = vessel_tree(seed=s, levels=levels, around=max(8, round(4 * k)), n_len=max(2, round(3 * k)),
+                                n_cap=max(1, round(k)), defects=False)
+        else:
+            nl = max(8, round(math.sqrt(t / 4.0)))
+            v, fc = perturbed_sphere(seed=s, n_lat=nl, n_lon=2 * nl)
+        vf, mn, mx = fit_to_lattice(v, (g, g, g), 1.0, span=0.9)
+        out.append((to_triangles(vf, fc), 1.0, mn, mx))
+    return out
 
 
 def _generate(kind, **kw):

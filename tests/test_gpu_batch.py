@@ -46,3 +46,56 @@ def test_batch_device_buffers_and_bad_member(engine):
     assert torch.all(outs[1] == 5.0)
     ref, _ = engine.compute_mesh_sdf(meshes[2][0], *meshes[2][1:], path=engine.PATH_FAST)
     assert np.array_equal(outs[2].cpu().numpy(), ref)
+
+
+def test_planned_batch_replays_and_follows_new_contents(engine):
+    """A planned batch replays its graph: the same contents give the same grids, new
+    contents of the same size give the new grids, and contents whose pair lists outgrow
+    the plan make the run re-plan itself."""
+    meshes = _meshes()
+    with engine.Batch(meshes) as b:
+        st, stats = b.run()
+        assert st == [0, 0, 0]
+        first = [o.copy() for o in b.outs]
+        st, _ = b.run()
+        assert st == [0, 0, 0]
+        for a, o in zip(first, b.outs):
+            assert np.array_equal(a.view(np.uint32), o.view(np.uint32))
+        # new contents in place: shift mesh 0 by a fraction of a voxel, grow mesh 2
+        t0, h0, mn0, mx0 = meshes[0]
+        t0[:, 0:9] += np.float32(0.37 * h0)
+        t2, h2, mn2, mx2 = meshes[2]
+        c = t2[:, 0:9].reshape(-1, 3).mean(0)
+        v = t2[:, 0:9].reshape(-1, 3)
+        t2[:, 0:9] = ((v - c) * np.float32(1.35) + c).reshape(-1, 9)
+        st, _ = b.run()
+        assert st == [0, 0, 0]
+        for (tris, h, mn, mx), got in zip(meshes, b.outs):
+            ref, _ = engine.compute_mesh_sdf(tris, h, mn, mx, path=engine.PATH_FAST)
+            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def test_planned_batch_exact_signs_and_device_buffers(engine):
+    import torch
+
+    meshes = _meshes()
+    dev = [(torch.from_numpy(t).cuda(), h, mn, mx) for t, h, mn, mx in meshes]
+    outs = [torch.empty(int(np.prod(mx.astype(np.int64) - mn + 1)), device="cuda") for _, _, mn, mx in meshes]
+    with engine.Batch(dev, outs=outs, mode=engine.MODE_EXACT_SIGNS) as b:
+        st, stats = b.run()
+        assert st == [0, 0, 0]
+        assert stats[0]["kernel_launches"] > 0
+    for (tris, h, mn, mx), got in zip(meshes, outs):
+        ref, _ = engine.compute_mesh_sdf(tris, h, mn, mx, mode=engine.MODE_EXACT_SIGNS, path=engine.PATH_FAST)
+        assert np.array_equal(got.cpu().numpy().view(np.uint32), ref.view(np.uint32))
+
+
+def test_planned_batch_bad_lattice_member(engine):
+    meshes = _meshes()
+    t, h, mn, mx = meshes[1]
+    bad = (t, h, mx, mn)  # max < min: empty lattice
+    outs = [np.full(int(np.prod(mx.astype(np.int64) - mn + 1)), 7.0, np.float32) for _, _, mn, mx in meshes]
+    with engine.Batch([meshes[0], bad, meshes[2]], outs=outs) as b:
+        st, _ = b.run()
+    assert st[0] == 0 and st[1] == 1 and st[2] == 0
+    assert np.all(outs[1] == 7.0)
