@@ -248,7 +248,9 @@ int gbsdf_legacy_sdf_noalloc(const gbsdf_tri* tris_dev, int64_t n_tris, float vo
 
 /* Engine self-tests (no counterpart in the reference). which = 0: the correctly rounded
  * division by 3 used by the eikonal update is compared with the IEEE quotient for every
- * non-NaN float input; *result = number of mismatches (0 expected). */
+ * non-NaN float input; which = 1: the x sweep's TMA tile layout (32-byte swizzle,
+ * out-of-lattice fill) is checked element by element on five boxes of a test grid.
+ * *result = number of mismatches (0 expected). */
 int gbsdf_selftest(int32_t which, int32_t device, uint64_t* result, char* err, size_t errlen);
 
 /* Library version string. */

@@ -88,6 +88,7 @@ struct Job {
     float* hout = nullptr;
     DevState* hs = nullptr;
     cudaStream_t st = nullptr;
+    GridMap map_a{}, map_b{};  // TMA descriptors of A and B
 };
 
 // Carves aligned sub-buffers out of one allocation: a sizing pass, then a placing pass.
@@ -206,7 +207,7 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
     for (int r = 0; r < kMaxRounds; ++r) {
         for (int axis = 0; axis < 3; ++axis)
             for (int dir = 1; dir >= -1; dir -= 2) {
-                launch_sweep(0, axis, dir, r, src, dst, L, j.ds, st);
+                launch_sweep(0, axis, dir, r, src, dst, L, j.ds, st, src == j.A ? &j.map_a : &j.map_b);
                 std::swap(src, dst);
             }
         launch_end_round(r, r, kMaxRounds, j.ds, st);
@@ -254,7 +255,11 @@ int plan(gbsdf_batch& b, BErr& e) {
     GBB_CK(cudaMalloc(&b.arena1, std::max<size_t>(c1.off, 256)));
     Carver p1{static_cast<char*>(b.arena1), 0};
     for (Job& j : b.jobs)
-        if (j.pre_status == GBSDF_OK) place_phase1(j, p1);
+        if (j.pre_status == GBSDF_OK) {
+            place_phase1(j, p1);
+            encode_grid_map(j.map_a, j.A, j.L);
+            encode_grid_map(j.map_b, j.B, j.L);
+        }
     // counting pass
     for (Job& j : b.jobs) {
         if (j.pre_status != GBSDF_OK) continue;
@@ -332,6 +337,7 @@ int status_of(const gbsdf_batch& b, const Job& j, bool& overflow) {
         overflow = true;
         return GBSDF_ECUDA;
     }
+    if (h.wait_timeouts) return GBSDF_ECUDA;
     if (h.invalid_tris > 0) return GBSDF_EINVAL;
     if (h.csr_entries == 0 || h.csr_entries > 100000000ull) return GBSDF_ECSR;
     if (h.verify_state != 1) return GBSDF_EVERIFY;

@@ -309,11 +309,16 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     const int rule = ref_eikonal ? 0 : 1;
     float* src = P<float>(w.A);
     float* dst = P<float>(w.B);
+    // TMA descriptors of the two grid copies for the staged x sweeps
+    GridMap map_a, map_b;
+    encode_grid_map(map_a, P<float>(w.A), L);
+    encode_grid_map(map_b, P<float>(w.B), L);
+    auto map_of = [&](const float* p) { return p == P<float>(w.A) ? &map_a : &map_b; };
     if (ref_eikonal) {
         for (int r = 0; r < kMaxRounds; ++r) {
             for (int axis = 0; axis < 3; ++axis)
                 for (int dir = 1; dir >= -1; dir -= 2) {
-                    launch_sweep(rule, axis, dir, r, src, dst, L, w.ds, st);
+                    launch_sweep(rule, axis, dir, r, src, dst, L, w.ds, st, map_of(src));
                     std::swap(src, dst);
                 }
             launch_end_round(r, r, kMaxRounds, w.ds, st);
@@ -326,7 +331,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
                 GB_CK(cudaMemsetAsync(&w.ds->changed[r % 64], 0, sizeof(int), st));
                 for (int axis = 0; axis < 3; ++axis)
                     for (int dir = 1; dir >= -1; dir -= 2) {
-                        launch_sweep(rule, axis, dir, r % 64, src, dst, L, w.ds, st);
+                        launch_sweep(rule, axis, dir, r % 64, src, dst, L, w.ds, st, map_of(src));
                         std::swap(src, dst);
                     }
                 launch_end_round(r % 64, r, cap, w.ds, st);
@@ -407,6 +412,8 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     GB_CK(cudaStreamSynchronize(st));
     const DevState& h = *w.hs;
     int status = GBSDF_OK;
+    if (h.wait_timeouts) return e.set(GBSDF_ECUDA, "%llu staged-tile waits of the eikonal sweeps timed out",
+                                      (unsigned long long)h.wait_timeouts);
     if (h.verify_state != 1) status = e.set(GBSDF_EVERIFY, "sign verification diverged: %d mismatches in probe %d",
                                             h.probe_m, h.probes - 1);
     if (status == GBSDF_OK && !out_dev) {
@@ -825,7 +832,7 @@ int gbsdf_selftest(int32_t which, int32_t device, uint64_t* result, char* err, s
     Err e{err, errlen};
     if (err && errlen) err[0] = 0;
     if (!result) return e.set(GBSDF_EINVAL, "null result");
-    if (which != 0) return e.set(GBSDF_EINVAL, "unknown self-test %d", which);
+    if (which != 0 && which != 1) return e.set(GBSDF_EINVAL, "unknown self-test %d", which);
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) {
         cudaGetLastError();
@@ -836,8 +843,13 @@ int gbsdf_selftest(int32_t which, int32_t device, uint64_t* result, char* err, s
     GB_CK(cudaMalloc(&d, sizeof(unsigned long long)));
     cudaError_t rc = cudaMemset(d, 0, sizeof(unsigned long long));
     if (rc == cudaSuccess) {
-        launch_selftest_div3(d, 0);
-        rc = cudaGetLastError();
+        if (which == 0) {
+            launch_selftest_div3(d, 0);
+            rc = cudaGetLastError();
+        } else if (selftest_tma_tile(d) != 0) {
+            cudaFree(d);
+            return e.set(GBSDF_ECUDA, "TMA tile self-test could not run (no tensor-map encoder or copy failed)");
+        }
     }
     unsigned long long h = 0;
     if (rc == cudaSuccess) rc = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);

@@ -2,6 +2,7 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace gbsdf {
@@ -63,6 +64,7 @@ struct DevState {
     unsigned long long safe_clamped;
     unsigned long long patched_voxels;
     unsigned long long overflow;       // a list outgrew the capacity planned for it (batches)
+    unsigned long long wait_timeouts;  // bounded waits (TMA tiles) that gave up
     int changed[64];                   // per eikonal round
     int stop;                          // eikonal converged flag
     int rounds;
@@ -142,8 +144,20 @@ void launch_verify_prepare(const Lattice& L, int gen, const uint32_t* ubits, lon
                            cudaStream_t st);
 void launch_verify_plan(int gen, DevState* ds, cudaStream_t st);
 void launch_patch_mark(const Lattice& L, uint32_t* ubits, DevState* ds, cudaStream_t st);
+// TMA descriptor of one grid copy (x fastest) for the staged x sweep. `valid` is false
+// when the lattice does not admit one (row pitch not a multiple of 16 bytes) or the
+// driver's encoder is unavailable; the x sweep then stages with cp.async.
+struct GridMap {
+    CUtensorMap map;
+    bool valid;
+};
+bool encode_grid_map(GridMap& m, const float* base, const Lattice& L);
+// `src_map`: the descriptor of `src` (or null).
 void launch_sweep(int rule, int axis, int dir, int round, const float* src, float* dst, const Lattice& L,
-                  DevState* ds, cudaStream_t st);
+                  DevState* ds, cudaStream_t st, const GridMap* src_map = nullptr);
+// Layout check of the x sweep's TMA tile (swizzled rows, out-of-lattice fill): writes the
+// number of mismatching elements to *mism.
+int selftest_tma_tile(unsigned long long* mism);
 void launch_end_round(int slot, int round, int cap, DevState* ds, cudaStream_t st);
 void launch_audit(const float* g, const Lattice& L, DevState* ds, cudaStream_t st);
 void launch_clamp(float* g, const uint32_t* sbits, const Lattice& L, DevState* ds, cudaStream_t st);

@@ -20,6 +20,7 @@
 //     stores the chunk back with coalesced row stores.
 // RULE 0 is the reference's update (godunov_ref), RULE 1 the corrected monotone one.
 #include <algorithm>
+#include <vector>
 
 #include "gbsdf_device.cuh"
 #include "gbsdf_internal.h"
@@ -319,6 +320,223 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_kernel(const float* __restr
     mark_changed(ch, &ds->changed[round]);
 }
 
+// ---- x sweeps, TMA-staged ------------------------------------------------------------
+// Same lines per CTA (32 y x 8 z), chunks (8 voxels) and ring as sweep_x_kernel, but each
+// chunk of the 34 x 10 staged lines is ONE cp.async.bulk.tensor copy issued by one thread,
+// completing on an mbarrier: no per-thread copy instructions. The tile lands with the
+// 32-byte swizzle (the two 16-byte halves of a 32-byte line are swapped on every other
+// group of four lines), so each thread reads its own line and its four neighbour lines
+// as 16-byte vectors with no bank conflicts (8 consecutive lines of a quarter-warp hit 8
+// distinct 16-byte bank groups). Out-of-lattice cells arrive as NaN; the neighbour-pair
+// minimum with the far sentinel turns them into it (fminf drops a NaN operand), which is
+// the reference's boundary rule (cuda_rasterizer.cu:454-461) bit for bit.
+// Every wait on a tile is bounded: on a timeout the CTA waits (bounded) for its copies in
+// flight, counts the event in DevState::wait_timeouts and returns.
+constexpr int kTBox = kXC * kXHY * kXHZ;            // floats per staged tile (2720)
+constexpr int kTSlotBytes = 11264;                  // tile bytes rounded up to 1 KB
+constexpr int kTS = 4, kTD = 2;                     // ring slots, prefetch distance
+constexpr size_t kTSmem = (size_t)kTS * kTSlotBytes + 64 + 1024;
+constexpr int kWaitPolls = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    for (int i = 0; i < kWaitPolls; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+// float offset of element j (0..7) of staged line r in a 32-byte-swizzled tile
+__device__ __forceinline__ int tsw(int r, int j) { return r * 8 + ((((j >> 2) ^ (r >> 2)) & 1) << 2) + (j & 3); }
+// 16-byte half c (0, 1) of staged line r
+__device__ __forceinline__ float4 tvec(const float* tile, int r, int c) {
+    return reinterpret_cast<const float4*>(tile)[r * 2 + ((c ^ (r >> 2)) & 1)];
+}
+__device__ __forceinline__ unsigned char* align1k(unsigned char* p) {
+    return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+}
+
+template <int RULE, int DIR>
+__global__ void __launch_bounds__(kXThreads) sweep_x_tma_kernel(const __grid_constant__ CUtensorMap tm,
+                                                                 float* __restrict__ dst, Lattice L, int round,
+                                                                 DevState* ds) {
+    if (ds->stop) return;
+    extern __shared__ unsigned char tsm_raw[];
+    unsigned char* tsm = align1k(tsm_raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(tsm + kTS * kTSlotBytes);
+    __shared__ int s_ok;
+    const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
+    const float h = L.h;
+    const size_t plane = (size_t)dx * dy;
+    const int tid = threadIdx.x, ty = tid & 31, tz = tid >> 5;
+    const int y0 = blockIdx.x * kXY, z0 = blockIdx.y * kXZ;
+    const int y = y0 + ty, z = z0 + tz;
+    const bool active = (y < dy) && (z < dz);
+    const int nchunks = (dx + kXC - 1) / kXC;
+    auto issue = [&](int ci) {
+        const int c = (DIR > 0) ? ci : (nchunks - 1 - ci);
+        const int s = ci % kTS;
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        mbar_expect_tx(&bars[s], kTBox * 4);
+        tma_load_3d(tsm + s * kTSlotBytes, &tm, c * kXC, y0 - 1, z0 - 1, &bars[s]);
+    };
+    if (tid == 0) {
+        for (int s = 0; s < kTS; ++s) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        s_ok = 1;
+        for (int d = 0; d < kTD && d < nchunks; ++d) issue(d);
+    }
+    const int rme = (tz + 1) * kXHY + (ty + 1);
+    const int rym = rme - 1, ryp = rme + 1, rzm = rme - kXHY, rzp = rme + kXHY;
+    float prev = kFarSentinel;
+    bool ch = false;
+#pragma unroll 1
+    for (int ci = 0; ci < nchunks; ++ci) {
+        __syncthreads();  // every thread is done with chunk ci - 1, so slot (ci + kTD) % kTS is free
+        if (tid == 0) {
+            if (ci + kTD < nchunks) issue(ci + kTD);
+            bool ok = mbar_wait(&bars[ci % kTS], (ci / kTS) & 1);
+            if (ok && ci + 1 < nchunks) ok = mbar_wait(&bars[(ci + 1) % kTS], ((ci + 1) / kTS) & 1);
+            if (!ok) {
+                // let the copies still in flight land before the CTA's shared memory goes
+                for (int k = ci; k < min(nchunks, ci + kTD + 1); ++k) mbar_wait(&bars[k % kTS], (k / kTS) & 1);
+                atomicAdd(&ds->wait_timeouts, 1ull);
+                s_ok = 0;
+            }
+        }
+        __syncthreads();
+        if (!s_ok) return;
+        const int c = (DIR > 0) ? ci : (nchunks - 1 - ci);
+        const int xc = c * kXC;
+        if (!active) continue;
+        const float* tile = reinterpret_cast<const float*>(tsm + (ci % kTS) * kTSlotBytes);
+        const float* ntile = reinterpret_cast<const float*>(tsm + ((ci + 1) % kTS) * kTSlotBytes);
+        float res[kXC];
+        if (xc + kXC <= dx && ci + 1 < nchunks) {
+            float cur[kXC], ay[kXC], az[kXC];
+            {
+                const float4 m0 = tvec(tile, rme, 0), m1 = tvec(tile, rme, 1);
+                cur[0] = m0.x; cur[1] = m0.y; cur[2] = m0.z; cur[3] = m0.w;
+                cur[4] = m1.x; cur[5] = m1.y; cur[6] = m1.z; cur[7] = m1.w;
+            }
+#pragma unroll
+            for (int hv = 0; hv < 2; ++hv) {
+                const float4 a = tvec(tile, rym, hv), b = tvec(tile, ryp, hv);
+                const float4 p = tvec(tile, rzm, hv), q = tvec(tile, rzp, hv);
+                ay[4 * hv + 0] = fminf(fminf(a.x, b.x), kFarSentinel);
+                ay[4 * hv + 1] = fminf(fminf(a.y, b.y), kFarSentinel);
+                ay[4 * hv + 2] = fminf(fminf(a.z, b.z), kFarSentinel);
+                ay[4 * hv + 3] = fminf(fminf(a.w, b.w), kFarSentinel);
+                az[4 * hv + 0] = fminf(fminf(p.x, q.x), kFarSentinel);
+                az[4 * hv + 1] = fminf(fminf(p.y, q.y), kFarSentinel);
+                az[4 * hv + 2] = fminf(fminf(p.z, q.z), kFarSentinel);
+                az[4 * hv + 3] = fminf(fminf(p.w, q.w), kFarSentinel);
+            }
+            // the first voxel of the next chunk in walk order
+            const float nxt = (DIR > 0) ? ntile[tsw(rme, 0)] : ntile[tsw(rme, kXC - 1)];
+#pragma unroll
+            for (int jj = 0; jj < kXC; ++jj) {
+                const int j = (DIR > 0) ? jj : (kXC - 1 - jj);
+                const float down = (DIR > 0) ? ((j + 1 < kXC) ? cur[j + 1] : nxt) : ((j > 0) ? cur[j - 1] : nxt);
+                const float u = godunov<RULE>(fminf(prev, down), ay[j], az[j], h);
+                const float out = (u < cur[j]) ? u : cur[j];
+                ch |= (u < cur[j]);
+                res[j] = out;
+                prev = out;
+            }
+        } else {
+#pragma unroll
+            for (int jj = 0; jj < kXC; ++jj) {
+                const int j = (DIR > 0) ? jj : (kXC - 1 - jj);
+                res[j] = 0.0f;
+                if (xc + j >= dx) continue;
+                const float cur = tile[tsw(rme, j)];
+                float down;
+                if (DIR > 0) down = (j + 1 < kXC) ? tile[tsw(rme, j + 1)]
+                                                  : ((ci + 1 < nchunks) ? ntile[tsw(rme, 0)] : kFarSentinel);
+                else down = (j > 0) ? tile[tsw(rme, j - 1)]
+                                    : ((ci + 1 < nchunks) ? ntile[tsw(rme, kXC - 1)] : kFarSentinel);
+                const float ayj = fminf(fminf(tile[tsw(rym, j)], tile[tsw(ryp, j)]), kFarSentinel);
+                const float azj = fminf(fminf(tile[tsw(rzm, j)], tile[tsw(rzp, j)]), kFarSentinel);
+                const float u = godunov<RULE>(fminf(prev, down), ayj, azj, h);
+                const float out = (u < cur) ? u : cur;
+                ch |= (u < cur);
+                res[j] = out;
+                prev = out;
+            }
+        }
+        float* drow = dst + (size_t)z * plane + (size_t)y * dx + xc;
+        if (xc + kXC <= dx) {
+            reinterpret_cast<float4*>(drow)[0] = make_float4(res[0], res[1], res[2], res[3]);
+            reinterpret_cast<float4*>(drow)[1] = make_float4(res[4], res[5], res[6], res[7]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < kXC; ++j)
+                if (xc + j < dx) drow[j] = res[j];
+        }
+    }
+    mark_changed(ch, &ds->changed[round]);
+}
+
+// Layout check of the staged tile: one CTA loads the box at (x, y, z) of a grid whose
+// cells hold their own linear index, and every thread compares elements (scalar reads
+// through tsw, vector reads through tvec) with the expected value or NaN outside.
+__global__ void selftest_tma_kernel(const __grid_constant__ CUtensorMap tm, int x, int y, int z, int dx, int dy,
+                                    int dz, unsigned long long* mism) {
+    extern __shared__ unsigned char tsm_raw[];
+    unsigned char* tsm = align1k(tsm_raw);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(tsm + kTSlotBytes);
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        mbar_expect_tx(bar, kTBox * 4);
+        tma_load_3d(tsm, &tm, x, y, z, bar);
+        s_ok = mbar_wait(bar, 0) ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_ok) {
+        if (threadIdx.x == 0) atomicAdd(mism, 1000000ull);
+        return;
+    }
+    const float* tile = reinterpret_cast<const float*>(tsm);
+    unsigned long long bad = 0;
+    for (int e = threadIdx.x; e < kTBox; e += blockDim.x) {
+        const int r = e / kXC, j = e % kXC;
+        const int gx = x + j, gy = y + r % kXHY, gz = z + r / kXHY;
+        const bool inb = gx >= 0 && gx < dx && gy >= 0 && gy < dy && gz >= 0 && gz < dz;
+        const float want = inb ? (float)(((long long)gz * dy + gy) * dx + gx) : 0.0f;
+        const float got = tile[tsw(r, j)];
+        const float4 v = tvec(tile, r, j >> 2);
+        const float gv = (j & 3) == 0 ? v.x : (j & 3) == 1 ? v.y : (j & 3) == 2 ? v.z : v.w;
+        if (inb ? (got != want || gv != want) : (got == got || gv == gv)) ++bad;
+    }
+    if (bad) atomicAdd(mism, bad);
+}
+
 __global__ void end_round_kernel(int slot, int round, int cap, DevState* ds) {
     if (ds->stop) return;
     ds->rounds = round + 1;
@@ -395,7 +613,7 @@ __global__ void __launch_bounds__(256) apply_kernel(const float* __restrict__ g,
 
 template <int RULE, int DIR>
 void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lattice& L, DevState* ds,
-                    cudaStream_t st) {
+                    cudaStream_t st, const GridMap* src_map) {
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
     GBSDF_COUNT_LAUNCH();
     if (axis == 2) {
@@ -408,6 +626,11 @@ void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lat
         cudaFuncSetAttribute(sweep_walk_kernel<1, RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kWSmem);
         sweep_walk_kernel<1, RULE, DIR><<<grid, kWThreads, kWSmem, st>>>(src, dst, L, round, ds);
+    } else if (src_map && src_map->valid) {
+        dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
+        cudaFuncSetAttribute(sweep_x_tma_kernel<RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kTSmem);
+        sweep_x_tma_kernel<RULE, DIR><<<grid, kXThreads, kTSmem, st>>>(src_map->map, dst, L, round, ds);
     } else {
         dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
         cudaFuncSetAttribute(sweep_x_kernel<RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kXSmem);
@@ -415,17 +638,79 @@ void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lat
     }
 }
 
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn tiled_encoder() {
+    static EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return static_cast<EncodeTiledFn>(nullptr);
+        }
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+bool encode_box(CUtensorMap* m, const float* base, int dx, int dy, int dz) {
+    EncodeTiledFn fn = tiled_encoder();
+    if (!fn) return false;
+    const cuuint64_t gdim[3] = {(cuuint64_t)dx, (cuuint64_t)dy, (cuuint64_t)dz};
+    const cuuint64_t gstride[2] = {(cuuint64_t)dx * 4, (cuuint64_t)dx * dy * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)kXC, (cuuint32_t)kXHY, (cuuint32_t)kXHZ};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), gdim, gstride, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NAN_REQUEST_ZERO_FMA) == CUDA_SUCCESS;
+}
+
 }  // namespace
 
+bool encode_grid_map(GridMap& m, const float* base, const Lattice& L) {
+    m.valid = false;
+    // row and plane pitches must be multiples of 16 bytes, the base 16-byte aligned
+    if ((L.dims[0] & 3) != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
+    m.valid = encode_box(&m.map, base, L.dims[0], L.dims[1], L.dims[2]);
+    return m.valid;
+}
+
 void launch_sweep(int rule, int axis, int dir, int round, const float* src, float* dst, const Lattice& L,
-                  DevState* ds, cudaStream_t st) {
+                  DevState* ds, cudaStream_t st, const GridMap* src_map) {
     if (rule == 0) {
-        if (dir > 0) launch_sweep_t<0, 1>(axis, round, src, dst, L, ds, st);
-        else launch_sweep_t<0, -1>(axis, round, src, dst, L, ds, st);
+        if (dir > 0) launch_sweep_t<0, 1>(axis, round, src, dst, L, ds, st, src_map);
+        else launch_sweep_t<0, -1>(axis, round, src, dst, L, ds, st, src_map);
     } else {
-        if (dir > 0) launch_sweep_t<1, 1>(axis, round, src, dst, L, ds, st);
-        else launch_sweep_t<1, -1>(axis, round, src, dst, L, ds, st);
+        if (dir > 0) launch_sweep_t<1, 1>(axis, round, src, dst, L, ds, st, src_map);
+        else launch_sweep_t<1, -1>(axis, round, src, dst, L, ds, st, src_map);
     }
+}
+
+int selftest_tma_tile(unsigned long long* mism_dev) {
+    const int dx = 48, dy = 40, dz = 16;
+    const size_t n = (size_t)dx * dy * dz;
+    std::vector<float> hv(n);
+    for (size_t i = 0; i < n; ++i) hv[i] = (float)i;
+    float* g = nullptr;
+    if (cudaMalloc(&g, n * 4) != cudaSuccess) return 1;
+    int rc = 0;
+    CUtensorMap m;
+    if (cudaMemcpy(g, hv.data(), n * 4, cudaMemcpyHostToDevice) != cudaSuccess || !encode_box(&m, g, dx, dy, dz)) {
+        rc = 1;
+    } else {
+        const int pts[5][3] = {{0, -1, -1}, {8, 5, 3}, {40, 31, 7}, {16, 10, 0}, {32, -1, 12}};
+        const size_t smem = kTSlotBytes + 64 + 1024;
+        cudaFuncSetAttribute(selftest_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        for (auto& p : pts) selftest_tma_kernel<<<1, 256, smem>>>(m, p[0], p[1], p[2], dx, dy, dz, mism_dev);
+        if (cudaDeviceSynchronize() != cudaSuccess) rc = 1;
+    }
+    cudaGetLastError();
+    cudaFree(g);
+    return rc;
 }
 
 void launch_end_round(int slot, int round, int cap, DevState* ds, cudaStream_t st) {
