@@ -102,7 +102,11 @@ typedef struct gbsdf_options {
     const float* mlp_params; /* learned mode: GBSDF_MLP_PARAMS FP32 parameters in device memory */
     const float* brick_scores; /* learned mode, instead of the network: caller-supplied risk
                                   logits, one per 8^3 brick (x fastest), in device memory */
-    int32_t reserved[2];
+    int32_t sweep_schedule; /* x-sweep schedule: 0 = autotuned (the first build of a lattice
+                               class times the candidates), 1 = cp.async-staged, 2 = TMA tiles
+                               on a CTA-barrier ring, 3 = TMA tiles on a warp-specialised
+                               mbarrier pipeline (2 and 3 need rows of a multiple of 4 voxels) */
+    int32_t reserved;
 } gbsdf_options;
 
 /* Learned sign-risk model: parameter count and brick feature count. */
@@ -133,7 +137,8 @@ typedef struct gbsdf_stats {
     int64_t csr_entries;   /* entries of the reference's supercell CSR */
     int64_t kernel_launches; /* CUDA kernels this call launched */
     int64_t proposed;      /* learned mode: bricks the network proposed for the exact winding number */
-    int64_t reserved[6];
+    int64_t sweep_schedule; /* x-sweep schedule that ran (see gbsdf_options.sweep_schedule) */
+    int64_t reserved[5];
 } gbsdf_stats;
 
 /* Fill `opt` with defaults: reference mode, AUTO path, device 0, host triangles. */

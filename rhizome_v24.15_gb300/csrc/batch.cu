@@ -89,6 +89,7 @@ struct Job {
     DevState* hs = nullptr;
     cudaStream_t st = nullptr;
     GridMap map_a{}, map_b{};  // TMA descriptors of A and B
+    int xsched = kXAuto;       // x-sweep schedule (a tuned class's winner, else the default)
 };
 
 // Carves aligned sub-buffers out of one allocation: a sizing pass, then a placing pass.
@@ -110,6 +111,7 @@ struct gbsdf_batch {
     int device = 0;
     int mode = GBSDF_MODE_REFERENCE;
     int num_sms = 0;
+    int sweep_schedule = 0;
     bool out_dev = false;
     bool tris_dev = false;
     std::vector<gbsdf::Job> jobs;
@@ -207,7 +209,8 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
     for (int r = 0; r < kMaxRounds; ++r) {
         for (int axis = 0; axis < 3; ++axis)
             for (int dir = 1; dir >= -1; dir -= 2) {
-                launch_sweep(0, axis, dir, r, src, dst, L, j.ds, st, src == j.A ? &j.map_a : &j.map_b);
+                launch_sweep(0, axis, dir, r, src, dst, L, j.ds, st, src == j.A ? &j.map_a : &j.map_b,
+                             j.xsched);
                 std::swap(src, dst);
             }
         launch_end_round(r, r, kMaxRounds, j.ds, st);
@@ -259,6 +262,9 @@ int plan(gbsdf_batch& b, BErr& e) {
             place_phase1(j, p1);
             encode_grid_map(j.map_a, j.A, j.L);
             encode_grid_map(j.map_b, j.B, j.L);
+            j.xsched = (b.sweep_schedule >= kXCpAsync && b.sweep_schedule <= kXTmaPipe)
+                           ? b.sweep_schedule
+                           : tuned_x_schedule(b.device, j.L, j.A, j.B, &j.map_a, j.ds, b.origin, false);
         }
     // counting pass
     for (Job& j : b.jobs) {
@@ -367,6 +373,7 @@ void fill_stats(const Job& j, int status, float ms, unsigned long long launches,
     s->gwn_pairs = (long long)h.gwn_pairs;
     s->brick_pairs = (long long)h.brick_pairs;
     s->csr_entries = (long long)h.csr_entries;
+    s->sweep_schedule = j.map_a.valid ? (j.xsched == kXAuto ? kXTmaPipe : j.xsched) : kXCpAsync;
 }
 
 int run_once(gbsdf_batch& b, bool& any_overflow, float& ms, BErr& e) {
@@ -454,6 +461,7 @@ int gbsdf_batch_create(const gbsdf_mesh_desc* meshes, int32_t n_meshes, int32_t 
     gbsdf_batch* b = new gbsdf_batch();
     b->device = o.device;
     b->mode = o.mode;
+    b->sweep_schedule = o.sweep_schedule;
     b->out_dev = out_on_device != 0;
     b->tris_dev = o.tris_on_device != 0;
     auto fail = [&](int rc) {

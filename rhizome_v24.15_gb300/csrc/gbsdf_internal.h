@@ -152,9 +152,17 @@ struct GridMap {
     bool valid;
 };
 bool encode_grid_map(GridMap& m, const float* base, const Lattice& L);
-// `src_map`: the descriptor of `src` (or null).
+// Schedules of the x sweep (all give identical results): staged by per-thread cp.async
+// copies, by TMA tiles on a CTA-barrier ring, or by TMA tiles on a warp-specialised
+// mbarrier pipeline. 0 picks the pipeline when a TMA descriptor is valid.
+enum XSchedule : int { kXAuto = 0, kXCpAsync = 1, kXTmaRing = 2, kXTmaPipe = 3 };
+// `src_map`: the descriptor of `src` (or null); `x_schedule`: an XSchedule.
 void launch_sweep(int rule, int axis, int dir, int round, const float* src, float* dst, const Lattice& L,
-                  DevState* ds, cudaStream_t st, const GridMap* src_map = nullptr);
+                  DevState* ds, cudaStream_t st, const GridMap* src_map = nullptr, int x_schedule = kXAuto);
+// The x-sweep schedule for this lattice class: the remembered winner, else (measure)
+// each candidate timed on src -> dst (writes dst and changed[63]), else the pipeline.
+int tuned_x_schedule(int device, const Lattice& L, const float* src, float* dst, const GridMap* src_map,
+                     DevState* ds, cudaStream_t st, bool measure);
 // Layout check of the x sweep's TMA tile (swizzled rows, out-of-lattice fill): writes the
 // number of mismatching elements to *mism.
 int selftest_tma_tile(unsigned long long* mism);

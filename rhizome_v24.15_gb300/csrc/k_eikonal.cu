@@ -500,6 +500,154 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_tma_kernel(const __grid_con
     mark_changed(ch, &ds->changed[round]);
 }
 
+// ---- x sweeps, TMA-staged, warp-specialised pipeline ---------------------------------
+// The tiles, swizzle and per-line arithmetic of sweep_x_tma_kernel, with the ring run as
+// a producer / consumer pipeline on mbarriers instead of CTA-wide barriers: warp 8 issues
+// the bulk copies (waiting for a slot's "empty" barrier, 8 warp arrivals), the 8 consumer
+// warps each wait for the "full" barriers of the chunks they read and release a slot when
+// their last read of it is done. Warps drift up to the ring depth apart, so the serial
+// chains of different warps overlap instead of meeting at a barrier every chunk. All
+// waits are bounded; a warp that gives up counts the event and leaves, and the producer
+// lets its copies in flight land before it leaves.
+constexpr int kPS = 4;                               // ring slots
+constexpr int kPThreads = kXThreads + 32;            // 8 consumer warps + 1 producer warp
+constexpr size_t kPSmem = (size_t)kPS * kTSlotBytes + 128 + 1024;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int RULE, int DIR>
+__global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_constant__ CUtensorMap tm,
+                                                                  float* __restrict__ dst, Lattice L, int round,
+                                                                  DevState* ds) {
+    if (ds->stop) return;
+    extern __shared__ unsigned char tsm_raw[];
+    unsigned char* tsm = align1k(tsm_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kPS * kTSlotBytes);
+    uint64_t* empty = full + kPS;
+    const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
+    const float h = L.h;
+    const size_t plane = (size_t)dx * dy;
+    const int tid = threadIdx.x;
+    const int y0 = blockIdx.x * kXY, z0 = blockIdx.y * kXZ;
+    const int nchunks = (dx + kXC - 1) / kXC;
+    if (tid == 0) {
+        for (int s = 0; s < kPS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kXThreads / 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();  // the only CTA-wide barrier: the ring's barriers are initialised
+    if (tid >= kXThreads) {
+        // producer warp: one lane issues every chunk's copy
+        if (tid != kXThreads) return;
+        int ci = 0;
+        for (; ci < nchunks; ++ci) {
+            const int s = ci % kPS;
+            if (ci >= kPS && !mbar_wait(&empty[s], ((ci / kPS) - 1) & 1)) break;
+            const int c = (DIR > 0) ? ci : (nchunks - 1 - ci);
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            mbar_expect_tx(&full[s], kTBox * 4);
+            tma_load_3d(tsm + s * kTSlotBytes, &tm, c * kXC, y0 - 1, z0 - 1, &full[s]);
+        }
+        if (ci < nchunks) {  // consumers stopped releasing slots: drain what is in flight
+            for (int k = max(0, ci - kPS); k < ci; ++k) mbar_wait(&full[k % kPS], (k / kPS) & 1);
+            atomicAdd(&ds->wait_timeouts, 1ull);
+        }
+        return;
+    }
+    const int ty = tid & 31, tz = tid >> 5;
+    const int y = y0 + ty, z = z0 + tz;
+    const bool active = (y < dy) && (z < dz);
+    const int rme = (tz + 1) * kXHY + (ty + 1);
+    const int rym = rme - 1, ryp = rme + 1, rzm = rme - kXHY, rzp = rme + kXHY;
+    float prev = kFarSentinel;
+    bool ch = false;
+#pragma unroll 1
+    for (int ci = 0; ci < nchunks; ++ci) {
+        bool ok = mbar_wait(&full[ci % kPS], (ci / kPS) & 1);
+        if (ok && ci + 1 < nchunks) ok = mbar_wait(&full[(ci + 1) % kPS], ((ci + 1) / kPS) & 1);
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (ty == 0) atomicAdd(&ds->wait_timeouts, 1ull);
+            return;
+        }
+        const int c = (DIR > 0) ? ci : (nchunks - 1 - ci);
+        const int xc = c * kXC;
+        if (active) {
+            const float* tile = reinterpret_cast<const float*>(tsm + (ci % kPS) * kTSlotBytes);
+            const float* ntile = reinterpret_cast<const float*>(tsm + ((ci + 1) % kPS) * kTSlotBytes);
+            float res[kXC];
+            if (xc + kXC <= dx && ci + 1 < nchunks) {
+                float cur[kXC], ay[kXC], az[kXC];
+                {
+                    const float4 m0 = tvec(tile, rme, 0), m1 = tvec(tile, rme, 1);
+                    cur[0] = m0.x; cur[1] = m0.y; cur[2] = m0.z; cur[3] = m0.w;
+                    cur[4] = m1.x; cur[5] = m1.y; cur[6] = m1.z; cur[7] = m1.w;
+                }
+#pragma unroll
+                for (int hv = 0; hv < 2; ++hv) {
+                    const float4 a = tvec(tile, rym, hv), b = tvec(tile, ryp, hv);
+                    const float4 p = tvec(tile, rzm, hv), q = tvec(tile, rzp, hv);
+                    ay[4 * hv + 0] = fminf(fminf(a.x, b.x), kFarSentinel);
+                    ay[4 * hv + 1] = fminf(fminf(a.y, b.y), kFarSentinel);
+                    ay[4 * hv + 2] = fminf(fminf(a.z, b.z), kFarSentinel);
+                    ay[4 * hv + 3] = fminf(fminf(a.w, b.w), kFarSentinel);
+                    az[4 * hv + 0] = fminf(fminf(p.x, q.x), kFarSentinel);
+                    az[4 * hv + 1] = fminf(fminf(p.y, q.y), kFarSentinel);
+                    az[4 * hv + 2] = fminf(fminf(p.z, q.z), kFarSentinel);
+                    az[4 * hv + 3] = fminf(fminf(p.w, q.w), kFarSentinel);
+                }
+                const float nxt = (DIR > 0) ? ntile[tsw(rme, 0)] : ntile[tsw(rme, kXC - 1)];
+#pragma unroll
+                for (int jj = 0; jj < kXC; ++jj) {
+                    const int j = (DIR > 0) ? jj : (kXC - 1 - jj);
+                    const float down = (DIR > 0) ? ((j + 1 < kXC) ? cur[j + 1] : nxt) : ((j > 0) ? cur[j - 1] : nxt);
+                    const float u = godunov<RULE>(fminf(prev, down), ay[j], az[j], h);
+                    const float out = (u < cur[j]) ? u : cur[j];
+                    ch |= (u < cur[j]);
+                    res[j] = out;
+                    prev = out;
+                }
+            } else {
+#pragma unroll
+                for (int jj = 0; jj < kXC; ++jj) {
+                    const int j = (DIR > 0) ? jj : (kXC - 1 - jj);
+                    res[j] = 0.0f;
+                    if (xc + j >= dx) continue;
+                    const float cur = tile[tsw(rme, j)];
+                    float down;
+                    if (DIR > 0) down = (j + 1 < kXC) ? tile[tsw(rme, j + 1)]
+                                                      : ((ci + 1 < nchunks) ? ntile[tsw(rme, 0)] : kFarSentinel);
+                    else down = (j > 0) ? tile[tsw(rme, j - 1)]
+                                        : ((ci + 1 < nchunks) ? ntile[tsw(rme, kXC - 1)] : kFarSentinel);
+                    const float ayj = fminf(fminf(tile[tsw(rym, j)], tile[tsw(ryp, j)]), kFarSentinel);
+                    const float azj = fminf(fminf(tile[tsw(rzm, j)], tile[tsw(rzp, j)]), kFarSentinel);
+                    const float u = godunov<RULE>(fminf(prev, down), ayj, azj, h);
+                    const float out = (u < cur) ? u : cur;
+                    ch |= (u < cur);
+                    res[j] = out;
+                    prev = out;
+                }
+            }
+            float* drow = dst + (size_t)z * plane + (size_t)y * dx + xc;
+            if (xc + kXC <= dx) {
+                reinterpret_cast<float4*>(drow)[0] = make_float4(res[0], res[1], res[2], res[3]);
+                reinterpret_cast<float4*>(drow)[1] = make_float4(res[4], res[5], res[6], res[7]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < kXC; ++j)
+                    if (xc + j < dx) drow[j] = res[j];
+            }
+        }
+        // this warp's last read of chunk ci's slot is done (it was also chunk ci-1's "next")
+        __syncwarp();
+        if (ty == 0) mbar_arrive(&empty[ci % kPS]);
+    }
+    mark_changed(ch, &ds->changed[round]);
+}
+
 // Layout check of the staged tile: one CTA loads the box at (x, y, z) of a grid whose
 // cells hold their own linear index, and every thread compares elements (scalar reads
 // through tsw, vector reads through tvec) with the expected value or NaN outside.
@@ -613,7 +761,10 @@ __global__ void __launch_bounds__(256) apply_kernel(const float* __restrict__ g,
 
 template <int RULE, int DIR>
 void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lattice& L, DevState* ds,
-                    cudaStream_t st, const GridMap* src_map) {
+                    cudaStream_t st, const GridMap* src_map, int xsched) {
+    const bool tma = src_map && src_map->valid;
+    if (xsched == 0) xsched = tma ? kXTmaPipe : kXCpAsync;
+    if (!tma) xsched = kXCpAsync;
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
     GBSDF_COUNT_LAUNCH();
     if (axis == 2) {
@@ -626,7 +777,12 @@ void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lat
         cudaFuncSetAttribute(sweep_walk_kernel<1, RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kWSmem);
         sweep_walk_kernel<1, RULE, DIR><<<grid, kWThreads, kWSmem, st>>>(src, dst, L, round, ds);
-    } else if (src_map && src_map->valid) {
+    } else if (xsched == kXTmaPipe) {
+        dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
+        cudaFuncSetAttribute(sweep_x_pipe_kernel<RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kPSmem);
+        sweep_x_pipe_kernel<RULE, DIR><<<grid, kPThreads, kPSmem, st>>>(src_map->map, dst, L, round, ds);
+    } else if (xsched == kXTmaRing) {
         dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
         cudaFuncSetAttribute(sweep_x_tma_kernel<RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kTSmem);
@@ -680,13 +836,13 @@ bool encode_grid_map(GridMap& m, const float* base, const Lattice& L) {
 }
 
 void launch_sweep(int rule, int axis, int dir, int round, const float* src, float* dst, const Lattice& L,
-                  DevState* ds, cudaStream_t st, const GridMap* src_map) {
+                  DevState* ds, cudaStream_t st, const GridMap* src_map, int x_schedule) {
     if (rule == 0) {
-        if (dir > 0) launch_sweep_t<0, 1>(axis, round, src, dst, L, ds, st, src_map);
-        else launch_sweep_t<0, -1>(axis, round, src, dst, L, ds, st, src_map);
+        if (dir > 0) launch_sweep_t<0, 1>(axis, round, src, dst, L, ds, st, src_map, x_schedule);
+        else launch_sweep_t<0, -1>(axis, round, src, dst, L, ds, st, src_map, x_schedule);
     } else {
-        if (dir > 0) launch_sweep_t<1, 1>(axis, round, src, dst, L, ds, st, src_map);
-        else launch_sweep_t<1, -1>(axis, round, src, dst, L, ds, st, src_map);
+        if (dir > 0) launch_sweep_t<1, 1>(axis, round, src, dst, L, ds, st, src_map, x_schedule);
+        else launch_sweep_t<1, -1>(axis, round, src, dst, L, ds, st, src_map, x_schedule);
     }
 }
 

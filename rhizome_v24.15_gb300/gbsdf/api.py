@@ -106,13 +106,14 @@ def _set_learned(o, mode, device, mlp_params, mlp_budget, mlp_threshold, brick_s
 
 def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE_REFERENCE, path=PATH_AUTO,
                      device=0, max_rounds=0, raise_on_error=True, mlp_params=None, mlp_budget=None,
-                     mlp_threshold=None, brick_scores=None):
+                     mlp_threshold=None, brick_scores=None, sweep_schedule=0):
     """Run the engine. ``tris``: (T,12) float32 numpy array (host) or CUDA tensor.
     ``out``: float32 buffer of N voxels (numpy = host, CUDA tensor = device); allocated
     on the host when None. ``MODE_LEARNED`` takes the sign-risk model's parameters
     (``mlp_params``; the shipped model when None), the most bricks it may propose and the
     probability threshold; ``brick_scores`` (one logit per 8^3 brick, x fastest) replaces
-    the network's scores. Returns ``(out, Result)``."""
+    the network's scores. ``sweep_schedule``: 0 autotuned, 1-3 a fixed x-sweep schedule
+    (identical results). Returns ``(out, Result)``."""
     mn = np.asarray(min_coord, np.int64).reshape(3)
     mx = np.asarray(max_coord, np.int64).reshape(3)
     dims = mx - mn + 1
@@ -128,6 +129,7 @@ def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE
     L = _lib.load()
     L.gbsdf_default_options(C.byref(o))
     o.mode, o.path, o.device, o.tris_on_device, o.max_rounds = int(mode), int(path), int(device), int(tdev), int(max_rounds)
+    o.sweep_schedule = int(sweep_schedule)
     keep = _set_learned(o, mode, device, mlp_params, mlp_budget, mlp_threshold, brick_scores)  # noqa: F841
     st = _lib.Stats()
     err = C.create_string_buffer(512)
@@ -191,7 +193,7 @@ class Batch:
     The arrays are referenced, not copied: their contents may change between runs, their
     sizes may not."""
 
-    def __init__(self, meshes, outs=None, mode=MODE_REFERENCE, device=0):
+    def __init__(self, meshes, outs=None, mode=MODE_REFERENCE, device=0, sweep_schedule=0):
         n = len(meshes)
         self.n = n
         self._descs = (_lib.MeshDesc * n)()
@@ -218,6 +220,7 @@ class Batch:
         o = _lib.Options()
         L.gbsdf_default_options(C.byref(o))
         o.mode, o.path, o.device, o.tris_on_device = int(mode), int(PATH_FAST), int(device), int(bool(tdev))
+        o.sweep_schedule = int(sweep_schedule)
         self._h = C.c_void_p()
         err = C.create_string_buffer(512)
         rc = L.gbsdf_batch_create(self._descs, n, int(bool(odev)), C.byref(o), C.byref(self._h), err, len(err))
