@@ -102,10 +102,12 @@ typedef struct gbsdf_options {
     const float* mlp_params; /* learned mode: GBSDF_MLP_PARAMS FP32 parameters in device memory */
     const float* brick_scores; /* learned mode, instead of the network: caller-supplied risk
                                   logits, one per 8^3 brick (x fastest), in device memory */
-    int32_t sweep_schedule; /* x-sweep schedule: 0 = autotuned (the first build of a lattice
-                               class times the candidates), 1 = cp.async-staged, 2 = TMA tiles
-                               on a CTA-barrier ring, 3 = TMA tiles on a warp-specialised
-                               mbarrier pipeline (2 and 3 need rows of a multiple of 4 voxels) */
+    int32_t sweep_schedule; /* eikonal sweep schedules (identical results): 0 = autotuned (the
+                               first build of a lattice class times the candidates); 1, 2, 3 =
+                               x sweep staged by cp.async, by TMA tiles on a CTA-barrier ring, by
+                               TMA tiles on a warp-specialised mbarrier pipeline (y / z walks:
+                               default); 4, 5 = x pipeline with cp.async-staged / TMA-pipelined
+                               y / z walks. TMA needs rows of a multiple of 4 voxels. */
     int32_t reserved;
 } gbsdf_options;
 
@@ -137,7 +139,8 @@ typedef struct gbsdf_stats {
     int64_t csr_entries;   /* entries of the reference's supercell CSR */
     int64_t kernel_launches; /* CUDA kernels this call launched */
     int64_t proposed;      /* learned mode: bricks the network proposed for the exact winding number */
-    int64_t sweep_schedule; /* x-sweep schedule that ran (see gbsdf_options.sweep_schedule) */
+    int64_t sweep_schedule; /* schedules that ran: x schedule (1-3) + 10 x walk schedule
+                               (1 cp.async, 2 TMA pipeline) */
     int64_t reserved[5];
 } gbsdf_stats;
 

@@ -89,7 +89,8 @@ struct Job {
     DevState* hs = nullptr;
     cudaStream_t st = nullptr;
     GridMap map_a{}, map_b{};  // TMA descriptors of A and B
-    int xsched = kXAuto;       // x-sweep schedule (a tuned class's winner, else the default)
+    int xsched = kXAuto;       // sweep schedules (a tuned class's winners, else the defaults)
+    int wsched = kWAuto;
 };
 
 // Carves aligned sub-buffers out of one allocation: a sizing pass, then a placing pass.
@@ -210,7 +211,7 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
         for (int axis = 0; axis < 3; ++axis)
             for (int dir = 1; dir >= -1; dir -= 2) {
                 launch_sweep(0, axis, dir, r, src, dst, L, j.ds, st, src == j.A ? &j.map_a : &j.map_b,
-                             j.xsched);
+                             j.xsched, j.wsched);
                 std::swap(src, dst);
             }
         launch_end_round(r, r, kMaxRounds, j.ds, st);
@@ -262,9 +263,14 @@ int plan(gbsdf_batch& b, BErr& e) {
             place_phase1(j, p1);
             encode_grid_map(j.map_a, j.A, j.L);
             encode_grid_map(j.map_b, j.B, j.L);
-            j.xsched = (b.sweep_schedule >= kXCpAsync && b.sweep_schedule <= kXTmaPipe)
-                           ? b.sweep_schedule
-                           : tuned_x_schedule(b.device, j.L, j.A, j.B, &j.map_a, j.ds, b.origin, false);
+            const SweepPlan plan = tuned_sweep_plan(b.device, j.L, j.A, j.B, &j.map_a, j.ds, b.origin, false);
+            j.xsched = plan.x;
+            j.wsched = plan.w;
+            if (b.sweep_schedule >= kXCpAsync && b.sweep_schedule <= kXTmaPipe) j.xsched = b.sweep_schedule;
+            if (b.sweep_schedule == 4 || b.sweep_schedule == 5) {
+                j.xsched = kXTmaPipe;
+                j.wsched = b.sweep_schedule == 4 ? kWCpAsync : kWTmaPipe;
+            }
         }
     // counting pass
     for (Job& j : b.jobs) {
@@ -373,7 +379,8 @@ void fill_stats(const Job& j, int status, float ms, unsigned long long launches,
     s->gwn_pairs = (long long)h.gwn_pairs;
     s->brick_pairs = (long long)h.brick_pairs;
     s->csr_entries = (long long)h.csr_entries;
-    s->sweep_schedule = j.map_a.valid ? (j.xsched == kXAuto ? kXTmaPipe : j.xsched) : kXCpAsync;
+    s->sweep_schedule = (j.map_a.valid ? (j.xsched == kXAuto ? kXTmaPipe : j.xsched) : kXCpAsync) +
+                        10 * (j.map_a.walk_valid ? (j.wsched == kWAuto ? kWTmaPipe : j.wsched) : kWCpAsync);
 }
 
 int run_once(gbsdf_batch& b, bool& any_overflow, float& ms, BErr& e) {

@@ -314,14 +314,20 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     encode_grid_map(map_a, P<float>(w.A), L);
     encode_grid_map(map_b, P<float>(w.B), L);
     auto map_of = [&](const float* p) { return p == P<float>(w.A) ? &map_a : &map_b; };
-    const int xsched = (o.sweep_schedule >= kXCpAsync && o.sweep_schedule <= kXTmaPipe)
-                           ? o.sweep_schedule
-                           : tuned_x_schedule(w.device, L, src, dst, &map_a, w.ds, st, true);
+    // sweep_schedule: 0 autotuned; 1..3 x schedule (with the walks' default); 4 / 5 force the
+    // cp.async / TMA-pipeline walks with the x pipeline
+    SweepPlan plan = tuned_sweep_plan(w.device, L, src, dst, &map_a, w.ds, st, o.sweep_schedule == 0);
+    if (o.sweep_schedule >= kXCpAsync && o.sweep_schedule <= kXTmaPipe) plan.x = o.sweep_schedule;
+    if (o.sweep_schedule == 4 || o.sweep_schedule == 5) {
+        plan.x = kXTmaPipe;
+        plan.w = o.sweep_schedule == 4 ? kWCpAsync : kWTmaPipe;
+    }
+    const int xsched = plan.x, wsched = plan.w;
     if (ref_eikonal) {
         for (int r = 0; r < kMaxRounds; ++r) {
             for (int axis = 0; axis < 3; ++axis)
                 for (int dir = 1; dir >= -1; dir -= 2) {
-                    launch_sweep(rule, axis, dir, r, src, dst, L, w.ds, st, map_of(src), xsched);
+                    launch_sweep(rule, axis, dir, r, src, dst, L, w.ds, st, map_of(src), xsched, wsched);
                     std::swap(src, dst);
                 }
             launch_end_round(r, r, kMaxRounds, w.ds, st);
@@ -334,7 +340,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
                 GB_CK(cudaMemsetAsync(&w.ds->changed[r % 64], 0, sizeof(int), st));
                 for (int axis = 0; axis < 3; ++axis)
                     for (int dir = 1; dir >= -1; dir -= 2) {
-                        launch_sweep(rule, axis, dir, r % 64, src, dst, L, w.ds, st, map_of(src), xsched);
+                        launch_sweep(rule, axis, dir, r % 64, src, dst, L, w.ds, st, map_of(src), xsched, wsched);
                         std::swap(src, dst);
                     }
                 launch_end_round(r % 64, r, cap, w.ds, st);
@@ -457,7 +463,8 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         stats->csr_entries = (long long)h.csr_entries;
         stats->path_taken = GBSDF_PATH_FAST;
         stats->proposed = (long long)h.proposed;
-        stats->sweep_schedule = (map_a.valid || xsched == kXCpAsync) ? xsched : kXCpAsync;
+        // x schedule + 10 x walk schedule of what ran
+        stats->sweep_schedule = (map_a.valid ? xsched : kXCpAsync) + 10 * (map_a.walk_valid ? wsched : kWCpAsync);
     }
     return status;
 }

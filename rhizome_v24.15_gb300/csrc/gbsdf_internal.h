@@ -148,21 +148,32 @@ void launch_patch_mark(const Lattice& L, uint32_t* ubits, DevState* ds, cudaStre
 // when the lattice does not admit one (row pitch not a multiple of 16 bytes) or the
 // driver's encoder is unavailable; the x sweep then stages with cp.async.
 struct GridMap {
-    CUtensorMap map;
+    CUtensorMap map;   // x sweep tile: 8 (x) x 34 (y) x 10 (z), 32-byte swizzle
+    CUtensorMap ymap;  // y walk batch: 40 (x) x 4 (y slices) x 18 (z rows)
+    CUtensorMap zmap;  // z walk batch: 40 (x) x 18 (y rows) x 4 (z slices)
     bool valid;
+    bool walk_valid;
 };
 bool encode_grid_map(GridMap& m, const float* base, const Lattice& L);
 // Schedules of the x sweep (all give identical results): staged by per-thread cp.async
 // copies, by TMA tiles on a CTA-barrier ring, or by TMA tiles on a warp-specialised
 // mbarrier pipeline. 0 picks the pipeline when a TMA descriptor is valid.
 enum XSchedule : int { kXAuto = 0, kXCpAsync = 1, kXTmaRing = 2, kXTmaPipe = 3 };
+// Schedules of the y and z walks: cp.async slice ring, or TMA batches on a
+// warp-specialised mbarrier pipeline. 0 picks the pipeline when its descriptors are valid.
+enum WSchedule : int { kWAuto = 0, kWCpAsync = 1, kWTmaPipe = 2 };
 // `src_map`: the descriptor of `src` (or null); `x_schedule`: an XSchedule.
 void launch_sweep(int rule, int axis, int dir, int round, const float* src, float* dst, const Lattice& L,
-                  DevState* ds, cudaStream_t st, const GridMap* src_map = nullptr, int x_schedule = kXAuto);
-// The x-sweep schedule for this lattice class: the remembered winner, else (measure)
-// each candidate timed on src -> dst (writes dst and changed[63]), else the pipeline.
-int tuned_x_schedule(int device, const Lattice& L, const float* src, float* dst, const GridMap* src_map,
-                     DevState* ds, cudaStream_t st, bool measure);
+                  DevState* ds, cudaStream_t st, const GridMap* src_map = nullptr, int x_schedule = kXAuto,
+                  int w_schedule = kWAuto);
+// The sweep schedules for this lattice class: the remembered winners, else (measure)
+// each candidate timed on src -> dst (writes dst and changed[63]), else the pipelines.
+struct SweepPlan {
+    int x;  // XSchedule
+    int w;  // WSchedule
+};
+SweepPlan tuned_sweep_plan(int device, const Lattice& L, const float* src, float* dst, const GridMap* src_map,
+                           DevState* ds, cudaStream_t st, bool measure);
 // Layout check of the x sweep's TMA tile (swizzled rows, out-of-lattice fill): writes the
 // number of mismatching elements to *mism.
 int selftest_tma_tile(unsigned long long* mism);

@@ -648,6 +648,145 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
     mark_changed(ch, &ds->changed[round]);
 }
 
+// ---- y and z walks, TMA batches on a warp-specialised pipeline ------------------------
+// The lines, tile (32 x 16 lines, two per thread) and per-line arithmetic of
+// sweep_walk_kernel; the slices come in batches of 4, one cp.async.bulk.tensor copy per
+// batch issued by a producer warp into a ring of kWPS slots with full / empty mbarriers.
+// A batch box spans x0 - 4 .. x0 + 35 (its x start stays 16-byte aligned; the one-cell
+// halo sits at columns 3 and 36), 18 rows and 4 slices; out-of-lattice cells arrive as
+// NaN and the neighbour-pair minimum with the far sentinel turns them into it.
+constexpr int kWPX = 40;                               // box columns
+constexpr int kWPB = 4;                                // slices per batch
+constexpr int kWPS = 4;                                // ring slots
+constexpr int kWPBox = kWPX * kWHR * kWPB;             // floats per batch (2880)
+constexpr int kWPSlotBytes = 12288;                    // batch bytes rounded up to 1 KB
+constexpr int kWPThreads = kWThreads + 32;             // 8 consumer warps + 1 producer warp
+constexpr size_t kWPSmem = (size_t)kWPS * kWPSlotBytes + 128 + 1024;
+
+template <int AXIS, int RULE, int DIR>
+__global__ void __launch_bounds__(kWPThreads) sweep_walk_pipe_kernel(const __grid_constant__ CUtensorMap tm,
+                                                                      float* __restrict__ dst, Lattice L,
+                                                                      int round, DevState* ds) {
+    if (ds->stop) return;
+    extern __shared__ unsigned char tsm_raw[];
+    unsigned char* tsm = align1k(tsm_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kWPS * kWPSlotBytes);
+    uint64_t* empty = full + kWPS;
+    const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
+    const size_t plane = (size_t)dx * dy;
+    const int n_walk = (AXIS == 2) ? dz : dy;
+    const int n_rows = (AXIS == 2) ? dy : dz;
+    const size_t step_stride = (AXIS == 2) ? plane : (size_t)dx;
+    const size_t row_stride = (AXIS == 2) ? (size_t)dx : plane;
+    // shared-memory strides of a batch: box order is (x, y, z), x fastest
+    constexpr int kSliceS = (AXIS == 2) ? kWHR * kWPX : kWPX;   // next slice
+    constexpr int kRowS = (AXIS == 2) ? kWPX : kWPB * kWPX;     // next row
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * kWX, r0 = blockIdx.y * kWR;
+    const int nbatches = (n_walk + kWPB - 1) / kWPB;
+    if (tid == 0) {
+        for (int s = 0; s < kWPS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kWThreads / 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    if (tid >= kWThreads) {
+        if (tid != kWThreads) return;
+        int b = 0;
+        for (; b < nbatches; ++b) {
+            const int s = b % kWPS;
+            if (b >= kWPS && !mbar_wait(&empty[s], ((b / kWPS) - 1) & 1)) break;
+            // lattice slices of this batch (walk order 4b .. 4b + 3)
+            const int sl0 = (DIR > 0) ? b * kWPB : n_walk - kWPB - b * kWPB;
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            mbar_expect_tx(&full[s], kWPBox * 4);
+            if (AXIS == 2) tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, r0 - 1, sl0, &full[s]);
+            else tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, sl0, r0 - 1, &full[s]);
+        }
+        if (b < nbatches) {
+            for (int k = max(0, b - kWPS); k < b; ++k) mbar_wait(&full[k % kWPS], (k / kWPS) & 1);
+            atomicAdd(&ds->wait_timeouts, 1ull);
+        }
+        return;
+    }
+    const int tx = tid & 31, tr = tid >> 5;
+    const int x = x0 + tx;
+    const int ra = r0 + tr, rb = r0 + tr + 8;
+    const bool act_a = (x < dx) && (ra < n_rows), act_b = (x < dx) && (rb < n_rows);
+    const float h = L.h;
+    // element of line a in slice q (box order) is tile[q * kSliceS + ma]
+    const int ma = (tr + 1) * kRowS + (tx + 4), mb = ma + 8 * kRowS;
+    auto slice_ptr = [&](int s) -> const float* {  // s in walk order
+        const int b = s / kWPB, q = s - b * kWPB;
+        const int qb = (DIR > 0) ? q : (kWPB - 1 - q);
+        return reinterpret_cast<const float*>(tsm + (b % kWPS) * kWPSlotBytes) + qb * kSliceS;
+    };
+    float prev_a = kFarSentinel, prev_b = kFarSentinel;
+    float cur_a = 0.0f, cur_b = 0.0f;
+    bool ch = false;
+    const long long sstep = (DIR > 0) ? (long long)step_stride : -(long long)step_stride;
+    float* pa = dst + (size_t)((DIR > 0) ? 0 : n_walk - 1) * step_stride + (size_t)ra * row_stride + x;
+    float* pb = dst + (size_t)((DIR > 0) ? 0 : n_walk - 1) * step_stride + (size_t)rb * row_stride + x;
+#pragma unroll 1
+    for (int b = 0; b < nbatches; ++b) {
+        bool ok = mbar_wait(&full[b % kWPS], (b / kWPS) & 1);
+        if (ok && b + 1 < nbatches) ok = mbar_wait(&full[(b + 1) % kWPS], ((b + 1) / kWPS) & 1);
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (tx == 0) atomicAdd(&ds->wait_timeouts, 1ull);
+            return;
+        }
+        if (b == 0) {
+            cur_a = slice_ptr(0)[ma];
+            cur_b = slice_ptr(0)[mb];
+        }
+#pragma unroll
+        for (int q = 0; q < kWPB; ++q) {
+            const int s = b * kWPB + q;
+            if (s >= n_walk) break;
+            const float* cs = slice_ptr(s);
+            const bool has_next = (s + 1 < n_walk);
+            const float* ns = has_next ? slice_ptr(s + 1) : cs;
+            const float nxt_a = has_next ? ns[ma] : kFarSentinel;
+            const float nxt_b = has_next ? ns[mb] : kFarSentinel;
+            if (act_a) {
+                const float ax = fminf(fminf(cs[ma - 1], cs[ma + 1]), kFarSentinel);
+                const float ar = fminf(fminf(cs[ma - kRowS], cs[ma + kRowS]), kFarSentinel);
+                const float al = fminf(prev_a, nxt_a);
+                const float u = (AXIS == 2) ? godunov<RULE>(ax, ar, al, h) : godunov<RULE>(ax, al, ar, h);
+                float out = cur_a;
+                if (u < cur_a) {
+                    out = u;
+                    ch = true;
+                }
+                *pa = out;
+                prev_a = out;
+            }
+            if (act_b) {
+                const float ax = fminf(fminf(cs[mb - 1], cs[mb + 1]), kFarSentinel);
+                const float ar = fminf(fminf(cs[mb - kRowS], cs[mb + kRowS]), kFarSentinel);
+                const float al = fminf(prev_b, nxt_b);
+                const float u = (AXIS == 2) ? godunov<RULE>(ax, ar, al, h) : godunov<RULE>(ax, al, ar, h);
+                float out = cur_b;
+                if (u < cur_b) {
+                    out = u;
+                    ch = true;
+                }
+                *pb = out;
+                prev_b = out;
+            }
+            cur_a = nxt_a;
+            cur_b = nxt_b;
+            pa += sstep;
+            pb += sstep;
+        }
+        __syncwarp();
+        if (tx == 0) mbar_arrive(&empty[b % kWPS]);
+    }
+    mark_changed(ch, &ds->changed[round]);
+}
+
 // Layout check of the staged tile: one CTA loads the box at (x, y, z) of a grid whose
 // cells hold their own linear index, and every thread compares elements (scalar reads
 // through tsw, vector reads through tvec) with the expected value or NaN outside.
@@ -761,13 +900,30 @@ __global__ void __launch_bounds__(256) apply_kernel(const float* __restrict__ g,
 
 template <int RULE, int DIR>
 void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lattice& L, DevState* ds,
-                    cudaStream_t st, const GridMap* src_map, int xsched) {
+                    cudaStream_t st, const GridMap* src_map, int xsched, int wsched) {
     const bool tma = src_map && src_map->valid;
     if (xsched == 0) xsched = tma ? kXTmaPipe : kXCpAsync;
     if (!tma) xsched = kXCpAsync;
+    const bool wtma = src_map && src_map->walk_valid;
+    if (wsched == 0) wsched = wtma ? kWTmaPipe : kWCpAsync;
+    if (!wtma) wsched = kWCpAsync;
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
     GBSDF_COUNT_LAUNCH();
-    if (axis == 2) {
+    if (axis != 0 && wsched == kWTmaPipe) {
+        const int n_rows = (axis == 2) ? dy : dz;
+        dim3 grid((dx + kWX - 1) / kWX, (n_rows + kWR - 1) / kWR);
+        if (axis == 2) {
+            cudaFuncSetAttribute(sweep_walk_pipe_kernel<2, RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kWPSmem);
+            sweep_walk_pipe_kernel<2, RULE, DIR><<<grid, kWPThreads, kWPSmem, st>>>(src_map->zmap, dst, L, round,
+                                                                                  ds);
+        } else {
+            cudaFuncSetAttribute(sweep_walk_pipe_kernel<1, RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kWPSmem);
+            sweep_walk_pipe_kernel<1, RULE, DIR><<<grid, kWPThreads, kWPSmem, st>>>(src_map->ymap, dst, L, round,
+                                                                                  ds);
+        }
+    } else if (axis == 2) {
         dim3 grid((dx + kWX - 1) / kWX, (dy + kWR - 1) / kWR);
         cudaFuncSetAttribute(sweep_walk_kernel<2, RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kWSmem);
@@ -813,15 +969,16 @@ EncodeTiledFn tiled_encoder() {
     return fn;
 }
 
-bool encode_box(CUtensorMap* m, const float* base, int dx, int dy, int dz) {
+bool encode_box(CUtensorMap* m, const float* base, int dx, int dy, int dz, int bx = kXC, int by = kXHY,
+                int bz = kXHZ, CUtensorMapSwizzle sw = CU_TENSOR_MAP_SWIZZLE_32B) {
     EncodeTiledFn fn = tiled_encoder();
     if (!fn) return false;
     const cuuint64_t gdim[3] = {(cuuint64_t)dx, (cuuint64_t)dy, (cuuint64_t)dz};
     const cuuint64_t gstride[2] = {(cuuint64_t)dx * 4, (cuuint64_t)dx * dy * 4};
-    const cuuint32_t box[3] = {(cuuint32_t)kXC, (cuuint32_t)kXHY, (cuuint32_t)kXHZ};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
     const cuuint32_t estr[3] = {1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), gdim, gstride, box, estr,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NAN_REQUEST_ZERO_FMA) == CUDA_SUCCESS;
 }
 
@@ -829,20 +986,26 @@ bool encode_box(CUtensorMap* m, const float* base, int dx, int dy, int dz) {
 
 bool encode_grid_map(GridMap& m, const float* base, const Lattice& L) {
     m.valid = false;
+    m.walk_valid = false;
     // row and plane pitches must be multiples of 16 bytes, the base 16-byte aligned
     if ((L.dims[0] & 3) != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
     m.valid = encode_box(&m.map, base, L.dims[0], L.dims[1], L.dims[2]);
+    m.walk_valid = m.valid &&
+                   encode_box(&m.ymap, base, L.dims[0], L.dims[1], L.dims[2], kWPX, kWPB, kWHR,
+                              CU_TENSOR_MAP_SWIZZLE_NONE) &&
+                   encode_box(&m.zmap, base, L.dims[0], L.dims[1], L.dims[2], kWPX, kWHR, kWPB,
+                              CU_TENSOR_MAP_SWIZZLE_NONE);
     return m.valid;
 }
 
 void launch_sweep(int rule, int axis, int dir, int round, const float* src, float* dst, const Lattice& L,
-                  DevState* ds, cudaStream_t st, const GridMap* src_map, int x_schedule) {
+                  DevState* ds, cudaStream_t st, const GridMap* src_map, int x_schedule, int w_schedule) {
     if (rule == 0) {
-        if (dir > 0) launch_sweep_t<0, 1>(axis, round, src, dst, L, ds, st, src_map, x_schedule);
-        else launch_sweep_t<0, -1>(axis, round, src, dst, L, ds, st, src_map, x_schedule);
+        if (dir > 0) launch_sweep_t<0, 1>(axis, round, src, dst, L, ds, st, src_map, x_schedule, w_schedule);
+        else launch_sweep_t<0, -1>(axis, round, src, dst, L, ds, st, src_map, x_schedule, w_schedule);
     } else {
-        if (dir > 0) launch_sweep_t<1, 1>(axis, round, src, dst, L, ds, st, src_map, x_schedule);
-        else launch_sweep_t<1, -1>(axis, round, src, dst, L, ds, st, src_map, x_schedule);
+        if (dir > 0) launch_sweep_t<1, 1>(axis, round, src, dst, L, ds, st, src_map, x_schedule, w_schedule);
+        else launch_sweep_t<1, -1>(axis, round, src, dst, L, ds, st, src_map, x_schedule, w_schedule);
     }
 }
 

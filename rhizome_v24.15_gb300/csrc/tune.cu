@@ -1,10 +1,11 @@
 // tune.cu — the sweep-schedule autotuner.
 //
-// The x sweep has three schedules with identical results (internal header, XSchedule).
-// Which one is fastest depends on the lattice (row length, number of CTAs per wave) and
-// the device, so the first build of a lattice class times each candidate on that build's
-// own buffers -- the band field about to be swept, one warm-up and two timed launches
-// each, CUDA events on the build's stream -- and remembers the winner for the class.
+// The x sweep has three schedules and the y / z walks two, all with identical results
+// (internal header, XSchedule / WSchedule). Which is fastest depends on the lattice (row
+// length, CTAs per wave) and the device, so the first build of a lattice class times each
+// candidate on that build's own buffers -- the band field about to be swept, one warm-up
+// and two timed launches each (x sweeps for the x schedules, z walks for the walk
+// schedules), CUDA events on the build's stream -- and remembers the winners.
 // A class is (device, row pitch a multiple of 16 bytes, round(log2 voxels), round(log2
 // row length)). Timing writes only the destination copy and one change-flag slot, both
 // rewritten by the eikonal stage that follows.
@@ -21,7 +22,7 @@ namespace {
 
 using Key = std::tuple<int, int, int, int>;
 std::mutex g_tune_mu;
-std::map<Key, int> g_tuned;
+std::map<Key, SweepPlan> g_tuned;
 
 Key key_of(int device, const Lattice& L) {
     return Key{device, (L.dims[0] & 3) == 0 ? 1 : 0, (int)std::lround(std::log2((double)L.N)),
@@ -30,50 +31,68 @@ Key key_of(int device, const Lattice& L) {
 
 }  // namespace
 
-int tuned_x_schedule(int device, const Lattice& L, const float* src, float* dst, const GridMap* src_map,
-                     DevState* ds, cudaStream_t st, bool measure) {
-    const bool tma = src_map && src_map->valid;
-    if (!tma) return kXCpAsync;
+SweepPlan tuned_sweep_plan(int device, const Lattice& L, const float* src, float* dst, const GridMap* src_map,
+                           DevState* ds, cudaStream_t st, bool measure) {
+    SweepPlan plan{kXCpAsync, kWCpAsync};
+    const bool tma = src_map && src_map->valid, wtma = src_map && src_map->walk_valid;
+    if (!tma && !wtma) return plan;
     const Key k = key_of(device, L);
     {
         std::lock_guard<std::mutex> g(g_tune_mu);
         auto it = g_tuned.find(k);
         if (it != g_tuned.end()) return it->second;
     }
-    if (!measure) return kXTmaPipe;
+    plan = SweepPlan{tma ? kXTmaPipe : kXCpAsync, wtma ? kWTmaPipe : kWCpAsync};
+    if (!measure) return plan;
     cudaEvent_t a, b;
     if (cudaEventCreate(&a) != cudaSuccess) {
         cudaGetLastError();
-        return kXTmaPipe;
+        return plan;
     }
     if (cudaEventCreate(&b) != cudaSuccess) {
         cudaGetLastError();
         cudaEventDestroy(a);
-        return kXTmaPipe;
+        return plan;
     }
-    int best = kXTmaPipe;
-    float best_ms = 1e30f;
     const int slot = 63;  // a change-flag slot the reference round loop never uses
-    for (int cand : {kXCpAsync, kXTmaRing, kXTmaPipe}) {
-        launch_sweep(0, 0, 1, slot, src, dst, L, ds, st, src_map, cand);
+    // one warm-up and two timed launches of one directional sweep; < 0 on failure
+    auto time_it = [&](int axis, int xs, int ws) -> float {
+        launch_sweep(0, axis, 1, slot, src, dst, L, ds, st, src_map, xs, ws);
         cudaEventRecord(a, st);
-        for (int r = 0; r < 2; ++r) launch_sweep(0, 0, 1, slot, src, dst, L, ds, st, src_map, cand);
+        for (int r = 0; r < 2; ++r) launch_sweep(0, axis, 1, slot, src, dst, L, ds, st, src_map, xs, ws);
         cudaEventRecord(b, st);
-        float ms = 1e30f;
+        float ms = -1.0f;
         if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
             cudaGetLastError();
-            continue;
+            return -1.0f;
         }
-        if (ms < best_ms) {
-            best_ms = ms;
-            best = cand;
+        return ms;
+    };
+    if (tma) {
+        float best = 1e30f;
+        for (int cand : {kXCpAsync, kXTmaRing, kXTmaPipe}) {
+            const float ms = time_it(0, cand, plan.w);
+            if (ms >= 0.0f && ms < best) {
+                best = ms;
+                plan.x = cand;
+            }
+        }
+    }
+    if (wtma) {
+        float best = 1e30f;
+        for (int cand : {kWCpAsync, kWTmaPipe}) {
+            const float ms = time_it(2, plan.x, cand);
+            if (ms >= 0.0f && ms < best) {
+                best = ms;
+                plan.w = cand;
+            }
         }
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     std::lock_guard<std::mutex> g(g_tune_mu);
-    g_tuned[k] = best;
-    return best;
+    g_tuned[k] = plan;
+    return plan;
 }
 
 }  // namespace gbsdf

@@ -1,6 +1,7 @@
-"""The x-sweep schedules (cp.async-staged, TMA tiles on a CTA-barrier ring, TMA tiles on a
-warp-specialised mbarrier pipeline) and the autotuner's pick give bit-identical grids,
-equal to the oracle, on lattices whose rows do and do not admit a TMA descriptor."""
+"""The eikonal sweep schedules -- x sweep staged by cp.async, by TMA tiles on a CTA-barrier
+ring or on a warp-specialised mbarrier pipeline; y / z walks staged by cp.async or by TMA
+batches on a pipeline -- and the autotuner's pick give bit-identical grids, equal to the
+oracle, on lattices whose rows do and do not admit TMA descriptors."""
 import numpy as np
 import pytest
 
@@ -14,20 +15,24 @@ def _case(dims):
     return tris, mn, mx, h
 
 
-@pytest.mark.parametrize("dims", [(96, 88, 92), (97, 83, 90), (44, 260, 30)])
+@pytest.mark.parametrize("dims", [(96, 88, 92), (97, 83, 90), (44, 260, 30), (200, 36, 70)])
 def test_schedules_identical(engine, oracle, dims):
     tris, mn, mx, h = _case(dims)
     outs = {}
-    for sched in (0, 1, 2, 3):
+    for sched in (0, 1, 2, 3, 4, 5):
         out, res = engine.compute_mesh_sdf(tris, h, mn, mx, mode=engine.MODE_EXACT_SIGNS, path=engine.PATH_FAST,
                                            sweep_schedule=sched)
         assert res.ok
         outs[sched] = out
-        expect = sched if sched else res.stats["sweep_schedule"]
+        ran = res.stats["sweep_schedule"]
+        x, w = ran % 10, ran // 10
         if dims[0] % 4:
-            expect = 1  # no TMA descriptor: the cp.async schedule runs
-        assert res.stats["sweep_schedule"] == expect
-    for sched in (1, 2, 3):
+            assert (x, w) == (1, 1)  # no TMA descriptor: the cp.async schedules run
+        elif sched in (1, 2, 3):
+            assert x == sched
+        elif sched in (4, 5):
+            assert (x, w) == (3, sched - 3)
+    for sched in (1, 2, 3, 4, 5):
         assert np.array_equal(outs[0].view(np.uint32), outs[sched].view(np.uint32)), sched
     st, ref, _, _ = oracle.fast_sdf(tris, h, mn, mx, fsm_mode=0, gwn_mode=1, signed_parity=True)
     assert st == oracle.OK
