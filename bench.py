@@ -369,7 +369,7 @@ def main():
                        "l2": "inputs larger than L2 (2.6 GB grid per step)"},
             "e2e": None if e2e is None else {"value": e2e, "unit": UNIT, "ms_per_step": e2e_ms,
                                              "h2d_bytes_per_step": int(T * 48), "d2h_bytes_per_step": int(N * 4)},
-            "roofline": {"kernel": "eikonal lockstep sweep (sweep_x/y/z)", "bound": "hbm", "achieved": achieved,
+            "roofline": {"kernel": "eikonal directional sweep (sweep_x_pipe / sweep_walk_pipe, autotuned)", "bound": "hbm", "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes,
                          "launch_ms": per_launch_ms},
