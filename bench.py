@@ -180,6 +180,39 @@ def run_batched(gbsdf, torch, dev, mode, steps, warmup, local):
     return res
 
 
+def run_decode(gbsdf, steps):
+    """The wire-format decoders on the bench mug (179,840 triangles): binary STL (decode +
+    weld) and OBJ text, through the public API (host bytes in, host arrays out, device
+    allocation per call as in the reference), against the oracle's single-threaded CPU
+    restatement of the reference's decoders. Host wall-clock per call, median of K."""
+    from gbsdf import meshgen
+    from oracle import oracle as O
+
+    kw, _, _ = meshgen.WORKLOADS[WORKLOAD]
+    kw = {k: v for k, v in kw.items() if k != "kind"}
+    v, f = meshgen.mug(**kw)
+    stl = meshgen.to_binary_stl(v, f)
+    obj = meshgen.to_obj_text(v, f, fancy=False)
+    res = {}
+    for name, data, gpu, cpu in (("binary_stl", stl, gbsdf.parse_binary_stl, O.parse_binary_stl),
+                                 ("obj", obj, gbsdf.parse_obj, O.parse_obj)):
+        gpu(data)  # warm-up (context, module load)
+        ts = []
+        for _ in range(max(3, steps)):
+            t0 = time.perf_counter()
+            gpu(data)
+            ts.append(time.perf_counter() - t0)
+        tc = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            cpu(data)
+            tc.append(time.perf_counter() - t0)
+        g, c = float(np.median(ts)), float(np.median(tc))
+        res[name] = {"bytes": len(data), "gpu_ms": g * 1e3, "gpu_mb_s": len(data) / g / 1e6, "cpu_ms": c * 1e3,
+                     "cpu_mb_s": len(data) / c / 1e6, "cpu_threads": 1}
+    return res
+
+
 def cpu_baseline(tris, mn, mx, h, z_slab=64, threads=None):
     """The oracle's restatement of the reference path (CPU), bounded to a z-slab of
     the lattice through the middle of the mug. Returns (Gvox/s, seconds, sample desc)."""
@@ -384,6 +417,8 @@ def main():
             "gpu_launches": int(sum(s["kernel_launches"] for s in stats))}
     if mode == gbsdf.MODE_LEARNED:
         line["pipeline"]["proposed_bricks"] = s0["proposed"]
+    if rank == 0 and not args.no_batch:
+        line["decode"] = run_decode(gbsdf, args.steps)
     if not args.no_batch and mode in (gbsdf.MODE_REFERENCE, gbsdf.MODE_EXACT_SIGNS):
         line["batched"] = run_batched(gbsdf, torch, dev, mode, args.steps, args.warmup, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

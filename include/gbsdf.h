@@ -231,6 +231,30 @@ int gbsdf_mlp_backward(const float* params_dev, const float* features_dev, const
 int gbsdf_mlp_adam(float* params_dev, const float* grad_dev, float* m_dev, float* v_dev, float lr, float beta1,
                    float beta2, float eps, float grad_scale, int32_t step, int32_t device, char* err, size_t errlen);
 
+/* Mesh wire formats. Both decode on the GPU of `device` and
+ * write host arrays; vertices are x, y, z floats, indices 3 per triangle.
+ *
+ * Replaces CudaRasterizer::parse_binary_stl_gpu (cuda_mesh_io.cu:592-722, record decode
+ * :524-590): 80-byte header, uint32 triangle count, 50-byte records. Vertices are welded
+ * on round(coordinate * 10000) keys in first-occurrence order and triangles whose welded
+ * corners repeat are dropped, as the reference's host weld does -- here on the GPU.
+ * out_vertices / out_indices must hold 3 x T entries (T from the header); out_normals
+ * (3 x T floats, may be NULL) receives every record's normal, normalised with the
+ * reference's fallbacks. An empty STL (T = 0) succeeds with no output. */
+int gbsdf_parse_binary_stl(const uint8_t* bytes, size_t n_bytes, float* out_vertices, int64_t vertex_capacity,
+                           uint32_t* out_indices, int64_t index_capacity, float* out_normals, int64_t* n_vertices,
+                           int64_t* n_indices, int32_t device, char* err, size_t errlen);
+
+/* Replaces CudaRasterizer::parse_obj_text_gpu (cuda_mesh_io.cu:962-1090): lines starting
+ * "v " (three numbers) and "f " (up to four 1-based or negative indices; quads split
+ * (0,1,2) (0,2,3)), at most n_bytes / 10 + 1024 of each in file order, triangles in file
+ * order. Capacities of n_bytes / 10 + 1024 vertices and 6 times that many indices always
+ * suffice. GBSDF_EINVAL when the text holds no vertex, face or triangle (the reference
+ * returns false) or an output is too small (the counts needed are written). */
+int gbsdf_parse_obj(const char* text, size_t n_bytes, float* out_vertices, int64_t vertex_capacity,
+                    uint32_t* out_indices, int64_t index_capacity, int64_t* n_vertices, int64_t* n_indices,
+                    int32_t device, char* err, size_t errlen);
+
 /* Releases the cached device workspace of `device` (buffers are otherwise reused
  * across calls on the same device). */
 void gbsdf_release_workspace(int32_t device);

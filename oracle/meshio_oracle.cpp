@@ -1,0 +1,241 @@
+// meshio_oracle.cpp — TEST INFRASTRUCTURE ONLY: CPU restatement of the reference's mesh
+// decoders (native/src/engine/io/cuda_mesh_io.cu), the checker of the engine's GPU
+// decoders (rhizome_v24.15_gb300/csrc/k_io.cu). Never linked into the product.
+//
+// * binary STL: CudaRasterizer::parse_binary_stl_gpu (cuda_mesh_io.cu:592-722) with the
+//   record decode of gpu_decode_binary_stl_kernel (:524-590): 80-byte header, uint32
+//   triangle count, 50-byte records (normal, 3 vertices, attribute); normals normalised
+//   (geometric fallback, then +z); vertices welded on round(coordinate * 10000) keys in
+//   first-occurrence order (:675-708); triangles whose welded corners repeat are dropped.
+// * ASCII OBJ: CudaRasterizer::parse_obj_text_gpu (cuda_mesh_io.cu:962-1090) with
+//   gpu_find_obj_lines_kernel (:859-888), gpu_parse_obj_vertices_kernel (:890-907),
+//   gpu_parse_obj_faces_kernel (:909-960) and device_fast_atof / _atoi (:810-857): lines
+//   starting "v " / "f " in file order (at most text_length / 10 + 1024 of each), three
+//   numbers per vertex, up to four 1-based (or negative, relative) indices per face, quads
+//   split (0,1,2) (0,2,3).
+// Every expression is restated as written in the reference source, each operation rounded
+// once (compile with -ffp-contract=off; oracle.py does), the same convention as the engine
+// (-fmad=false). A build of the reference that fuses multiply-adds can differ from this by
+// an ulp in parsed coordinates and normals.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+struct QKey {
+    int32_t x, y, z;
+    bool operator==(const QKey& o) const { return x == o.x && y == o.y && z == o.z; }
+};
+struct QHash {
+    size_t operator()(const QKey& k) const {
+        return (size_t)((uint64_t)(uint32_t)k.x * 0x9E3779B97F4A7C15ull ^ (uint64_t)(uint32_t)k.y * 0xC2B2AE3D27D4EB4Full ^
+                        (uint64_t)(uint32_t)k.z * 0x165667B19E3779F9ull);
+    }
+};
+
+float rd_f32(const uint8_t* p) {
+    float v;
+    std::memcpy(&v, p, 4);
+    return v;
+}
+
+int32_t quant(float v) { return (int32_t)std::round(v * 10000.0f); }
+
+// device_fast_atof (cuda_mesh_io.cu:810-843)
+float fast_atof(const char*& p) {
+    while (*p == ' ' || *p == '\t') ++p;
+    float sign = 1.0f;
+    if (*p == '-') {
+        sign = -1.0f;
+        ++p;
+    } else if (*p == '+') {
+        ++p;
+    }
+    float val = 0.0f;
+    while (*p >= '0' && *p <= '9') {
+        val = val * 10.0f + (float)(*p - '0');
+        ++p;
+    }
+    if (*p == '.') {
+        ++p;
+        float factor = 0.1f;
+        while (*p >= '0' && *p <= '9') {
+            val += (float)(*p - '0') * factor;
+            factor *= 0.1f;
+            ++p;
+        }
+    }
+    if (*p == 'e' || *p == 'E') {
+        ++p;
+        float es = 1.0f;
+        if (*p == '-') {
+            es = -1.0f;
+            ++p;
+        } else if (*p == '+') {
+            ++p;
+        }
+        int ev = 0;
+        while (*p >= '0' && *p <= '9') {
+            ev = ev * 10 + (*p - '0');
+            ++p;
+        }
+        val *= std::pow(10.0f, es * (float)ev);
+    }
+    return sign * val;
+}
+
+// device_fast_atoi (cuda_mesh_io.cu:845-857)
+int fast_atoi(const char*& p) {
+    while (*p == ' ' || *p == '\t') ++p;
+    int sign = 1;
+    if (*p == '-') {
+        sign = -1;
+        ++p;
+    } else if (*p == '+') {
+        ++p;
+    }
+    int val = 0;
+    while (*p >= '0' && *p <= '9') {
+        val = val * 10 + (*p - '0');
+        ++p;
+    }
+    return sign * val;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Returns 0 on success, 1 on a malformed buffer (shorter than its header says).
+int orc_parse_binary_stl(const uint8_t* bytes, size_t n, float* verts, uint32_t* idx, float* normals, int64_t* nv,
+                         int64_t* ni) {
+    *nv = 0;
+    *ni = 0;
+    if (n < 84) return 1;
+    uint32_t T = 0;
+    std::memcpy(&T, bytes + 80, 4);
+    if (T == 0) return 0;
+    if (n < 84 + (size_t)T * 50) return 1;
+    std::unordered_map<QKey, uint32_t, QHash> map;
+    map.reserve((size_t)T * 3);
+    int64_t V = 0, I = 0;
+    for (uint32_t t = 0; t < T; ++t) {
+        const uint8_t* rec = bytes + 84 + (size_t)t * 50;
+        float nx = rd_f32(rec), ny = rd_f32(rec + 4), nz = rd_f32(rec + 8);
+        float v[3][3];
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 3; ++c) v[k][c] = rd_f32(rec + 12 + 12 * k + 4 * c);
+        const float len = std::sqrt(nx * nx + ny * ny + nz * nz);
+        if (len > 1e-7f) {
+            nx /= len;
+            ny /= len;
+            nz /= len;
+        } else {
+            const float e1x = v[1][0] - v[0][0], e1y = v[1][1] - v[0][1], e1z = v[1][2] - v[0][2];
+            const float e2x = v[2][0] - v[0][0], e2y = v[2][1] - v[0][1], e2z = v[2][2] - v[0][2];
+            nx = e1y * e2z - e1z * e2y;
+            ny = e1z * e2x - e1x * e2z;
+            nz = e1x * e2y - e1y * e2x;
+            const float gl = std::sqrt(nx * nx + ny * ny + nz * nz);
+            if (gl > 1e-7f) {
+                nx /= gl;
+                ny /= gl;
+                nz /= gl;
+            } else {
+                nx = 0.0f;
+                ny = 0.0f;
+                nz = 1.0f;
+            }
+        }
+        if (normals) {
+            normals[3 * t] = nx;
+            normals[3 * t + 1] = ny;
+            normals[3 * t + 2] = nz;
+        }
+        uint32_t id[3];
+        for (int k = 0; k < 3; ++k) {
+            const QKey q{quant(v[k][0]), quant(v[k][1]), quant(v[k][2])};
+            auto it = map.find(q);
+            if (it != map.end()) {
+                id[k] = it->second;
+            } else {
+                id[k] = (uint32_t)V;
+                map.emplace(q, id[k]);
+                for (int c = 0; c < 3; ++c) verts[3 * V + c] = v[k][c];
+                ++V;
+            }
+        }
+        if (id[0] != id[1] && id[1] != id[2] && id[2] != id[0]) {
+            idx[I++] = id[0];
+            idx[I++] = id[1];
+            idx[I++] = id[2];
+        }
+    }
+    *nv = V;
+    *ni = I;
+    return 0;
+}
+
+// Returns 0 on success, 1 when the text holds no vertex or face line or no triangle.
+// verts / idx must hold (n / 10 + 1024) * 3 floats / (n / 10 + 1024) * 6 indices.
+int orc_parse_obj(const char* text_in, size_t n, float* verts, uint32_t* idx, int64_t* nv, int64_t* ni) {
+    *nv = 0;
+    *ni = 0;
+    if (n == 0 || !text_in) return 1;
+    std::vector<char> text(text_in, text_in + n);
+    text.push_back('\0');
+    const size_t max_lines = n / 10 + 1024;
+    std::vector<size_t> vo, fo;
+    for (size_t i = 0; i + 1 < n; ++i) {
+        const bool start = (i == 0) || text[i - 1] == '\n';
+        if (!start) continue;
+        if (text[i] == 'v' && text[i + 1] == ' ') {
+            if (vo.size() < max_lines) vo.push_back(i + 2);
+        } else if (text[i] == 'f' && text[i + 1] == ' ') {
+            if (fo.size() < max_lines) fo.push_back(i + 2);
+        }
+    }
+    if (vo.empty() || fo.empty()) return 1;
+    const int64_t V = (int64_t)vo.size();
+    for (int64_t k = 0; k < V; ++k) {
+        const char* p = text.data() + vo[k];
+        verts[3 * k] = fast_atof(p);
+        verts[3 * k + 1] = fast_atof(p);
+        verts[3 * k + 2] = fast_atof(p);
+    }
+    int64_t I = 0;
+    for (size_t k = 0; k < fo.size(); ++k) {
+        const char* p = text.data() + fo[k];
+        int f[4];
+        int c = 0;
+        while (*p != '\n' && *p != '\r' && *p != '\0' && c < 4) {
+            while (*p == ' ' || *p == '\t') ++p;
+            if (*p == '\n' || *p == '\r' || *p == '\0') break;
+            int vi = fast_atoi(p);
+            while (*p != ' ' && *p != '\t' && *p != '\n' && *p != '\r' && *p != '\0') ++p;
+            if (vi < 0) vi = (int)V + vi + 1;
+            if (vi > 0) f[c++] = vi - 1;
+        }
+        if (c == 3) {
+            idx[I++] = (uint32_t)f[0];
+            idx[I++] = (uint32_t)f[1];
+            idx[I++] = (uint32_t)f[2];
+        } else if (c == 4) {
+            idx[I++] = (uint32_t)f[0];
+            idx[I++] = (uint32_t)f[1];
+            idx[I++] = (uint32_t)f[2];
+            idx[I++] = (uint32_t)f[0];
+            idx[I++] = (uint32_t)f[2];
+            idx[I++] = (uint32_t)f[3];
+        }
+    }
+    if (I == 0) return 1;
+    *nv = V;
+    *ni = I;
+    return 0;
+}
+
+}  // extern "C"

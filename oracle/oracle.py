@@ -19,6 +19,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "liboracle.so"
 SRC = HERE / "sdf_oracle.cpp"
+SRCS = [SRC, HERE / "meshio_oracle.cpp"]
 REF_LIB_PATH = HERE / "_ref" / "libref_math.so"
 
 # fast-path status codes (orc_fast_stats.status)
@@ -27,9 +28,9 @@ OK, INVALID, INT_GUARD, CSR_GUARD, VERIFY_DIVERGED = 0, 1, 2, 3, 4
 
 def build(force: bool = False) -> Path:
     """Compile the oracle with g++ (no FP contraction, so x86 and Arm agree)."""
-    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < SRC.stat().st_mtime:
+    if force or not LIB_PATH.exists() or any(LIB_PATH.stat().st_mtime < p.stat().st_mtime for p in SRCS):
         cmd = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
-               str(SRC), "-o", str(LIB_PATH)]
+               *map(str, SRCS), "-o", str(LIB_PATH)]
         subprocess.check_call(cmd)
     return LIB_PATH
 
@@ -255,3 +256,33 @@ def ref_lib():
         return None
     L = C.CDLL(str(REF_LIB_PATH))
     return L
+
+
+def parse_binary_stl(data: bytes):
+    """Binary STL decode + weld (cuda_mesh_io.cu:524-722). Returns (status, vertices (V,3),
+    indices (I,), normals (T,3))."""
+    b = np.frombuffer(data, np.uint8)
+    T = int(np.frombuffer(data[80:84], np.uint32)[0]) if len(data) >= 84 else 0
+    verts = np.zeros((max(3 * T, 1), 3), np.float32)
+    idx = np.zeros(max(3 * T, 1), np.uint32)
+    normals = np.zeros((max(T, 1), 3), np.float32)
+    nv, ni = C.c_int64(0), C.c_int64(0)
+    L = lib()
+    L.orc_parse_binary_stl.restype = C.c_int
+    st = L.orc_parse_binary_stl(_p(b), C.c_size_t(len(data)), _p(verts), _p(idx), _p(normals), C.byref(nv),
+                                C.byref(ni))
+    return st, verts[:nv.value], idx[:ni.value], normals[:T]
+
+
+def parse_obj(text: bytes):
+    """ASCII OBJ decode (cuda_mesh_io.cu:859-1090). Returns (status, vertices (V,3), indices (I,))."""
+    n = len(text)
+    cap = n // 10 + 1024
+    buf = np.frombuffer(text, np.uint8)
+    verts = np.zeros((cap, 3), np.float32)
+    idx = np.zeros(cap * 6, np.uint32)
+    nv, ni = C.c_int64(0), C.c_int64(0)
+    L = lib()
+    L.orc_parse_obj.restype = C.c_int
+    st = L.orc_parse_obj(_p(buf), C.c_size_t(n), _p(verts), _p(idx), C.byref(nv), C.byref(ni))
+    return st, verts[:nv.value], idx[:ni.value]

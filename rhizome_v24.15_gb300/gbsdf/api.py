@@ -24,7 +24,8 @@ from . import _lib
 from ._lib import (MODE_EXACT, MODE_EXACT_SIGNS, MODE_LEARNED, MODE_REFERENCE, PATH_AUTO, PATH_FAST, PATH_LEGACY,
                    STATUS_NAMES)
 
-__all__ = ["GbsdfError", "Result", "Batch", "compute_mesh_sdf", "compute_mesh_sdf_batch", "mesh_lattice", "build_from_mesh", "CudaRasterizer",
+__all__ = ["GbsdfError", "Result", "Batch", "compute_mesh_sdf", "compute_mesh_sdf_batch", "parse_binary_stl",
+           "parse_obj", "mesh_lattice", "build_from_mesh", "CudaRasterizer",
            "CudaVolumeGrid", "MODE_REFERENCE", "MODE_EXACT", "MODE_EXACT_SIGNS", "MODE_LEARNED", "PATH_AUTO", "PATH_FAST",
            "PATH_LEGACY"]
 
@@ -253,6 +254,40 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def parse_binary_stl(data: bytes, device=0, normals=False):
+    """GPU decode + weld of a binary STL (gbsdf_parse_binary_stl). Returns (vertices (V,3)
+    float32, indices (I,) uint32) and, with ``normals``, the (T,3) record normals."""
+    b = np.frombuffer(data, np.uint8)
+    T = int(np.frombuffer(data[80:84], np.uint32)[0]) if len(data) >= 84 else 0
+    verts = np.empty((max(3 * T, 1), 3), np.float32)
+    idx = np.empty(max(3 * T, 1), np.uint32)
+    nrm = np.empty((max(T, 1), 3), np.float32)
+    nv, ni = C.c_int64(0), C.c_int64(0)
+    err = C.create_string_buffer(512)
+    rc = _lib.load().gbsdf_parse_binary_stl(b.ctypes.data, len(data), verts.ctypes.data, 3 * T, idx.ctypes.data, 3 * T,
+                                            nrm.ctypes.data, C.byref(nv), C.byref(ni), int(device), err, len(err))
+    if rc != _lib.OK:
+        raise GbsdfError(rc, err.value.decode(errors="replace"))
+    out = (verts[:nv.value], idx[:ni.value])
+    return out + (nrm[:T],) if normals else out
+
+
+def parse_obj(text: bytes, device=0):
+    """GPU decode of OBJ text (gbsdf_parse_obj). Returns (vertices (V,3) float32, indices (I,) uint32)."""
+    data = bytes(text)
+    cap = len(data) // 10 + 1024
+    b = np.frombuffer(data, np.uint8)
+    verts = np.empty((cap, 3), np.float32)
+    idx = np.empty(6 * cap, np.uint32)
+    nv, ni = C.c_int64(0), C.c_int64(0)
+    err = C.create_string_buffer(512)
+    rc = _lib.load().gbsdf_parse_obj(b.ctypes.data, len(data), verts.ctypes.data, cap, idx.ctypes.data, 6 * cap,
+                                     C.byref(nv), C.byref(ni), int(device), err, len(err))
+    if rc != _lib.OK:
+        raise GbsdfError(rc, err.value.decode(errors="replace"))
+    return verts[:nv.value], idx[:ni.value]
 
 
 def mesh_lattice(vertices, voxel_size):

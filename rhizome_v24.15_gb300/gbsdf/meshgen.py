@@ -40,6 +40,8 @@ __all__ = [
     "to_triangles",
     "workload",
     "batch_workload",
+    "to_binary_stl",
+    "to_obj_text",
     "WORKLOADS",
 ]
 
@@ -430,6 +432,58 @@ WORKLOADS = {
     "vessel_c3_512": (dict(kind="vessel", seed=3), (512, 512, 512), 0.15),
     "blob_c5_1024": (dict(kind="blob", seed=5), (1024, 1024, 1024), 0.1),
 }
+
+
+def to_binary_stl(verts, faces, normals=None, header: bytes = b"gbsdf binary STL") -> bytes:
+    """Binary STL bytes (80-byte header, uint32 count, 50-byte records) of an indexed mesh;
+    ``normals`` (T,3) defaults to the unnormalised face normals."""
+    v = np.asarray(verts, np.float32)
+    f = np.asarray(faces, np.int64).reshape(-1, 3)
+    tri = v[f]
+    if normals is None:
+        normals = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    rec = np.zeros(len(f), dtype=[("n", "<f4", 3), ("v", "<f4", (3, 3)), ("attr", "<u2")])
+    rec["n"] = np.asarray(normals, np.float32)
+    rec["v"] = tri
+    return header[:80].ljust(80, b" ") + np.uint32(len(f)).tobytes() + rec.tobytes()
+
+
+def to_obj_text(verts, faces, seed: int = 0, fancy: bool = True) -> bytes:
+    """OBJ text of an indexed mesh. With ``fancy`` the writer varies the spellings the
+    decoders must accept: comments, normals / texture lines, v/vt/vn face tokens, negative
+    (relative) indices, tabs between numbers, CRLF line ends, signs, exponents and quads
+    ("v" and "f" are always followed by a space: the reference recognises only those)."""
+    rng = np.random.default_rng(seed)
+    v = np.asarray(verts, np.float32)
+    f = np.asarray(faces, np.int64).reshape(-1, 3)
+    out = ["# gbsdf OBJ writer\n", "o mesh\n"]
+    for i, p in enumerate(v):
+        if fancy and rng.random() < 0.1:
+            out.append("vn 0 0 1\n")
+        if fancy and rng.random() < 0.2:
+            out.append("v %+.6e\t%.7g  %.9g\r\n" % (p[0], p[1], p[2]))
+        else:
+            out.append("v %.6f %.6f %.6f\n" % (p[0], p[1], p[2]))
+    nv = len(v)
+    k = 0
+    while k < len(f):
+        a, b, c = (int(x) for x in f[k])
+        if fancy and k + 1 < len(f) and rng.random() < 0.1 and f[k + 1][0] == a and f[k + 1][1] == c:
+            d = int(f[k + 1][2])  # (a, b, c) + (a, c, d) written as one quad
+            out.append("f %d %d %d %d\n" % (a + 1, b + 1, c + 1, d + 1))
+            k += 2
+            continue
+        r = rng.random() if fancy else 1.0
+        if r < 0.15:
+            out.append("f %d/%d/%d %d/%d/%d %d/%d/%d\n" % (a + 1, 1, 1, b + 1, 1, 1, c + 1, 1, 1))
+        elif r < 0.25:
+            out.append("f %d %d %d\n" % (a - nv, b - nv, c - nv))
+        elif r < 0.3:
+            out.append("f %d//1\t%d//1 %d//1\r\n" % (a + 1, b + 1, c + 1))
+        else:
+            out.append("f %d %d %d\n" % (a + 1, b + 1, c + 1))
+        k += 1
+    return "".join(out).encode()
 
 
 def batch_workload(seed: int = 4, n: int = 64, t_lo: float = 2000.0, t_hi: float = 300000.0, g_lo: int = 64,
