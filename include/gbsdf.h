@@ -108,7 +108,9 @@ typedef struct gbsdf_options {
                                TMA tiles on a warp-specialised mbarrier pipeline (y / z walks:
                                default); 4, 5 = x pipeline with cp.async-staged / TMA-pipelined
                                y / z walks. TMA needs rows of a multiple of 4 voxels. */
-    int32_t reserved;
+    int32_t host_output;    /* host outputs: 0 = a page-locked output is written by the sign-apply
+                               kernel through its device mapping (no staging copy), others are
+                               staged in device memory and copied; 1 = always stage and copy */
 } gbsdf_options;
 
 /* Learned sign-risk model: parameter count and brick feature count. */

@@ -413,7 +413,19 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     }
     GB_CK(cudaEventRecord(w.ev[7], st));
     // ---- [F]
+    // a pinned (page-locked) host output is written by the apply kernel itself through its
+    // device mapping, which streams the grid over the host link without a staging copy
     float* final_dst = out_dev ? out : P<float>(w.B);
+    bool direct_host = false;
+    if (!out_dev && o.host_output == 0) {
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, out) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+            final_dst = static_cast<float*>(pa.devicePointer);
+            direct_host = true;
+        } else {
+            cudaGetLastError();
+        }
+    }
     launch_apply(P<float>(w.A), P<uint32_t>(w.S), L, final_dst, w.ds, exact_signs ? stol * L.h : 0.0f, st);
     GB_CK(cudaGetLastError());
     GB_CK(cudaEventRecord(w.ev[8], st));
@@ -425,7 +437,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
                                       (unsigned long long)h.wait_timeouts);
     if (h.verify_state != 1) status = e.set(GBSDF_EVERIFY, "sign verification diverged: %d mismatches in probe %d",
                                             h.probe_m, h.probes - 1);
-    if (status == GBSDF_OK && !out_dev) {
+    if (status == GBSDF_OK && !out_dev && !direct_host) {
         GB_CK(cudaMemcpyAsync(out, w.B.p, (size_t)N * 4, cudaMemcpyDeviceToHost, st));
     }
     GB_CK(cudaEventRecord(w.ev[9], st));

@@ -864,7 +864,7 @@ __global__ void clamp_kernel(float* __restrict__ g, const uint32_t* __restrict__
 __global__ void __launch_bounds__(256) apply_kernel(const float* __restrict__ g, const uint32_t* __restrict__ sbits,
                                                     Lattice L, float* __restrict__ out, const DevState* ds,
                                                     float surf_tol) {
-    if (ds->verify_state != 1 || ds->abort_) return;
+    if (ds->verify_state != 1 || ds->abort_ || ds->wait_timeouts) return;
     const int dx = L.dims[0];
     const long long nrows = (long long)L.dims[1] * L.dims[2];
     const bool vec = (dx & 3) == 0;

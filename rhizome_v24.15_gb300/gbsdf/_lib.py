@@ -23,7 +23,7 @@ class Options(C.Structure):
     _fields_ = [("mode", C.c_int32), ("path", C.c_int32), ("device", C.c_int32), ("tris_on_device", C.c_int32),
                 ("max_rounds", C.c_int32), ("mlp_budget", C.c_int32), ("mlp_threshold", C.c_float),
                 ("reserved0", C.c_int32), ("mlp_params", C.c_void_p), ("brick_scores", C.c_void_p),
-                ("sweep_schedule", C.c_int32), ("reserved", C.c_int32)]
+                ("sweep_schedule", C.c_int32), ("host_output", C.c_int32)]
 
 
 MLP_PARAMS, MLP_FEATURES = 6337, 32

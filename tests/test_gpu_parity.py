@@ -178,3 +178,24 @@ def test_cuda_rasterizer_mirror(engine):
     assert ok and out.size == int(np.prod(mx.astype(np.int64) - mn + 1)) and ms > 0
     ok, out2, _ = engine.CudaRasterizer.compute_mesh_sdf(tris, h, mx, mn)
     assert not ok and out2 is None
+
+
+def test_pinned_host_output_written_directly(engine):
+    """A page-locked host output is written by the sign-apply kernel through its device
+    mapping; the grid equals the staged-and-copied one and the device-resident one."""
+    import torch
+
+    from gbsdf import meshgen
+
+    tris, mn, mx, h = meshgen.workload("mug_c1_128", dims=(72, 64, 80), h=1.4)
+    n = int(np.prod(mx.astype(np.int64) - mn + 1))
+    pinned = torch.empty(n, dtype=torch.float32).pin_memory()
+    a, ra = engine.compute_mesh_sdf(tris, h, mn, mx, out=pinned.numpy(), mode=engine.MODE_EXACT_SIGNS,
+                                    path=engine.PATH_FAST)
+    b, rb = engine.compute_mesh_sdf(tris, h, mn, mx, mode=engine.MODE_EXACT_SIGNS, path=engine.PATH_FAST,
+                                    host_output=1)
+    dev = torch.empty(n, dtype=torch.float32, device="cuda")
+    engine.compute_mesh_sdf(tris, h, mn, mx, out=dev, mode=engine.MODE_EXACT_SIGNS, path=engine.PATH_FAST)
+    assert ra.ok and rb.ok
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(a.view(np.uint32), dev.cpu().numpy().view(np.uint32))
