@@ -257,6 +257,18 @@ int gbsdf_parse_obj(const char* text, size_t n_bytes, float* out_vertices, int64
                     uint32_t* out_indices, int64_t index_capacity, int64_t* n_vertices, int64_t* n_indices,
                     int32_t device, char* err, size_t errlen);
 
+/* Replaces CudaRasterizer::orient_mesh_gpu (cuda_mesh_topology.cu:707-842), the pre-pass
+ * the reference's OBJ loader runs after decoding: makes the winding of `indices` (host,
+ * 3 per triangle, rewritten in place) consistent across every edge shared by two
+ * triangles -- each connected component oriented like its smallest triangle -- and
+ * outward (the mesh is inverted when its signed volume is below -1e-5). Reports whether
+ * the mesh is orientable, whether any winding was inconsistent, whether it was inverted,
+ * and the signed volume (FP64). Runs the label propagation to convergence (the reference
+ * stops after 256 steps). */
+int gbsdf_orient_mesh(const float* vertices, int64_t n_vertices, uint32_t* indices, int64_t n_indices,
+                      int32_t* is_orientable, int32_t* had_inconsistent_winding, int32_t* was_inverted,
+                      double* signed_volume, int32_t device, char* err, size_t errlen);
+
 /* Releases the cached device workspace of `device` (buffers are otherwise reused
  * across calls on the same device). */
 void gbsdf_release_workspace(int32_t device);

@@ -239,3 +239,88 @@ int orc_parse_obj(const char* text_in, size_t n, float* verts, uint32_t* idx, in
 }
 
 }  // extern "C"
+
+// ---- orientation pre-pass ------------------------------------------------------------
+// CudaRasterizer::orient_mesh_gpu (native/src/engine/mesh/cuda_mesh_topology.cu:707-842,
+// kernels :303-455): an edge shared by exactly two triangles links them, "same direction"
+// when both traverse it the same way (inconsistent winding); each connected component is
+// oriented like its smallest triangle (flip parity along any path), a component whose
+// links contradict themselves is non-orientable; flips are applied when any link was
+// inconsistent; the mesh is inverted when its signed volume sum(v0 . (v1 x v2)) / 6 is
+// below -1e-5. Restated with a breadth-first search per component and an FP64 volume.
+#include <algorithm>
+#include <map>
+#include <queue>
+
+extern "C" int orc_orient_mesh(const float* verts, int64_t nv, uint32_t* idx, int64_t ni, int32_t* orientable,
+                               int32_t* inconsistent, int32_t* inverted, double* volume) {
+    (void)nv;
+    const int64_t T = ni / 3;
+    *orientable = 1;
+    *inconsistent = 0;
+    *inverted = 0;
+    *volume = 0.0;
+    if (T <= 0) return 0;
+    struct Use {
+        int64_t tri;
+        bool fwd;
+    };
+    std::map<std::pair<uint32_t, uint32_t>, std::vector<Use>> edges;
+    for (int64_t t = 0; t < T; ++t)
+        for (int e = 0; e < 3; ++e) {
+            const uint32_t u = idx[3 * t + e], v = idx[3 * t + (e + 1) % 3];
+            if (u == v) continue;
+            edges[{std::min(u, v), std::max(u, v)}].push_back({t, u < v});
+        }
+    std::vector<std::vector<std::pair<int64_t, int>>> adj(T);
+    for (auto& kv : edges) {
+        if (kv.second.size() != 2) continue;
+        const Use a = kv.second[0], b = kv.second[1];
+        if (a.tri == b.tri) continue;
+        const int same = (a.fwd == b.fwd) ? 1 : 0;
+        if (same) *inconsistent = 1;
+        adj[a.tri].push_back({b.tri, same});
+        adj[b.tri].push_back({a.tri, same});
+    }
+    std::vector<int> flip(T, -1);
+    for (int64_t r = 0; r < T; ++r) {
+        if (flip[r] >= 0) continue;
+        flip[r] = 0;
+        std::queue<int64_t> q;
+        q.push(r);
+        while (!q.empty()) {
+            const int64_t t = q.front();
+            q.pop();
+            for (auto [nb, same] : adj[t]) {
+                const int req = flip[t] ^ same;
+                if (flip[nb] < 0) {
+                    flip[nb] = req;
+                    q.push(nb);
+                } else if (flip[nb] != req) {
+                    *orientable = 0;
+                }
+            }
+        }
+    }
+    if (*inconsistent)
+        for (int64_t t = 0; t < T; ++t)
+            if (flip[t]) std::swap(idx[3 * t + 1], idx[3 * t + 2]);
+    double v6 = 0.0;
+    for (int64_t t = 0; t < T; ++t) {
+        const float* a = verts + 3 * (size_t)idx[3 * t];
+        const float* b = verts + 3 * (size_t)idx[3 * t + 1];
+        const float* c = verts + 3 * (size_t)idx[3 * t + 2];
+        const double cx = (double)b[1] * c[2] - (double)b[2] * c[1];
+        const double cy = (double)b[2] * c[0] - (double)b[0] * c[2];
+        const double cz = (double)b[0] * c[1] - (double)b[1] * c[0];
+        v6 += (double)a[0] * cx + (double)a[1] * cy + (double)a[2] * cz;
+    }
+    double vol = v6 / 6.0;
+    if (vol < -1e-5) {
+        for (int64_t t = 0; t < T; ++t) std::swap(idx[3 * t + 1], idx[3 * t + 2]);
+        vol = -vol;
+        *inverted = 1;
+    }
+    *volume = vol;
+    return 0;
+}

@@ -286,3 +286,17 @@ def parse_obj(text: bytes):
     L.orc_parse_obj.restype = C.c_int
     st = L.orc_parse_obj(_p(buf), C.c_size_t(n), _p(verts), _p(idx), C.byref(nv), C.byref(ni))
     return st, verts[:nv.value], idx[:ni.value]
+
+
+def orient_mesh(vertices, indices):
+    """Orientation pre-pass (cuda_mesh_topology.cu:707-842). Returns (indices oriented,
+    orientable, had_inconsistent_winding, was_inverted, signed volume)."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    idx = np.ascontiguousarray(indices, np.uint32).ravel().copy()
+    o, i, w = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+    vol = C.c_double(0.0)
+    L = lib()
+    L.orc_orient_mesh.restype = C.c_int
+    L.orc_orient_mesh(_p(v), C.c_int64(len(v)), _p(idx), C.c_int64(len(idx)), C.byref(o), C.byref(i), C.byref(w),
+                      C.byref(vol))
+    return idx, bool(o.value), bool(i.value), bool(w.value), vol.value

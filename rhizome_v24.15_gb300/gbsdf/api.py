@@ -25,7 +25,7 @@ from ._lib import (MODE_EXACT, MODE_EXACT_SIGNS, MODE_LEARNED, MODE_REFERENCE, P
                    STATUS_NAMES)
 
 __all__ = ["GbsdfError", "Result", "Batch", "compute_mesh_sdf", "compute_mesh_sdf_batch", "parse_binary_stl",
-           "parse_obj", "mesh_lattice", "build_from_mesh", "CudaRasterizer",
+           "parse_obj", "orient_mesh", "mesh_lattice", "build_from_mesh", "CudaRasterizer",
            "CudaVolumeGrid", "MODE_REFERENCE", "MODE_EXACT", "MODE_EXACT_SIGNS", "MODE_LEARNED", "PATH_AUTO", "PATH_FAST",
            "PATH_LEGACY"]
 
@@ -291,6 +291,21 @@ def parse_obj(text: bytes, device=0):
     if rc != _lib.OK:
         raise GbsdfError(rc, err.value.decode(errors="replace"))
     return verts[:nv.value], idx[:ni.value]
+
+
+def orient_mesh(vertices, indices, device=0):
+    """GPU orientation pre-pass (gbsdf_orient_mesh). Returns (indices oriented (I,) uint32,
+    orientable, had_inconsistent_winding, was_inverted, signed volume)."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    idx = np.ascontiguousarray(indices, np.uint32).ravel().copy()
+    o, i, w = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+    vol = C.c_double(0.0)
+    err = C.create_string_buffer(512)
+    rc = _lib.load().gbsdf_orient_mesh(v.ctypes.data, len(v), idx.ctypes.data, len(idx), C.byref(o), C.byref(i),
+                                       C.byref(w), C.byref(vol), int(device), err, len(err))
+    if rc != _lib.OK:
+        raise GbsdfError(rc, err.value.decode(errors="replace"))
+    return idx, bool(o.value), bool(i.value), bool(w.value), vol.value
 
 
 def mesh_lattice(vertices, voxel_size):

@@ -85,3 +85,30 @@ def test_decoded_mesh_builds_the_same_sdf(engine):
     b, mn2, mx2, _ = engine.build_from_mesh(dv, di, 2.0)
     assert np.array_equal(mn, mn2) and np.array_equal(mx, mx2)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_orientation_matches_oracle(engine, oracle):
+    from test_meshio_oracle import orient_cases
+
+    for name, v, f, _ in orient_cases():
+        gi, go, gc, gw, gv = engine.orient_mesh(v, f)
+        oi, oo, oc, ow, ov = oracle.orient_mesh(v, f)
+        assert (go, gc) == (oo, oc), name
+        if oo:  # orientable: the orientation, hence the volume and the inversion, is unique
+            assert gw == ow and np.array_equal(gi, oi), name
+            assert abs(gv - ov) <= 1e-9 * max(1.0, abs(ov)), name
+
+
+def test_orientation_large_component(engine, oracle):
+    """A component whose diameter is far beyond 256 links converges (the reference's loop
+    stops after 256 steps)."""
+    from gbsdf import meshgen
+
+    v, f = meshgen.perturbed_sphere(seed=5, n_lat=400, n_lon=800)
+    rng = np.random.default_rng(3)
+    g = f.copy()
+    fl = rng.random(len(g)) < 0.5
+    g[fl] = g[fl][:, [0, 2, 1]]
+    gi, go, gc, gw, gv = engine.orient_mesh(v.astype(np.float32), g)
+    assert go and gc and gv > 0
+    assert np.array_equal(gi.reshape(-1, 3), f)

@@ -84,3 +84,56 @@ def test_reference_mug_specimen():
     assert st == 0 and len(v) == 1553 and len(i) == 3 * 3106
     ext = v.max(0) - v.min(0)
     assert np.allclose(ext, [100.0, 76.5, 85.0], atol=0.05)
+
+
+def _mobius(n=24):
+    th = 2 * np.pi * np.arange(n) / n
+    v = []
+    for t in th:
+        for w in (-0.3, 0.3):
+            r = 1 + w * np.cos(t / 2)
+            v.append([r * np.cos(t), r * np.sin(t), w * np.sin(t / 2)])
+    f = []
+    for i in range(n):
+        a, b = 2 * i, 2 * i + 1
+        if i + 1 < n:
+            c, d = 2 * (i + 1), 2 * (i + 1) + 1
+        else:
+            c, d = 1, 0  # the twist: the strip's sides swap where it closes
+        f += [[a, b, d], [a, d, c]]
+    return np.asarray(v, np.float32), np.asarray(f, np.int64)
+
+
+def orient_cases():
+    """(name, vertices, faces, expected source faces or None) cases of the pre-pass."""
+    from gbsdf import meshgen
+
+    rng = np.random.default_rng(7)
+    v, f = meshgen.perturbed_sphere(seed=2, n_lat=24, n_lon=48)
+    v = v.astype(np.float32)
+    g = f.copy()
+    fl = rng.random(len(g)) < 0.35
+    g[fl] = g[fl][:, [0, 2, 1]]
+    out = [("flipped", v, g, f), ("inverted", v, f[:, [0, 2, 1]], f)]
+    v2 = np.concatenate([v, v + np.float32(200.0)])
+    f2 = np.concatenate([f, (f + len(v))[:, [0, 2, 1]]])  # second shell inside out
+    out.append(("two_shells", v2, f2, None))
+    mv, mf = _mobius()
+    out.append(("mobius", mv, mf, None))
+    extra = np.c_[f[:4, 0], f[:4, 1], f[4:8, 2]]  # third users of four edges: non-manifold
+    out.append(("nonmanifold", v, np.concatenate([f, extra]), None))
+    return out
+
+
+def test_orientation_oracle():
+    for name, v, f, expect in orient_cases():
+        idx, orientable, inconsistent, inverted, vol = O.orient_mesh(v, f)
+        if expect is not None:
+            assert np.array_equal(idx.reshape(-1, 3), expect), name
+            assert orientable and vol > 0, name
+        if name == "flipped":
+            assert inconsistent
+        if name == "inverted":
+            assert inverted and not inconsistent
+        if name == "mobius":
+            assert not orientable and inconsistent
