@@ -111,6 +111,10 @@ typedef struct gbsdf_options {
     int32_t host_output;    /* host outputs: 0 = a page-locked output is written by the sign-apply
                                kernel through its device mapping (no staging copy), others are
                                staged in device memory and copied; 1 = always stage and copy */
+    int32_t winding_eval;   /* exact winding decisions: 0 = clustered (far clusters by a dipole
+                               with a rigorous error bound, undecided voxels summed exactly;
+                               same decisions), 1 = every voxel summed triangle by triangle */
+    int32_t reserved;
 } gbsdf_options;
 
 /* Learned sign-risk model: parameter count and brick feature count. */
@@ -143,7 +147,9 @@ typedef struct gbsdf_stats {
     int64_t proposed;      /* learned mode: bricks the network proposed for the exact winding number */
     int64_t sweep_schedule; /* schedules that ran: x schedule (1-3) + 10 x walk schedule
                                (1 cp.async, 2 TMA pipeline) */
-    int64_t reserved[5];
+    int64_t winding_certified; /* exact winding decisions settled by the cluster bound */
+    int64_t winding_summed;    /* ... and by the triangle-by-triangle sum */
+    int64_t reserved[3];
 } gbsdf_stats;
 
 /* Fill `opt` with defaults: reference mode, AUTO path, device 0, host triangles. */

@@ -89,6 +89,7 @@ struct Job {
     DevState* hs = nullptr;
     cudaStream_t st = nullptr;
     GridMap map_a{}, map_b{};  // TMA descriptors of A and B
+    Fwn fwn{};                 // clusters of the hierarchical winding evaluation
     int xsched = kXAuto;       // sweep schedules (a tuned class's winners, else the defaults)
     int wsched = kWAuto;
 };
@@ -154,6 +155,18 @@ void place_phase1(Job& j, Carver& c) {
     j.list = c.take<long long>((size_t)j.list_cap * 8);
     j.recheck = c.take<long long>((size_t)j.list_cap * 8);
     j.ds = c.take<DevState>(sizeof(DevState));
+    const long long ncap = std::max<long long>(1, std::min<long long>(L.nbricks, T));
+    j.fwn.cells = c.take<FwnCell>((size_t)ncap * sizeof(FwnCell));
+    j.fwn.tri = c.take<unsigned>((size_t)T * 4);
+    j.fwn.cell_of = c.take<unsigned>((size_t)T * 4);
+    j.fwn.counts = c.take<unsigned>((size_t)L.nbricks * 4);
+    j.fwn.cursor = c.take<unsigned>((size_t)L.nbricks * 4);
+    j.fwn.flag = c.take<unsigned>((size_t)L.nbricks * 4);
+    j.fwn.off = c.take<unsigned long long>((size_t)L.nbricks * 8);
+    j.fwn.cidx = c.take<unsigned long long>((size_t)L.nbricks * 8);
+    j.fwn.scan = c.take<unsigned long long>((size_t)fwn_scan_elems(L) * 8);
+    j.fwn.fb = c.take<long long>((size_t)j.list_cap * 8);
+    j.fwn.fb_cap = j.list_cap;
 }
 
 void place_phase2(Job& j, Carver& c) {
@@ -188,6 +201,7 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
     cudaMemsetAsync(j.bcur, 0, (size_t)L.nbricks * 4, st);
     cudaMemsetAsync(j.scur, 0, (size_t)L.nstrips * 4, st);
     launch_bin_fill(j.stt, j.ptt, T, L, j.boff, j.bcur, j.blist, j.soff, j.scur, j.slist, st, j.ds, j.cap_b, j.cap_s);
+    launch_fwn_build(j.t9, T, L, j.fwn, j.ds, st);
     // [init] + [A]: one CTA per brick of the lattice, the surplus over the active count exits
     launch_fill(j.A, N, kFarSentinel, st);
     launch_splat(j.stt, j.boff, j.bcount, j.blist, j.active, -1, L, j.A, j.ds, st);
@@ -200,8 +214,8 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
         cudaMemsetAsync(&j.ds->list_overflow, 0, sizeof(unsigned long long), st);
         cudaMemsetAsync(&j.ds->recheck_n, 0, sizeof(unsigned long long), st);
         launch_list_unknown(j.U, j.S, L, j.list, j.list_cap, j.ds, 0, st);
-        launch_gwn_team(j.t9, T, L, j.list, j.list_cap, kGwnFixup, j.S, j.recheck, j.list_cap, j.A, 0, stol, j.ds,
-                        b.num_sms, st);
+        launch_winding(&j.fwn, j.t9, T, L, j.list, j.list_cap, kGwnFixup, 0, j.S, j.recheck, j.list_cap, j.A, 0, stol,
+                       j.ds, b.num_sms, st);
         launch_gwn_recheck(j.t9, T, L, j.recheck, j.list_cap, kGwnFixup, j.S, j.ds, b.num_sms, st);
     }
     // [D]: the reference's round loop, stopped on the device when a round changes nothing
@@ -221,15 +235,15 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
     // [E]
     for (int gen = 0; gen < kProbeGens; ++gen) {
         launch_verify_prepare(L, gen, j.U, j.list, j.ds, st);
-        launch_gwn(j.t9, T, L, j.list, j.list_cap, kGwnVerify, 0, j.S, j.recheck, j.list_cap, j.A, 0, stol, j.ds,
-                   b.num_sms, st);
+        launch_winding(&j.fwn, j.t9, T, L, j.list, j.list_cap, kGwnVerify, 0, j.S, j.recheck, j.list_cap, j.A, 0,
+                       stol, j.ds, b.num_sms, st);
         launch_gwn_recheck(j.t9, T, L, j.recheck, j.list_cap, kGwnVerify, j.S, j.ds, b.num_sms, st);
         launch_verify_plan(gen, j.ds, st);
         if (gen == kProbeGens - 1) break;
         launch_patch_mark(L, j.U, j.ds, st);
         launch_list_unknown(j.U, j.S, L, j.list, j.list_cap, j.ds, 1, st);
-        launch_gwn(j.t9, T, L, j.list, j.list_cap, kGwnFixup, 1, j.S, j.recheck, j.list_cap, j.A, 0, stol, j.ds,
-                   b.num_sms, st);
+        launch_winding(&j.fwn, j.t9, T, L, j.list, j.list_cap, kGwnFixup, 1, j.S, j.recheck, j.list_cap, j.A, 0,
+                       stol, j.ds, b.num_sms, st);
         launch_gwn_recheck(j.t9, T, L, j.recheck, j.list_cap, kGwnFixup, j.S, j.ds, b.num_sms, st);
     }
     // [F], written only when the build passed its checks
@@ -379,6 +393,8 @@ void fill_stats(const Job& j, int status, float ms, unsigned long long launches,
     s->gwn_pairs = (long long)h.gwn_pairs;
     s->brick_pairs = (long long)h.brick_pairs;
     s->csr_entries = (long long)h.csr_entries;
+    s->winding_certified = (long long)h.fwn_certified;
+    s->winding_summed = (long long)h.fwn_fallback_total;
     s->sweep_schedule = (j.map_a.valid ? (j.xsched == kXAuto ? kXTmaPipe : j.xsched) : kXCpAsync) +
                         10 * (j.map_a.walk_valid ? (j.wsched == kWAuto ? kWTmaPipe : j.wsched) : kWCpAsync);
 }

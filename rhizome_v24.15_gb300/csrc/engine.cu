@@ -64,7 +64,8 @@ struct Workspace {
     cudaEvent_t ev[12] = {};
     std::mutex mu;
     Buf A, B, S, U, t12, t9, stt, ptt, bcount, bcur, boff, active, blist, scount, scur, soff, slist, scan, list,
-        recheck, hb, verts, idx, flags, fpos, S2, U2, fbase, fX, logits, opencnt, ekeys, ecnt, mparts, mlossp, phist, E;
+        recheck, hb, verts, idx, flags, fpos, S2, U2, fbase, fX, logits, opencnt, ekeys, ecnt, mparts, mlossp, phist, E, fwc, fwt, fwo, fwn, fwu, fwf, fwoff,
+        fwci, fwscan, fwfb;
     DevState* ds = nullptr;
     DevState* hs = nullptr;  // pinned host mirror
 };
@@ -139,7 +140,8 @@ void free_ws(Workspace& w) {
     Buf* bufs[] = {&w.A, &w.B, &w.S, &w.U, &w.t12, &w.t9, &w.stt, &w.ptt, &w.bcount, &w.bcur, &w.boff,
                    &w.active, &w.blist, &w.scount, &w.scur, &w.soff, &w.slist, &w.scan, &w.list, &w.recheck,
                    &w.hb, &w.verts, &w.idx, &w.flags, &w.fpos, &w.S2, &w.U2, &w.fbase, &w.fX, &w.logits,
-                   &w.opencnt, &w.ekeys, &w.ecnt, &w.mparts, &w.mlossp, &w.phist, &w.E};
+                   &w.opencnt, &w.ekeys, &w.ecnt, &w.mparts, &w.mlossp, &w.phist, &w.E,
+                   &w.fwc, &w.fwt, &w.fwo, &w.fwn, &w.fwu, &w.fwf, &w.fwoff, &w.fwci, &w.fwscan, &w.fwfb};
     for (Buf* b : bufs) {
         if (b->p) cudaFree(b->p);
         *b = Buf{};
@@ -169,7 +171,30 @@ constexpr long long kListCap = 8ll * 1024 * 1024;  // >= 64 patch boxes of 49^3 
 
 // Exact winding of every voxel flagged in U (initial unknown columns): compaction
 // into the dense list, FP32 pass, FP64 re-checks; repeats while the list overflowed.
-int fixup_unknown(Workspace& w, const Lattice& L, long long T, float stol, Err& e, uint32_t* ebits = nullptr) {
+// Clusters of the hierarchical winding evaluation for the packed triangles (w.t9).
+int build_fwn(Workspace& w, const Lattice& L, long long T, Fwn& f, Err& e) {
+    cudaStream_t st = w.st;
+    const long long ncap = std::max<long long>(1, std::min<long long>(L.nbricks, T));
+    GB_CK(ensure(w.fwc, (size_t)ncap * sizeof(FwnCell)));
+    GB_CK(ensure(w.fwt, (size_t)T * 4));
+    GB_CK(ensure(w.fwo, (size_t)T * 4));
+    GB_CK(ensure(w.fwn, (size_t)L.nbricks * 4));
+    GB_CK(ensure(w.fwu, (size_t)L.nbricks * 4));
+    GB_CK(ensure(w.fwf, (size_t)L.nbricks * 4));
+    GB_CK(ensure(w.fwoff, (size_t)L.nbricks * 8));
+    GB_CK(ensure(w.fwci, (size_t)L.nbricks * 8));
+    GB_CK(ensure(w.fwscan, (size_t)fwn_scan_elems(L) * 8));
+    GB_CK(ensure(w.fwfb, (size_t)kListCap * 8));
+    f = Fwn{P<FwnCell>(w.fwc), P<unsigned>(w.fwt), P<unsigned>(w.fwo), P<unsigned>(w.fwn), P<unsigned>(w.fwu),
+            P<unsigned>(w.fwf), P<unsigned long long>(w.fwoff), P<unsigned long long>(w.fwci),
+            P<unsigned long long>(w.fwscan), P<long long>(w.fwfb), kListCap};
+    launch_fwn_build(P<float>(w.t9), T, L, f, w.ds, st);
+    GB_CK(cudaGetLastError());
+    return GBSDF_OK;
+}
+
+int fixup_unknown(Workspace& w, const Lattice& L, long long T, float stol, Err& e, uint32_t* ebits = nullptr,
+                  const Fwn* fwn = nullptr) {
     cudaStream_t st = w.st;
     for (int pass = 0; pass < 1 << 20; ++pass) {
         GB_CK(cudaMemsetAsync(&w.ds->listed, 0, sizeof(unsigned long long), st));
@@ -181,7 +206,10 @@ int fixup_unknown(Workspace& w, const Lattice& L, long long T, float stol, Err& 
         GB_CK(cudaStreamSynchronize(st));
         long long n = std::min<long long>((long long)w.hs->listed, kListCap);
         if (n <= 0) return GBSDF_OK;
-        if (n < 64 * 1024)
+        if (fwn)
+            launch_winding(fwn, P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 0, P<uint32_t>(w.S),
+                           P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, w.num_sms, st);
+        else if (n < 64 * 1024)
             launch_gwn_small(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, P<uint32_t>(w.S),
                              P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, n, st);
         else
@@ -275,6 +303,13 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     const long long n_active = (long long)w.hs->active_bricks;
     GB_CK(ensure(w.blist, (size_t)std::max<long long>(brick_pairs, 1) * 4));
     GB_CK(ensure(w.slist, (size_t)std::max<long long>(strip_pairs, 1) * 4));
+    Fwn fwn_s{};
+    const Fwn* fwn = nullptr;
+    if (o.winding_eval == 0) {
+        int rcw = build_fwn(w, L, T, fwn_s, e);
+        if (rcw != GBSDF_OK) return rcw;
+        fwn = &fwn_s;
+    }
     GB_CK(cudaMemsetAsync(w.bcur.p, 0, (size_t)L.nbricks * 4, st));
     GB_CK(cudaMemsetAsync(w.scur.p, 0, (size_t)L.nstrips * 4, st));
     launch_bin_fill(P<SplatTri>(w.stt), P<ParTri>(w.ptt), T, L, P<unsigned long long>(w.boff), P<unsigned>(w.bcur),
@@ -302,7 +337,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     }
     GB_CK(cudaEventRecord(w.ev[4], st));
     // ---- [C]
-    int rc = fixup_unknown(w, L, T, stol, e, ebits);
+    int rc = fixup_unknown(w, L, T, stol, e, ebits, fwn);
     if (rc != GBSDF_OK) return rc;
     GB_CK(cudaEventRecord(w.ev[5], st));
     // ---- [D]
@@ -358,8 +393,8 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     // ---- [E]
     for (int gen = 0; gen < kProbeGens; ++gen) {
         launch_verify_prepare(L, gen, P<uint32_t>(w.U), P<long long>(w.list), w.ds, st);
-        launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnVerify, 0, P<uint32_t>(w.S),
-                   P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, w.num_sms, st);
+        launch_winding(fwn, P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnVerify, 0, P<uint32_t>(w.S),
+                       P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnVerify, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
         launch_verify_plan(gen, w.ds, st);
@@ -367,8 +402,8 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         launch_patch_mark(L, P<uint32_t>(w.U), w.ds, st);
         launch_list_unknown(P<uint32_t>(w.U), P<uint32_t>(w.S), L, P<long long>(w.list), kListCap, w.ds, 1, st,
                             ebits);
-        launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 1, P<uint32_t>(w.S),
-                   P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, w.num_sms, st);
+        launch_winding(fwn, P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 1, P<uint32_t>(w.S),
+                       P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
     }
@@ -408,7 +443,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         const int cut = propose_cut_bin(hist.data(), budget);
         launch_propose(logits, L, lthr, cut, &w.ds->proposed, P<uint32_t>(w.U), st);
         GB_CK(cudaGetLastError());
-        int rcp = fixup_unknown(w, L, T, stol, e);
+        int rcp = fixup_unknown(w, L, T, stol, e, nullptr, fwn);
         if (rcp != GBSDF_OK) return rcp;
     }
     GB_CK(cudaEventRecord(w.ev[7], st));
@@ -475,13 +510,16 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         stats->csr_entries = (long long)h.csr_entries;
         stats->path_taken = GBSDF_PATH_FAST;
         stats->proposed = (long long)h.proposed;
+        stats->winding_certified = (long long)h.fwn_certified;
+        stats->winding_summed = (long long)h.fwn_fallback_total;
         // x schedule + 10 x walk schedule of what ran
         stats->sweep_schedule = (map_a.valid ? xsched : kXCpAsync) + 10 * (map_a.walk_valid ? wsched : kWCpAsync);
     }
     return status;
 }
 
-int run_legacy(Workspace& w, long long T, const Lattice& L, float* out, bool out_dev, gbsdf_stats* stats, Err& e) {
+int run_legacy(Workspace& w, long long T, const Lattice& L, float* out, bool out_dev, gbsdf_stats* stats, Err& e,
+               int winding_eval = 0) {
     cudaStream_t st = w.st;
     const long long N = L.N;
     const long long ntiles = (T + 127) / 128;
@@ -501,14 +539,21 @@ int run_legacy(Workspace& w, long long T, const Lattice& L, float* out, bool out
     GB_CK(cudaGetLastError());
     GB_CK(cudaEventRecord(w.ev[3], st));
     // exact winding sign of every voxel, in list-sized chunks
+    Fwn fwn_s{};
+    const Fwn* fwn = nullptr;
+    if (winding_eval == 0) {
+        int rcw = build_fwn(w, L, T, fwn_s, e);
+        if (rcw != GBSDF_OK) return rcw;
+        fwn = &fwn_s;
+    }
     for (long long v0 = 0; v0 < N; v0 += kListCap) {
         long long n = std::min(kListCap, N - v0);
         launch_iota(P<long long>(w.list), n, v0, st);
         unsigned long long nn = (unsigned long long)n;
         GB_CK(cudaMemcpyAsync(&w.ds->listed, &nn, sizeof(nn), cudaMemcpyHostToDevice, st));
         GB_CK(cudaMemsetAsync(&w.ds->recheck_n, 0, sizeof(unsigned long long), st));
-        launch_gwn(P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 0, P<uint32_t>(w.S),
-                   P<long long>(w.recheck), kListCap, P<float>(w.A), 1, kSurfaceTolVoxels, w.ds, w.num_sms, st);
+        launch_winding(fwn, P<float>(w.t9), T, L, P<long long>(w.list), kListCap, kGwnFixup, 0, P<uint32_t>(w.S),
+                       P<long long>(w.recheck), kListCap, P<float>(w.A), 1, kSurfaceTolVoxels, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnFixup, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
         GB_CK(cudaStreamSynchronize(st));  // `nn` lives on the host stack
@@ -531,6 +576,8 @@ int run_legacy(Workspace& w, long long T, const Lattice& L, float* out, bool out
         stats->ms_d2h = ev_ms(w.ev[8], w.ev[9]);
         stats->gwn_pairs = (long long)w.hs->gwn_pairs;
         stats->fp64_rechecks = (long long)w.hs->fp64_rechecks;
+        stats->winding_certified = (long long)w.hs->fwn_certified;
+        stats->winding_summed = (long long)w.hs->fwn_fallback_total;
         stats->path_taken = GBSDF_PATH_LEGACY;
     }
     return GBSDF_OK;
@@ -589,10 +636,11 @@ int compute(const float* tris12, long long T, bool tris_dev, float h, const int3
     if (path == GBSDF_PATH_FAST) {
         rc = run_fast(w, T, L, o, out, out_dev, stats, e);
         if (rc == GBSDF_EVERIFY || rc == GBSDF_ECSR) {
-            if (o.path == GBSDF_PATH_AUTO) rc = run_legacy(w, T, L, out, out_dev, stats, e);  // reference fall-through
+            if (o.path == GBSDF_PATH_AUTO)
+                rc = run_legacy(w, T, L, out, out_dev, stats, e, o.winding_eval);  // reference fall-through
         }
     } else {
-        rc = run_legacy(w, T, L, out, out_dev, stats, e);
+        rc = run_legacy(w, T, L, out, out_dev, stats, e, o.winding_eval);
     }
     if (stats) {
         stats->ms_h2d = ev_ms(w.ev[0], w.ev[1]);

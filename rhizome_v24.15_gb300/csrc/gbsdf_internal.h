@@ -65,6 +65,10 @@ struct DevState {
     unsigned long long patched_voxels;
     unsigned long long overflow;       // a list outgrew the capacity planned for it (batches)
     unsigned long long wait_timeouts;  // bounded waits (TMA tiles) that gave up
+    unsigned long long fwn_cells;      // clusters of the hierarchical winding evaluation
+    unsigned long long fwn_certified;  // voxels whose side the cluster bound decided
+    unsigned long long fwn_fallback;   // voxels handed to the exact sum (current pass)
+    unsigned long long fwn_fallback_total;
     int changed[64];                   // per eikonal round
     int stop;                          // eikonal converged flag
     int rounds;
@@ -130,10 +134,47 @@ void launch_gwn(const float* tri9, long long T, const Lattice& L, const long lon
                 int consumer, int only_if, uint32_t* sbits, long long* recheck, long long recheck_cap,
                 const float* dist, int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st);
 // Persistent exact-winding pass over a device-sized list, 32 threads per voxel (any list
-// length, no host round trip).
+// length, no host round trip); `only_if`: skip unless a patch round is in flight.
 void launch_gwn_team(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
                      int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, const float* dist,
-                     int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st);
+                     int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st, int only_if = 0);
+
+// ---- hierarchical winding numbers --------------------------------------------------
+// Triangles clustered by the 8^3 brick of their centroid; each cluster keeps its
+// area-weighted centroid c, area vector D = sum(a_i n_i), area A and radius r (every
+// vertex within r of c). Seen from q at distance d > beta r, a cluster's solid angle is
+// D . (c - q) / d^3 within 2 r A / (d - r)^3 (the kernel (y - q) / |y - q|^3 has gradient
+// norm 2 / |y - q|^3); nearer clusters are summed exactly. A voxel whose |w| clears 0.5
+// by more than the summed bound (plus rounding slack) is decided; the others go to the
+// exact per-triangle sum. Decisions therefore equal the exact path's.
+struct FwnCell {
+    float cx, cy, cz, r;      // centroid, radius
+    float ax, ay, az, area;   // area vector, area
+    unsigned off, cnt, pad0, pad1;
+};
+static_assert(sizeof(FwnCell) == 48, "FwnCell layout");
+struct Fwn {
+    FwnCell* cells;           // capacity: min(bricks, triangles)
+    unsigned* tri;            // triangles by cluster
+    unsigned* cell_of;        // cluster brick of each triangle
+    unsigned* counts;         // per brick
+    unsigned* cursor;         // per brick
+    unsigned* flag;           // per brick: non-empty
+    unsigned long long* off;  // per brick
+    unsigned long long* cidx; // per brick: cluster index
+    unsigned long long* scan; // scan scratch
+    long long* fb;            // voxels left to the exact sum
+    long long fb_cap;
+};
+long long fwn_scan_elems(const Lattice& L);
+// Builds the clusters of the packed triangles (device only, no host round trip).
+void launch_fwn_build(const float* tri9, long long T, const Lattice& L, const Fwn& f, DevState* ds, cudaStream_t st);
+// Decides the listed voxels (as launch_gwn does) by the cluster bound, then sums the rest
+// exactly; the FP64 re-check pass (launch_gwn_recheck) follows as after launch_gwn.
+void launch_winding(const Fwn* f, const float* tri9, long long T, const Lattice& L, const long long* list,
+                    long long list_cap, int consumer, int only_if, uint32_t* sbits, long long* recheck,
+                    long long recheck_cap, const float* dist, int dist_sq, float surf_tol_vox, DevState* ds,
+                    int num_sms, cudaStream_t st);
 // Batches: decides on the device whether the build passed its checks (valid triangles,
 // the reference's CSR guard when `csr_guard`, no list overflow); sets ds->abort_ if not.
 void launch_batch_finalize(DevState* ds, int csr_guard, cudaStream_t st);

@@ -167,6 +167,202 @@ __global__ void __launch_bounds__(kGwnThreads) gwn_kernel(const float* __restric
     if (pairs) atomicAdd(&ds->gwn_pairs, pairs);
 }
 
+// ---- hierarchical winding numbers (clusters of the 8^3 brick of each centroid) --------
+constexpr float kFwnBeta = 5.0f;       // a cluster is far when d > beta r
+constexpr float kFwnSlackRel = 1e-5f;  // rounding slack per unit of summed |terms|
+constexpr float kFwnSlackAbs = 1e-5f;  // rounding slack in w
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__global__ void fwn_count_kernel(const float* __restrict__ t9, long long T, Lattice L, unsigned* __restrict__ cell_of,
+                                 unsigned* __restrict__ counts) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    const float* v = t9 + 9 * t;
+    const float inv = 1.0f / L.h;
+    int b[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float g = (v[k] + v[3 + k] + v[6 + k]) * (1.0f / 3.0f);
+        const float rel = g * inv - (float)L.mn[k];
+        const float c = floorf(rel / (float)kBrick);
+        b[k] = clampi(c != c ? 0 : (int)fmaxf(fminf(c, 1e9f), -1e9f), 0, L.nb[k] - 1);
+    }
+    const unsigned cell = (unsigned)(((long long)b[2] * L.nb[1] + b[1]) * L.nb[0] + b[0]);
+    cell_of[t] = cell;
+    atomicAdd(&counts[cell], 1u);
+}
+
+__global__ void fwn_flag_kernel(const unsigned* __restrict__ counts, long long nb, unsigned* __restrict__ flag) {
+    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nb) flag[b] = counts[b] ? 1u : 0u;
+}
+
+__global__ void fwn_fill_kernel(long long T, const unsigned* __restrict__ cell_of,
+                                const unsigned long long* __restrict__ off, unsigned* __restrict__ cursor,
+                                unsigned* __restrict__ tri) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    const unsigned c = cell_of[t];
+    tri[off[c] + atomicAdd(&cursor[c], 1u)] = (unsigned)t;
+}
+
+// one thread per brick; the statistics in FP64, the radius rounded up
+__global__ void fwn_stats_kernel(const float* __restrict__ t9, Lattice L, const unsigned* __restrict__ counts,
+                                 const unsigned long long* __restrict__ off, const unsigned* __restrict__ flag,
+                                 const unsigned long long* __restrict__ cidx, const unsigned* __restrict__ tri,
+                                 FwnCell* __restrict__ cells, DevState* ds) {
+    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= L.nbricks) return;
+    if (b == L.nbricks - 1) ds->fwn_cells = cidx[b] + flag[b];
+    const unsigned n = counts[b];
+    if (!n) return;
+    const unsigned long long o = off[b];
+    double A = 0.0, ax = 0.0, ay = 0.0, az = 0.0, gx = 0.0, gy = 0.0, gz = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
+    for (unsigned k = 0; k < n; ++k) {
+        const float* v = t9 + 9ull * tri[o + k];
+        const double e1x = (double)v[3] - v[0], e1y = (double)v[4] - v[1], e1z = (double)v[5] - v[2];
+        const double e2x = (double)v[6] - v[0], e2y = (double)v[7] - v[1], e2z = (double)v[8] - v[2];
+        const double cx = 0.5 * (e1y * e2z - e1z * e2y), cy = 0.5 * (e1z * e2x - e1x * e2z),
+                     cz = 0.5 * (e1x * e2y - e1y * e2x);
+        const double a = sqrt(cx * cx + cy * cy + cz * cz);
+        const double px = ((double)v[0] + v[3] + v[6]) / 3.0, py = ((double)v[1] + v[4] + v[7]) / 3.0,
+                     pz = ((double)v[2] + v[5] + v[8]) / 3.0;
+        A += a;
+        ax += cx;
+        ay += cy;
+        az += cz;
+        gx += a * px;
+        gy += a * py;
+        gz += a * pz;
+        mx += px;
+        my += py;
+        mz += pz;
+    }
+    double c0, c1, c2;
+    if (A > 0.0) {
+        c0 = gx / A;
+        c1 = gy / A;
+        c2 = gz / A;
+    } else {
+        c0 = mx / n;
+        c1 = my / n;
+        c2 = mz / n;
+    }
+    // the centroid as stored (FP32), the radius about that point, rounded up
+    const float fc0 = (float)c0, fc1 = (float)c1, fc2 = (float)c2;
+    double r2 = 0.0;
+    for (unsigned k = 0; k < n; ++k) {
+        const float* v = t9 + 9ull * tri[o + k];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const double dx = (double)v[3 * q] - fc0, dy = (double)v[3 * q + 1] - fc1, dz = (double)v[3 * q + 2] - fc2;
+            r2 = fmax(r2, dx * dx + dy * dy + dz * dz);
+        }
+    }
+    FwnCell c;
+    c.cx = fc0;
+    c.cy = fc1;
+    c.cz = fc2;
+    c.r = (float)(sqrt(r2) * (1.0 + 1e-6)) + 1e-30f;
+    c.ax = (float)ax;
+    c.ay = (float)ay;
+    c.az = (float)az;
+    c.area = (float)(A * (1.0 + 1e-6));
+    c.off = (unsigned)o;
+    c.cnt = n;
+    c.pad0 = c.pad1 = 0;
+    cells[cidx[b]] = c;
+}
+
+// One warp per listed voxel: far clusters by their dipole with the error bound, near
+// clusters triangle by triangle; lane 0 decides or hands the voxel to the exact sum.
+__global__ void __launch_bounds__(kGwnThreads) fwn_query_kernel(
+    const float* __restrict__ t9, const FwnCell* __restrict__ cells, const unsigned* __restrict__ tri, Lattice L,
+    const long long* __restrict__ list, long long cap, int consumer, int only_if, uint32_t* __restrict__ sbits,
+    const float* __restrict__ dist, int dist_sq, float surf_tol_vox, DevState* ds, long long* __restrict__ fb,
+    long long fb_cap) {
+    if (only_if && !ds->patching) return;
+    const float tau = surf_tol_vox * L.h;
+    const long long n = min((long long)ds->listed, cap);
+    const long long ncells = (long long)ds->fwn_cells;
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    unsigned long long certified = 0, handed = 0;
+    for (long long j = warp; j < n; j += nwarps) {
+        const long long v = list[j];
+        if (v < 0) continue;
+        int x, y, z;
+        voxel_coords(L, v, x, y, z);
+        const f3 p = lattice_point(L.mn[0], L.mn[1], L.mn[2], x, y, z, L.h);
+        if (dist) {
+            const float d = dist[v];
+            if (dist_sq ? (d <= tau * tau) : (d <= tau)) {  // on the surface: inside
+                if (lane == 0) consume(L, v, true, consumer, sbits, ds);
+                continue;
+            }
+        }
+        float s = 0.0f, c = 0.0f, err = 0.0f, mag = 0.0f;
+        bool amb = false;
+        for (long long k = lane; k < ncells; k += 32) {
+            const FwnCell cl = cells[k];
+            const float dx = cl.cx - p.x, dy = cl.cy - p.y, dz = cl.cz - p.z;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const float d = sqrtf(d2);
+            if (d > kFwnBeta * cl.r) {
+                const float term = (cl.ax * dx + cl.ay * dy + cl.az * dz) / (d2 * d);
+                kahan_add(s, c, term);
+                mag += fabsf(term);
+                const float e = (d - cl.r) * 0.99999f;
+                err += 2.0f * cl.r * cl.area / (e * e * e);
+            } else {
+                for (unsigned q = 0; q < cl.cnt; ++q) {
+                    const float* tv = t9 + 9ull * tri[cl.off + q];
+                    const float term =
+                        solid_angle_fast(p, mk(tv[0], tv[1], tv[2]), mk(tv[3], tv[4], tv[5]), mk(tv[6], tv[7], tv[8]), amb);
+                    kahan_add(s, c, term);
+                    mag += fabsf(term);
+                }
+            }
+        }
+        float tot = s - c;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            tot += __shfl_xor_sync(0xffffffffu, tot, o);
+            err += __shfl_xor_sync(0xffffffffu, err, o);
+            mag += __shfl_xor_sync(0xffffffffu, mag, o);
+        }
+        amb = __any_sync(0xffffffffu, amb);
+        if (lane == 0) {
+            const float w = fabsf(tot * kInv4Pi);
+            const float E = (err + kFwnSlackRel * mag) * kInv4Pi + kFwnSlackAbs;
+            if (!amb && w - E >= 0.5f) {
+                consume(L, v, true, consumer, sbits, ds);
+                ++certified;
+            } else if (!amb && w + E < 0.5f) {
+                consume(L, v, false, consumer, sbits, ds);
+                ++certified;
+            } else {
+                const unsigned long long k = atomicAdd(&ds->fwn_fallback, 1ull);
+                if ((long long)k < fb_cap) fb[k] = v;
+                ++handed;
+            }
+        }
+    }
+    if (lane == 0) {
+        if (certified) atomicAdd(&ds->fwn_certified, certified);
+        if (handed) atomicAdd(&ds->fwn_fallback_total, handed);
+    }
+}
+
+// the exact sum takes the fallback list as its list
+__global__ void fwn_handoff_kernel(DevState* ds, int only_if, long long fb_cap) {
+    if (only_if && !ds->patching) return;
+    ds->listed = min(ds->fwn_fallback, (unsigned long long)fb_cap);
+    ds->fwn_fallback = 0ull;
+}
+
 constexpr int kRecheckThreads = 256;
 
 __global__ void __launch_bounds__(kRecheckThreads) gwn_recheck_kernel(const float* __restrict__ tri9, long long T,
@@ -301,11 +497,49 @@ void launch_gwn(const float* tri9, long long T, const Lattice& L, const long lon
 
 void launch_gwn_team(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
                      int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, const float* dist,
-                     int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st) {
+                     int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st, int only_if) {
     GBSDF_COUNT_LAUNCH();
-    gwn_kernel<32><<<(unsigned)(num_sms * 8), kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, 0, sbits,
-                                                                     recheck, recheck_cap, dist, dist_sq,
+    gwn_kernel<32><<<(unsigned)(num_sms * 8), kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, only_if,
+                                                                     sbits, recheck, recheck_cap, dist, dist_sq,
                                                                      surf_tol_vox, ds);
+}
+
+long long fwn_scan_elems(const Lattice& L) { return scan_tmp_elems(L.nbricks); }
+
+void launch_fwn_build(const float* tri9, long long T, const Lattice& L, const Fwn& f, DevState* ds, cudaStream_t st) {
+    if (T <= 0) return;
+    cudaMemsetAsync(f.counts, 0, (size_t)L.nbricks * 4, st);
+    cudaMemsetAsync(f.cursor, 0, (size_t)L.nbricks * 4, st);
+    GBSDF_COUNT_LAUNCH();
+    fwn_count_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(tri9, T, L, f.cell_of, f.counts);
+    launch_exclusive_scan(f.counts, f.off, L.nbricks, f.scan, 0, st);
+    GBSDF_COUNT_LAUNCH();
+    fwn_flag_kernel<<<(unsigned)((L.nbricks + 255) / 256), 256, 0, st>>>(f.counts, L.nbricks, f.flag);
+    launch_exclusive_scan(f.flag, f.cidx, L.nbricks, f.scan, 0, st);
+    GBSDF_COUNT_LAUNCH();
+    fwn_fill_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(T, f.cell_of, f.off, f.cursor, f.tri);
+    GBSDF_COUNT_LAUNCH();
+    fwn_stats_kernel<<<(unsigned)((L.nbricks + 127) / 128), 128, 0, st>>>(tri9, L, f.counts, f.off, f.flag, f.cidx,
+                                                                         f.tri, f.cells, ds);
+}
+
+void launch_winding(const Fwn* f, const float* tri9, long long T, const Lattice& L, const long long* list,
+                    long long list_cap, int consumer, int only_if, uint32_t* sbits, long long* recheck,
+                    long long recheck_cap, const float* dist, int dist_sq, float surf_tol_vox, DevState* ds,
+                    int num_sms, cudaStream_t st) {
+    if (!f) {
+        launch_gwn(tri9, T, L, list, list_cap, consumer, only_if, sbits, recheck, recheck_cap, dist, dist_sq,
+                   surf_tol_vox, ds, num_sms, st);
+        return;
+    }
+    GBSDF_COUNT_LAUNCH();
+    fwn_query_kernel<<<(unsigned)(num_sms * 8), kGwnThreads, 0, st>>>(
+        tri9, f->cells, f->tri, L, list, list_cap, consumer, only_if, sbits, dist, dist_sq, surf_tol_vox, ds, f->fb,
+        f->fb_cap);
+    GBSDF_COUNT_LAUNCH();
+    fwn_handoff_kernel<<<1, 1, 0, st>>>(ds, only_if, f->fb_cap);
+    launch_gwn_team(tri9, T, L, f->fb, f->fb_cap, consumer, sbits, recheck, recheck_cap, dist, dist_sq, surf_tol_vox,
+                    ds, num_sms, st, only_if);
 }
 
 void launch_gwn_small(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,

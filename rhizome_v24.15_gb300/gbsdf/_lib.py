@@ -23,7 +23,8 @@ class Options(C.Structure):
     _fields_ = [("mode", C.c_int32), ("path", C.c_int32), ("device", C.c_int32), ("tris_on_device", C.c_int32),
                 ("max_rounds", C.c_int32), ("mlp_budget", C.c_int32), ("mlp_threshold", C.c_float),
                 ("reserved0", C.c_int32), ("mlp_params", C.c_void_p), ("brick_scores", C.c_void_p),
-                ("sweep_schedule", C.c_int32), ("host_output", C.c_int32)]
+                ("sweep_schedule", C.c_int32), ("host_output", C.c_int32),
+                ("winding_eval", C.c_int32), ("reserved", C.c_int32)]
 
 
 MLP_PARAMS, MLP_FEATURES = 6337, 32
@@ -40,7 +41,8 @@ class Stats(C.Structure):
                 ("safe_clamped", C.c_int64), ("patched_voxels", C.c_int64), ("fp64_rechecks", C.c_int64),
                 ("band_voxels", C.c_int64), ("splat_evals", C.c_int64), ("gwn_pairs", C.c_int64),
                 ("brick_pairs", C.c_int64), ("csr_entries", C.c_int64), ("kernel_launches", C.c_int64),
-                ("proposed", C.c_int64), ("sweep_schedule", C.c_int64), ("reserved", C.c_int64 * 5)]
+                ("proposed", C.c_int64), ("sweep_schedule", C.c_int64), ("winding_certified", C.c_int64),
+                ("winding_summed", C.c_int64), ("reserved", C.c_int64 * 3)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "pad0")}

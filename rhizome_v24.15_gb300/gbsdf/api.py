@@ -107,7 +107,7 @@ def _set_learned(o, mode, device, mlp_params, mlp_budget, mlp_threshold, brick_s
 
 def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE_REFERENCE, path=PATH_AUTO,
                      device=0, max_rounds=0, raise_on_error=True, mlp_params=None, mlp_budget=None,
-                     mlp_threshold=None, brick_scores=None, sweep_schedule=0, host_output=0):
+                     mlp_threshold=None, brick_scores=None, sweep_schedule=0, host_output=0, winding_eval=0):
     """Run the engine. ``tris``: (T,12) float32 numpy array (host) or CUDA tensor.
     ``out``: float32 buffer of N voxels (numpy = host, CUDA tensor = device); allocated
     on the host when None. ``MODE_LEARNED`` takes the sign-risk model's parameters
@@ -116,6 +116,7 @@ def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE
     the network's scores. ``sweep_schedule``: 0 autotuned, 1-3 a fixed x-sweep schedule
     (identical results). ``host_output``: 0 lets a page-locked host output be written
     directly by the sign-apply kernel, 1 stages it in device memory and copies.
+    ``winding_eval``: 0 clustered exact winding decisions, 1 triangle-by-triangle sums.
     Returns ``(out, Result)``."""
     mn = np.asarray(min_coord, np.int64).reshape(3)
     mx = np.asarray(max_coord, np.int64).reshape(3)
@@ -134,6 +135,7 @@ def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE
     o.mode, o.path, o.device, o.tris_on_device, o.max_rounds = int(mode), int(path), int(device), int(tdev), int(max_rounds)
     o.sweep_schedule = int(sweep_schedule)
     o.host_output = int(host_output)
+    o.winding_eval = int(winding_eval)
     keep = _set_learned(o, mode, device, mlp_params, mlp_budget, mlp_threshold, brick_scores)  # noqa: F841
     st = _lib.Stats()
     err = C.create_string_buffer(512)

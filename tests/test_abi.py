@@ -56,7 +56,7 @@ def test_library_loads_and_binds(lib_path):
 def test_struct_layouts():
     from gbsdf import _lib
 
-    assert C.sizeof(_lib.Options) == 56
+    assert C.sizeof(_lib.Options) == 64
     # 2 int32 + 10 float + 6 int32 + 11 int64 + 8 reserved int64
     assert C.sizeof(_lib.Stats) == 8 + 40 + 24 + 88 + 64
 
