@@ -141,18 +141,21 @@ void launch_gwn_team(const float* tri9, long long T, const Lattice& L, const lon
 
 // ---- hierarchical winding numbers --------------------------------------------------
 // Triangles clustered by the 8^3 brick of their centroid; each cluster keeps its
-// area-weighted centroid c, area vector D = sum(a_i n_i), area A and radius r (every
-// vertex within r of c). Seen from q at distance d > beta r, a cluster's solid angle is
-// D . (c - q) / d^3 within 2 r A / (d - r)^3 (the kernel (y - q) / |y - q|^3 has gradient
-// norm 2 / |y - q|^3); nearer clusters are summed exactly. A voxel whose |w| clears 0.5
+// area-weighted centroid c, area vector D = sum(a_i n_i), first moment M = sum(a_i n_i
+// (g_i - c)^T) (g_i the triangle centroids; exact for flat triangles), area A and radius r
+// (every vertex within r of c). Seen from q at distance d > beta r, with y = c - q, the
+// kernel K(x) = (x - q) / |x - q|^3 expanded to second order gives the cluster's solid
+// angle D . y / d^3 + (tr M - 3 y^T M y / d^2) / d^3 within 3 r^2 A / (d - r)^4 (the second
+// derivative of K has norm at most 6 / |x - q|^4); nearer clusters are summed exactly. A voxel whose |w| clears 0.5
 // by more than the summed bound (plus rounding slack) is decided; the others go to the
 // exact per-triangle sum. Decisions therefore equal the exact path's.
 struct FwnCell {
     float cx, cy, cz, r;      // centroid, radius
     float ax, ay, az, area;   // area vector, area
-    unsigned off, cnt, pad0, pad1;
+    float m[9];               // first moment sum_t D_t,i (g_t - c)_j, row-major (i, j)
+    unsigned off, cnt, pad0;
 };
-static_assert(sizeof(FwnCell) == 48, "FwnCell layout");
+static_assert(sizeof(FwnCell) == 80, "FwnCell layout");
 struct Fwn {
     FwnCell* cells;           // capacity: min(bricks, triangles)
     unsigned* tri;            // triangles by cluster

@@ -168,7 +168,10 @@ __global__ void __launch_bounds__(kGwnThreads) gwn_kernel(const float* __restric
 }
 
 // ---- hierarchical winding numbers (clusters of the 8^3 brick of each centroid) --------
-constexpr float kFwnBeta = 5.0f;       // a cluster is far when d > beta r
+#ifndef GBSDF_FWN_BETA
+#define GBSDF_FWN_BETA 4.0f
+#endif
+constexpr float kFwnBeta = GBSDF_FWN_BETA;  // a cluster is far when d > beta r
 constexpr float kFwnSlackRel = 1e-5f;  // rounding slack per unit of summed |terms|
 constexpr float kFwnSlackAbs = 1e-5f;  // rounding slack in w
 
@@ -219,6 +222,7 @@ __global__ void fwn_stats_kernel(const float* __restrict__ t9, Lattice L, const 
     if (!n) return;
     const unsigned long long o = off[b];
     double A = 0.0, ax = 0.0, ay = 0.0, az = 0.0, gx = 0.0, gy = 0.0, gz = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
+    double M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // sum_t D_t (g_t)^T; shifted to c below
     for (unsigned k = 0; k < n; ++k) {
         const float* v = t9 + 9ull * tri[o + k];
         const double e1x = (double)v[3] - v[0], e1y = (double)v[4] - v[1], e1z = (double)v[5] - v[2];
@@ -238,6 +242,9 @@ __global__ void fwn_stats_kernel(const float* __restrict__ t9, Lattice L, const 
         mx += px;
         my += py;
         mz += pz;
+        const double Dt[3] = {cx, cy, cz}, gt[3] = {px, py, pz};
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) M[3 * i + j] += Dt[i] * gt[j];
     }
     double c0, c1, c2;
     if (A > 0.0) {
@@ -269,9 +276,13 @@ __global__ void fwn_stats_kernel(const float* __restrict__ t9, Lattice L, const 
     c.ay = (float)ay;
     c.az = (float)az;
     c.area = (float)(A * (1.0 + 1e-6));
+    // moment about the stored centroid: sum D_t (g_t - c)^T = M - D c^T
+    const double D3[3] = {ax, ay, az}, cc[3] = {(double)fc0, (double)fc1, (double)fc2};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) c.m[3 * i + j] = (float)(M[3 * i + j] - D3[i] * cc[j]);
     c.off = (unsigned)o;
     c.cnt = n;
-    c.pad0 = c.pad1 = 0;
+    c.pad0 = 0;
     cells[cidx[b]] = c;
 }
 
@@ -311,11 +322,21 @@ __global__ void __launch_bounds__(kGwnThreads) fwn_query_kernel(
             const float d2 = dx * dx + dy * dy + dz * dz;
             const float d = sqrtf(d2);
             if (d > kFwnBeta * cl.r) {
-                const float term = (cl.ax * dx + cl.ay * dy + cl.az * dz) / (d2 * d);
+                // y = c - q: K(c) = -y / d^3 seen from the centroid's side; grad K(c) =
+                // (I - 3 yy^T / d^2) / d^3 contracted with M (sign: the kernel is x - q)
+                const float inv3 = 1.0f / (d2 * d);
+                const float dip = (cl.ax * dx + cl.ay * dy + cl.az * dz) * inv3;
+                const float tr = cl.m[0] + cl.m[4] + cl.m[8];
+                const float my0 = cl.m[0] * dx + cl.m[1] * dy + cl.m[2] * dz;
+                const float my1 = cl.m[3] * dx + cl.m[4] * dy + cl.m[5] * dz;
+                const float my2 = cl.m[6] * dx + cl.m[7] * dy + cl.m[8] * dz;
+                const float yMy = dx * my0 + dy * my1 + dz * my2;
+                const float quad = (tr - 3.0f * yMy / d2) * inv3;
+                const float term = dip + quad;
                 kahan_add(s, c, term);
-                mag += fabsf(term);
+                mag += fabsf(dip) + fabsf(quad);
                 const float e = (d - cl.r) * 0.99999f;
-                err += 2.0f * cl.r * cl.area / (e * e * e);
+                err += 3.0f * cl.r * cl.r * cl.area / (e * e * e * e);
             } else {
                 for (unsigned q = 0; q < cl.cnt; ++q) {
                     const float* tv = t9 + 9ull * tri[cl.off + q];
