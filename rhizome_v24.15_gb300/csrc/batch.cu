@@ -155,16 +155,18 @@ void place_phase1(Job& j, Carver& c) {
     j.list = c.take<long long>((size_t)j.list_cap * 8);
     j.recheck = c.take<long long>((size_t)j.list_cap * 8);
     j.ds = c.take<DevState>(sizeof(DevState));
-    const long long ncap = std::max<long long>(1, std::min<long long>(L.nbricks, T));
+    j.fwn.g = fwn_grid(L, T);
+    const long long nc = j.fwn.g.cells;
+    const long long ncap = std::max<long long>(1, std::min<long long>(nc, T));
     j.fwn.cells = c.take<FwnCell>((size_t)ncap * sizeof(FwnCell));
     j.fwn.tri = c.take<unsigned>((size_t)T * 4);
     j.fwn.cell_of = c.take<unsigned>((size_t)T * 4);
-    j.fwn.counts = c.take<unsigned>((size_t)L.nbricks * 4);
-    j.fwn.cursor = c.take<unsigned>((size_t)L.nbricks * 4);
-    j.fwn.flag = c.take<unsigned>((size_t)L.nbricks * 4);
-    j.fwn.off = c.take<unsigned long long>((size_t)L.nbricks * 8);
-    j.fwn.cidx = c.take<unsigned long long>((size_t)L.nbricks * 8);
-    j.fwn.scan = c.take<unsigned long long>((size_t)fwn_scan_elems(L) * 8);
+    j.fwn.counts = c.take<unsigned>((size_t)nc * 4);
+    j.fwn.cursor = c.take<unsigned>((size_t)nc * 4);
+    j.fwn.flag = c.take<unsigned>((size_t)nc * 4);
+    j.fwn.off = c.take<unsigned long long>((size_t)nc * 8);
+    j.fwn.cidx = c.take<unsigned long long>((size_t)nc * 8);
+    j.fwn.scan = c.take<unsigned long long>((size_t)fwn_scan_elems(j.fwn.g) * 8);
     j.fwn.fb = c.take<long long>((size_t)j.list_cap * 8);
     j.fwn.fb_cap = j.list_cap;
 }

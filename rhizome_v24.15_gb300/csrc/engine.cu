@@ -174,18 +174,19 @@ constexpr long long kListCap = 8ll * 1024 * 1024;  // >= 64 patch boxes of 49^3 
 // Clusters of the hierarchical winding evaluation for the packed triangles (w.t9).
 int build_fwn(Workspace& w, const Lattice& L, long long T, Fwn& f, Err& e) {
     cudaStream_t st = w.st;
-    const long long ncap = std::max<long long>(1, std::min<long long>(L.nbricks, T));
+    const FwnGrid g = fwn_grid(L, T);
+    const long long ncap = std::max<long long>(1, std::min<long long>(g.cells, T));
     GB_CK(ensure(w.fwc, (size_t)ncap * sizeof(FwnCell)));
     GB_CK(ensure(w.fwt, (size_t)T * 4));
     GB_CK(ensure(w.fwo, (size_t)T * 4));
-    GB_CK(ensure(w.fwn, (size_t)L.nbricks * 4));
-    GB_CK(ensure(w.fwu, (size_t)L.nbricks * 4));
-    GB_CK(ensure(w.fwf, (size_t)L.nbricks * 4));
-    GB_CK(ensure(w.fwoff, (size_t)L.nbricks * 8));
-    GB_CK(ensure(w.fwci, (size_t)L.nbricks * 8));
-    GB_CK(ensure(w.fwscan, (size_t)fwn_scan_elems(L) * 8));
+    GB_CK(ensure(w.fwn, (size_t)g.cells * 4));
+    GB_CK(ensure(w.fwu, (size_t)g.cells * 4));
+    GB_CK(ensure(w.fwf, (size_t)g.cells * 4));
+    GB_CK(ensure(w.fwoff, (size_t)g.cells * 8));
+    GB_CK(ensure(w.fwci, (size_t)g.cells * 8));
+    GB_CK(ensure(w.fwscan, (size_t)fwn_scan_elems(g) * 8));
     GB_CK(ensure(w.fwfb, (size_t)kListCap * 8));
-    f = Fwn{P<FwnCell>(w.fwc), P<unsigned>(w.fwt), P<unsigned>(w.fwo), P<unsigned>(w.fwn), P<unsigned>(w.fwu),
+    f = Fwn{g, P<FwnCell>(w.fwc), P<unsigned>(w.fwt), P<unsigned>(w.fwo), P<unsigned>(w.fwn), P<unsigned>(w.fwu),
             P<unsigned>(w.fwf), P<unsigned long long>(w.fwoff), P<unsigned long long>(w.fwci),
             P<unsigned long long>(w.fwscan), P<long long>(w.fwfb), kListCap};
     launch_fwn_build(P<float>(w.t9), T, L, f, w.ds, st);

@@ -140,7 +140,7 @@ void launch_gwn_team(const float* tri9, long long T, const Lattice& L, const lon
                      int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st, int only_if = 0);
 
 // ---- hierarchical winding numbers --------------------------------------------------
-// Triangles clustered by the 8^3 brick of their centroid; each cluster keeps its
+// Triangles clustered by the grid cube of their centroid; each cluster keeps its
 // area-weighted centroid c, area vector D = sum(a_i n_i), first moment M = sum(a_i n_i
 // (g_i - c)^T) (g_i the triangle centroids; exact for flat triangles), area A and radius r
 // (every vertex within r of c). Seen from q at distance d > beta r, with y = c - q, the
@@ -156,20 +156,30 @@ struct FwnCell {
     unsigned off, cnt, pad0;
 };
 static_assert(sizeof(FwnCell) == 80, "FwnCell layout");
+// The cluster grid: cubes of s voxels (s = 8, halved down to 2 while the triangles would
+// average more than 16 per cube), covering the lattice; triangles are binned by centroid
+// (clamped to the grid).
+struct FwnGrid {
+    int s;
+    int n[3];
+    long long cells;
+};
+FwnGrid fwn_grid(const Lattice& L, long long T);
 struct Fwn {
-    FwnCell* cells;           // capacity: min(bricks, triangles)
+    FwnGrid g;
+    FwnCell* cells;           // capacity: min(grid cells, triangles)
     unsigned* tri;            // triangles by cluster
     unsigned* cell_of;        // cluster brick of each triangle
-    unsigned* counts;         // per brick
-    unsigned* cursor;         // per brick
-    unsigned* flag;           // per brick: non-empty
-    unsigned long long* off;  // per brick
-    unsigned long long* cidx; // per brick: cluster index
+    unsigned* counts;         // per grid cell
+    unsigned* cursor;         // per grid cell
+    unsigned* flag;           // per grid cell: non-empty
+    unsigned long long* off;  // per grid cell
+    unsigned long long* cidx; // per grid cell: cluster index
     unsigned long long* scan; // scan scratch
     long long* fb;            // voxels left to the exact sum
     long long fb_cap;
 };
-long long fwn_scan_elems(const Lattice& L);
+long long fwn_scan_elems(const FwnGrid& g);
 // Builds the clusters of the packed triangles (device only, no host round trip).
 void launch_fwn_build(const float* tri9, long long T, const Lattice& L, const Fwn& f, DevState* ds, cudaStream_t st);
 // Decides the listed voxels (as launch_gwn does) by the cluster bound, then sums the rest

@@ -177,8 +177,8 @@ constexpr float kFwnSlackAbs = 1e-5f;  // rounding slack in w
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-__global__ void fwn_count_kernel(const float* __restrict__ t9, long long T, Lattice L, unsigned* __restrict__ cell_of,
-                                 unsigned* __restrict__ counts) {
+__global__ void fwn_count_kernel(const float* __restrict__ t9, long long T, Lattice L, FwnGrid g,
+                                 unsigned* __restrict__ cell_of, unsigned* __restrict__ counts) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T) return;
     const float* v = t9 + 9 * t;
@@ -186,12 +186,12 @@ __global__ void fwn_count_kernel(const float* __restrict__ t9, long long T, Latt
     int b[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const float g = (v[k] + v[3 + k] + v[6 + k]) * (1.0f / 3.0f);
-        const float rel = g * inv - (float)L.mn[k];
-        const float c = floorf(rel / (float)kBrick);
-        b[k] = clampi(c != c ? 0 : (int)fmaxf(fminf(c, 1e9f), -1e9f), 0, L.nb[k] - 1);
+        const float gc = (v[k] + v[3 + k] + v[6 + k]) * (1.0f / 3.0f);
+        const float rel = gc * inv - (float)L.mn[k];
+        const float c = floorf(rel / (float)g.s);
+        b[k] = clampi(c != c ? 0 : (int)fmaxf(fminf(c, 1e9f), -1e9f), 0, g.n[k] - 1);
     }
-    const unsigned cell = (unsigned)(((long long)b[2] * L.nb[1] + b[1]) * L.nb[0] + b[0]);
+    const unsigned cell = (unsigned)(((long long)b[2] * g.n[1] + b[1]) * g.n[0] + b[0]);
     cell_of[t] = cell;
     atomicAdd(&counts[cell], 1u);
 }
@@ -210,76 +210,84 @@ __global__ void fwn_fill_kernel(long long T, const unsigned* __restrict__ cell_o
     tri[off[c] + atomicAdd(&cursor[c], 1u)] = (unsigned)t;
 }
 
-// one thread per brick; the statistics in FP64, the radius rounded up
-__global__ void fwn_stats_kernel(const float* __restrict__ t9, Lattice L, const unsigned* __restrict__ counts,
+__device__ __forceinline__ double warp_sum_d(double x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// one warp per grid cell: FP64 statistics, the lanes splitting the cell's triangles;
+// the radius about the stored (FP32) centroid, rounded up
+__global__ void fwn_stats_kernel(const float* __restrict__ t9, long long ncg, const unsigned* __restrict__ counts,
                                  const unsigned long long* __restrict__ off, const unsigned* __restrict__ flag,
                                  const unsigned long long* __restrict__ cidx, const unsigned* __restrict__ tri,
                                  FwnCell* __restrict__ cells, DevState* ds) {
-    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= L.nbricks) return;
-    if (b == L.nbricks - 1) ds->fwn_cells = cidx[b] + flag[b];
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (b >= ncg) return;
+    if (b == ncg - 1 && lane == 0) ds->fwn_cells = cidx[b] + flag[b];
     const unsigned n = counts[b];
     if (!n) return;
     const unsigned long long o = off[b];
-    double A = 0.0, ax = 0.0, ay = 0.0, az = 0.0, gx = 0.0, gy = 0.0, gz = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
-    double M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // sum_t D_t (g_t)^T; shifted to c below
-    for (unsigned k = 0; k < n; ++k) {
+    double A = 0.0, D[3] = {0, 0, 0}, G[3] = {0, 0, 0}, mean[3] = {0, 0, 0};
+    double M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // sum_t D_t g_t^T; shifted to c below
+    for (unsigned k = lane; k < n; k += 32) {
         const float* v = t9 + 9ull * tri[o + k];
         const double e1x = (double)v[3] - v[0], e1y = (double)v[4] - v[1], e1z = (double)v[5] - v[2];
         const double e2x = (double)v[6] - v[0], e2y = (double)v[7] - v[1], e2z = (double)v[8] - v[2];
-        const double cx = 0.5 * (e1y * e2z - e1z * e2y), cy = 0.5 * (e1z * e2x - e1x * e2z),
-                     cz = 0.5 * (e1x * e2y - e1y * e2x);
-        const double a = sqrt(cx * cx + cy * cy + cz * cz);
-        const double px = ((double)v[0] + v[3] + v[6]) / 3.0, py = ((double)v[1] + v[4] + v[7]) / 3.0,
-                     pz = ((double)v[2] + v[5] + v[8]) / 3.0;
+        const double Dt[3] = {0.5 * (e1y * e2z - e1z * e2y), 0.5 * (e1z * e2x - e1x * e2z),
+                              0.5 * (e1x * e2y - e1y * e2x)};
+        const double a = sqrt(Dt[0] * Dt[0] + Dt[1] * Dt[1] + Dt[2] * Dt[2]);
+        const double gt[3] = {((double)v[0] + v[3] + v[6]) / 3.0, ((double)v[1] + v[4] + v[7]) / 3.0,
+                              ((double)v[2] + v[5] + v[8]) / 3.0};
         A += a;
-        ax += cx;
-        ay += cy;
-        az += cz;
-        gx += a * px;
-        gy += a * py;
-        gz += a * pz;
-        mx += px;
-        my += py;
-        mz += pz;
-        const double Dt[3] = {cx, cy, cz}, gt[3] = {px, py, pz};
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) M[3 * i + j] += Dt[i] * gt[j];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            D[i] += Dt[i];
+            G[i] += a * gt[i];
+            mean[i] += gt[i];
+#pragma unroll
+            for (int j2 = 0; j2 < 3; ++j2) M[3 * i + j2] += Dt[i] * gt[j2];
+        }
     }
-    double c0, c1, c2;
-    if (A > 0.0) {
-        c0 = gx / A;
-        c1 = gy / A;
-        c2 = gz / A;
-    } else {
-        c0 = mx / n;
-        c1 = my / n;
-        c2 = mz / n;
+    A = warp_sum_d(A);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        D[i] = warp_sum_d(D[i]);
+        G[i] = warp_sum_d(G[i]);
+        mean[i] = warp_sum_d(mean[i]);
     }
-    // the centroid as stored (FP32), the radius about that point, rounded up
-    const float fc0 = (float)c0, fc1 = (float)c1, fc2 = (float)c2;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) M[i] = warp_sum_d(M[i]);
+    const double c0 = (A > 0.0) ? G[0] / A : mean[0] / n;
+    const double c1 = (A > 0.0) ? G[1] / A : mean[1] / n;
+    const double c2 = (A > 0.0) ? G[2] / A : mean[2] / n;
+    const float fc[3] = {(float)c0, (float)c1, (float)c2};
     double r2 = 0.0;
-    for (unsigned k = 0; k < n; ++k) {
+    for (unsigned k = lane; k < n; k += 32) {
         const float* v = t9 + 9ull * tri[o + k];
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            const double dx = (double)v[3 * q] - fc0, dy = (double)v[3 * q + 1] - fc1, dz = (double)v[3 * q + 2] - fc2;
+            const double dx = (double)v[3 * q] - fc[0], dy = (double)v[3 * q + 1] - fc[1],
+                         dz = (double)v[3 * q + 2] - fc[2];
             r2 = fmax(r2, dx * dx + dy * dy + dz * dz);
         }
     }
+#pragma unroll
+    for (int off2 = 16; off2 > 0; off2 >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xffffffffu, r2, off2));
+    if (lane != 0) return;
     FwnCell c;
-    c.cx = fc0;
-    c.cy = fc1;
-    c.cz = fc2;
+    c.cx = fc[0];
+    c.cy = fc[1];
+    c.cz = fc[2];
     c.r = (float)(sqrt(r2) * (1.0 + 1e-6)) + 1e-30f;
-    c.ax = (float)ax;
-    c.ay = (float)ay;
-    c.az = (float)az;
+    c.ax = (float)D[0];
+    c.ay = (float)D[1];
+    c.az = (float)D[2];
     c.area = (float)(A * (1.0 + 1e-6));
     // moment about the stored centroid: sum D_t (g_t - c)^T = M - D c^T
-    const double D3[3] = {ax, ay, az}, cc[3] = {(double)fc0, (double)fc1, (double)fc2};
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) c.m[3 * i + j] = (float)(M[3 * i + j] - D3[i] * cc[j]);
+        for (int j2 = 0; j2 < 3; ++j2) c.m[3 * i + j2] = (float)(M[3 * i + j2] - D[i] * (double)fc[j2]);
     c.off = (unsigned)o;
     c.cnt = n;
     c.pad0 = 0;
@@ -525,23 +533,39 @@ void launch_gwn_team(const float* tri9, long long T, const Lattice& L, const lon
                                                                      surf_tol_vox, ds);
 }
 
-long long fwn_scan_elems(const Lattice& L) { return scan_tmp_elems(L.nbricks); }
+FwnGrid fwn_grid(const Lattice& L, long long T) {
+    FwnGrid g{};
+    int s = 8;
+    auto cells_at = [&](int side) {
+        long long c = 1;
+        for (int k = 0; k < 3; ++k) c *= (L.dims[k] + side - 1) / side;
+        return c;
+    };
+    while (s > 2 && T > 16 * cells_at(s)) s /= 2;
+    g.s = s;
+    for (int k = 0; k < 3; ++k) g.n[k] = (L.dims[k] + s - 1) / s;
+    g.cells = cells_at(s);
+    return g;
+}
+
+long long fwn_scan_elems(const FwnGrid& g) { return scan_tmp_elems(g.cells); }
 
 void launch_fwn_build(const float* tri9, long long T, const Lattice& L, const Fwn& f, DevState* ds, cudaStream_t st) {
     if (T <= 0) return;
-    cudaMemsetAsync(f.counts, 0, (size_t)L.nbricks * 4, st);
-    cudaMemsetAsync(f.cursor, 0, (size_t)L.nbricks * 4, st);
+    const long long nc = f.g.cells;
+    cudaMemsetAsync(f.counts, 0, (size_t)nc * 4, st);
+    cudaMemsetAsync(f.cursor, 0, (size_t)nc * 4, st);
     GBSDF_COUNT_LAUNCH();
-    fwn_count_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(tri9, T, L, f.cell_of, f.counts);
-    launch_exclusive_scan(f.counts, f.off, L.nbricks, f.scan, 0, st);
+    fwn_count_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(tri9, T, L, f.g, f.cell_of, f.counts);
+    launch_exclusive_scan(f.counts, f.off, nc, f.scan, 0, st);
     GBSDF_COUNT_LAUNCH();
-    fwn_flag_kernel<<<(unsigned)((L.nbricks + 255) / 256), 256, 0, st>>>(f.counts, L.nbricks, f.flag);
-    launch_exclusive_scan(f.flag, f.cidx, L.nbricks, f.scan, 0, st);
+    fwn_flag_kernel<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(f.counts, nc, f.flag);
+    launch_exclusive_scan(f.flag, f.cidx, nc, f.scan, 0, st);
     GBSDF_COUNT_LAUNCH();
     fwn_fill_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(T, f.cell_of, f.off, f.cursor, f.tri);
     GBSDF_COUNT_LAUNCH();
-    fwn_stats_kernel<<<(unsigned)((L.nbricks + 127) / 128), 128, 0, st>>>(tri9, L, f.counts, f.off, f.flag, f.cidx,
-                                                                         f.tri, f.cells, ds);
+    fwn_stats_kernel<<<(unsigned)((nc * 32 + 255) / 256), 256, 0, st>>>(tri9, nc, f.counts, f.off, f.flag, f.cidx,
+                                                                        f.tri, f.cells, ds);
 }
 
 void launch_winding(const Fwn* f, const float* tri9, long long T, const Lattice& L, const long long* list,
