@@ -294,6 +294,46 @@ __global__ void fill_tail_kernel(float* __restrict__ g, long long from, long lon
 
 constexpr int kSplatThreads = 128;
 constexpr int kSplatChunk = 64;
+constexpr unsigned kSplatCullMin = 256;  // triangles binned to a brick before culling starts
+
+// The staged chunk's triangles against one thread's 4 voxels (x, y, zb + 2k). CULL: skip
+// a triangle whose bounding-box distance^2 exceeds the voxel's best exact distance^2 by
+// more than both computations' rounding (a few ulps of the largest coordinate), which
+// cannot lower the minimum -- the result stays bit-identical.
+template <bool CULL>
+__device__ __forceinline__ void splat_chunk(const SplatTri* s, unsigned m, int x, int y, float px, float py,
+                                            const float wz[4], float bw, float band_sq, float best[4],
+                                            unsigned& evals) {
+    for (unsigned i = 0; i < m; ++i) {
+        const SplatTri& r = s[i];
+        if (x < r.fx0 || x > r.fx1 || y < r.fy0 || y > r.fy1) continue;
+        const float tx0 = r.bb[0], tx1 = r.bb[1], ty0 = r.bb[2], ty1 = r.bb[3], tz0 = r.bb[4], tz1 = r.bb[5];
+        const float bdx = (px < tx0) ? (tx0 - px) : ((px > tx1) ? (px - tx1) : 0.0f);
+        const float bdy = (py < ty0) ? (ty0 - py) : ((py > ty1) ? (py - ty1) : 0.0f);
+        const float bxy = bdx * bdx + bdy * bdy;
+        const f3 a = mk(r.v[0], r.v[1], r.v[2]), bb = mk(r.v[3], r.v[4], r.v[5]), c = mk(r.v[6], r.v[7], r.v[8]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float z = wz[k];
+            if (z < tz0 - bw || z > tz1 + bw) continue;
+            const float bdz = (z < tz0) ? (tz0 - z) : ((z > tz1) ? (z - tz1) : 0.0f);
+            const float lb = bxy + bdz * bdz;
+            if (lb > band_sq) continue;
+            if constexpr (CULL) {
+                if (best[k] < band_sq) {
+                    const float sc = fmaxf(fmaxf(fmaxf(fabsf(px), fabsf(py)), fmaxf(fabsf(tx0), fabsf(tx1))),
+                                           fmaxf(fmaxf(fabsf(ty0), fabsf(ty1)), fmaxf(fabsf(tz0), fabsf(tz1))));
+                    const float dz = fmaxf(sc, fabsf(z)) * 3.814697265625e-6f;  // 2^-18 of the magnitude
+                    const float margin = 4.0f * dz * (sqrtf(best[k]) + dz) + best[k] * 1e-5f;
+                    if (lb > best[k] + margin) continue;
+                }
+            }
+            const float d2 = ptd_sq(mk(px, py, z), a, bb, c);
+            ++evals;
+            if (d2 <= band_sq && d2 < best[k]) best[k] = d2;
+        }
+    }
+}
 
 __global__ void __launch_bounds__(kSplatThreads) splat_kernel(
     const SplatTri* __restrict__ stt, const unsigned long long* __restrict__ off, const unsigned* __restrict__ cnt,
@@ -321,6 +361,9 @@ __global__ void __launch_bounds__(kSplatThreads) splat_kernel(
     }
     const unsigned long long o = off[b];
     const unsigned n = cnt[b];
+    // culling pays where many triangles compete for a brick (dense meshes); with few, its
+    // test costs more than the evaluations it saves
+    const bool cull = n > kSplatCullMin;
     unsigned evals = 0;
     for (unsigned c0 = 0; c0 < n; c0 += kSplatChunk) {
         unsigned m = min((unsigned)kSplatChunk, n - c0);
@@ -333,25 +376,10 @@ __global__ void __launch_bounds__(kSplatThreads) splat_kernel(
             dsm[w] = __ldg(src + (size_t)t * 24 + word);
         }
         __syncthreads();
-        for (unsigned i = 0; i < m; ++i) {
-            const SplatTri& r = s[i];
-            if (x < r.fx0 || x > r.fx1 || y < r.fy0 || y > r.fy1) continue;
-            const float tx0 = r.bb[0], tx1 = r.bb[1], ty0 = r.bb[2], ty1 = r.bb[3], tz0 = r.bb[4], tz1 = r.bb[5];
-            const float bdx = (px < tx0) ? (tx0 - px) : ((px > tx1) ? (px - tx1) : 0.0f);
-            const float bdy = (py < ty0) ? (ty0 - py) : ((py > ty1) ? (py - ty1) : 0.0f);
-            const float bxy = bdx * bdx + bdy * bdy;
-            const f3 a = mk(r.v[0], r.v[1], r.v[2]), bb = mk(r.v[3], r.v[4], r.v[5]), c = mk(r.v[6], r.v[7], r.v[8]);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float z = wz[k];
-                if (z < tz0 - bw || z > tz1 + bw) continue;
-                const float bdz = (z < tz0) ? (tz0 - z) : ((z > tz1) ? (z - tz1) : 0.0f);
-                if (bxy + bdz * bdz > band_sq) continue;
-                const float d2 = ptd_sq(mk(px, py, z), a, bb, c);
-                ++evals;
-                if (d2 <= band_sq && d2 < best[k]) best[k] = d2;
-            }
-        }
+        if (cull)
+            splat_chunk<true>(s, m, x, y, px, py, wz, bw, band_sq, best, evals);
+        else
+            splat_chunk<false>(s, m, x, y, px, py, wz, bw, band_sq, best, evals);
         __syncthreads();
     }
     unsigned found = 0;
