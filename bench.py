@@ -115,10 +115,10 @@ def whole_job_gvox(world: int, voxels_per_rank: int, ms_per_step: float) -> floa
     return world * voxels_per_rank / (ms_per_step * 1e-3) / 1e9
 
 
-def make_workload(dims=None, h=None):
+def make_workload(dims=None, h=None, name=WORKLOAD):
     from gbsdf import meshgen
 
-    tris, mn, mx, h = meshgen.workload(WORKLOAD, dims=dims, h=h)
+    tris, mn, mx, h = meshgen.workload(name, dims=dims, h=h)
     return tris, mn, mx, h
 
 
@@ -266,6 +266,8 @@ def main():
     ap.add_argument("--ref-slab", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     # profiling of a smaller lattice of the same mesh (never the reported configuration)
+    ap.add_argument("--workload", default=WORKLOAD, help="a named workload of gbsdf.meshgen.WORKLOADS "
+                    "(the bench's own is mug_c2_860; the others are for profiling and comparison runs)")
     ap.add_argument("--dims", default=None, help="lattice override nx,ny,nz (profiling runs)")
     ap.add_argument("--h", type=float, default=None, help="voxel size override (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
@@ -300,7 +302,7 @@ def main():
              "learned": gbsdf.MODE_LEARNED}
     mode = modes[args.mode]
     dims_override = tuple(int(x) for x in args.dims.split(",")) if args.dims else None
-    tris, mn, mx, h = make_workload(dims_override, args.h)
+    tris, mn, mx, h = make_workload(dims_override, args.h, args.workload)
     mlp = None
     if mode == gbsdf.MODE_LEARNED:
         from gbsdf import learn
@@ -395,7 +397,8 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{WORKLOAD}: procedural mug (cup of revolution + swept-torus handle), "
+            "config": {"workload": (f"{WORKLOAD}: procedural mug (cup of revolution + swept-torus handle), "
+                                    if args.workload == WORKLOAD else f"{args.workload}: ") +
                                    f"{'x'.join(str(int(d)) for d in dims)} lattice at {h:g} mm, {T} triangles, "
                                    "fast path",
                        "mode": args.mode, "parallelism": "replicas" if world > 1 else "single GPU",
