@@ -102,12 +102,12 @@ typedef struct gbsdf_options {
     const float* mlp_params; /* learned mode: GBSDF_MLP_PARAMS FP32 parameters in device memory */
     const float* brick_scores; /* learned mode, instead of the network: caller-supplied risk
                                   logits, one per 8^3 brick (x fastest), in device memory */
-    int32_t sweep_schedule; /* eikonal sweep schedules (identical results): 0 = autotuned (the
-                               first build of a lattice class times the candidates); 1, 2, 3 =
-                               x sweep staged by cp.async, by TMA tiles on a CTA-barrier ring, by
-                               TMA tiles on a warp-specialised mbarrier pipeline (y / z walks:
-                               default); 4, 5 = x pipeline with cp.async-staged / TMA-pipelined
-                               y / z walks. TMA needs rows of a multiple of 4 voxels. */
+    int32_t sweep_schedule; /* eikonal sweep schedules (identical results), x + 10 w: x = 1 x sweep
+                               staged by cp.async, 2 by TMA tiles on a CTA-barrier ring, 3 by TMA
+                               tiles on a warp-specialised mbarrier pipeline; w = 1 y / z walks
+                               staged by cp.async, 2 by TMA batches on a pipeline; a 0 digit (and
+                               0 overall) = autotuned (the first build of a lattice class times
+                               the candidates). TMA needs rows of a multiple of 4 voxels. */
     int32_t host_output;    /* host outputs: 0 = a page-locked output is written by the sign-apply
                                kernel through its device mapping (no staging copy), others are
                                staged in device memory and copied; 1 = always stage and copy */

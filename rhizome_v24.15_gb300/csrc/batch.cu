@@ -282,11 +282,9 @@ int plan(gbsdf_batch& b, BErr& e) {
             const SweepPlan plan = tuned_sweep_plan(b.device, j.L, j.A, j.B, &j.map_a, j.ds, b.origin, false);
             j.xsched = plan.x;
             j.wsched = plan.w;
-            if (b.sweep_schedule >= kXCpAsync && b.sweep_schedule <= kXTmaPipe) j.xsched = b.sweep_schedule;
-            if (b.sweep_schedule == 4 || b.sweep_schedule == 5) {
-                j.xsched = kXTmaPipe;
-                j.wsched = b.sweep_schedule == 4 ? kWCpAsync : kWTmaPipe;
-            }
+            const int xs_opt = b.sweep_schedule % 10, ws_opt = b.sweep_schedule / 10;
+            if (xs_opt >= kXCpAsync && xs_opt <= kXTmaPipe) j.xsched = xs_opt;
+            if (ws_opt == kWCpAsync || ws_opt == kWTmaPipe) j.wsched = ws_opt;
         }
     // counting pass
     for (Job& j : b.jobs) {

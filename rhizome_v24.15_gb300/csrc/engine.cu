@@ -350,14 +350,11 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     encode_grid_map(map_a, P<float>(w.A), L);
     encode_grid_map(map_b, P<float>(w.B), L);
     auto map_of = [&](const float* p) { return p == P<float>(w.A) ? &map_a : &map_b; };
-    // sweep_schedule: 0 autotuned; 1..3 x schedule (with the walks' default); 4 / 5 force the
-    // cp.async / TMA-pipeline walks with the x pipeline
-    SweepPlan plan = tuned_sweep_plan(w.device, L, src, dst, &map_a, w.ds, st, o.sweep_schedule == 0);
-    if (o.sweep_schedule >= kXCpAsync && o.sweep_schedule <= kXTmaPipe) plan.x = o.sweep_schedule;
-    if (o.sweep_schedule == 4 || o.sweep_schedule == 5) {
-        plan.x = kXTmaPipe;
-        plan.w = o.sweep_schedule == 4 ? kWCpAsync : kWTmaPipe;
-    }
+    // sweep_schedule: 0 autotuned; else x schedule + 10 x walk schedule (a 0 digit: tuned)
+    const int xs_opt = o.sweep_schedule % 10, ws_opt = o.sweep_schedule / 10;
+    SweepPlan plan = tuned_sweep_plan(w.device, L, src, dst, &map_a, w.ds, st, xs_opt == 0 || ws_opt == 0);
+    if (xs_opt >= kXCpAsync && xs_opt <= kXTmaPipe) plan.x = xs_opt;
+    if (ws_opt == kWCpAsync || ws_opt == kWTmaPipe) plan.w = ws_opt;
     const int xsched = plan.x, wsched = plan.w;
     if (ref_eikonal) {
         for (int r = 0; r < kMaxRounds; ++r) {

@@ -210,8 +210,9 @@ struct GridMap {
 };
 bool encode_grid_map(GridMap& m, const float* base, const Lattice& L);
 // Schedules of the x sweep (all give identical results): staged by per-thread cp.async
-// copies, by TMA tiles on a CTA-barrier ring, or by TMA tiles on a warp-specialised
-// mbarrier pipeline. 0 picks the pipeline when a TMA descriptor is valid.
+// copies, by TMA tiles on a CTA-barrier ring, by TMA tiles on a warp-specialised mbarrier
+// pipeline. 0 picks the pipeline when a TMA
+// descriptor is valid.
 enum XSchedule : int { kXAuto = 0, kXCpAsync = 1, kXTmaRing = 2, kXTmaPipe = 3 };
 // Schedules of the y and z walks: cp.async slice ring, or TMA batches on a
 // warp-specialised mbarrier pipeline. 0 picks the pipeline when its descriptors are valid.
