@@ -105,7 +105,8 @@ typedef struct gbsdf_options {
     int32_t sweep_schedule; /* eikonal sweep schedules (identical results), x + 10 w: x = 1 x sweep
                                staged by cp.async, 2 by TMA tiles on a CTA-barrier ring, 3 by TMA
                                tiles on a warp-specialised mbarrier pipeline; w = 1 y / z walks
-                               staged by cp.async, 2 by TMA batches on a pipeline; a 0 digit (and
+                               staged by cp.async, 2 by TMA batches on a pipeline, 3 the same
+                               with four adjacent lines per thread; a 0 digit (and
                                0 overall) = autotuned (the first build of a lattice class times
                                the candidates). TMA needs rows of a multiple of 4 voxels. */
     int32_t host_output;    /* host outputs: 0 = a page-locked output is written by the sign-apply
@@ -146,7 +147,7 @@ typedef struct gbsdf_stats {
     int64_t kernel_launches; /* CUDA kernels this call launched */
     int64_t proposed;      /* learned mode: bricks the network proposed for the exact winding number */
     int64_t sweep_schedule; /* schedules that ran: x schedule (1-3) + 10 x walk schedule
-                               (1 cp.async, 2 TMA pipeline) */
+                               (1 cp.async, 2 TMA pipeline, 3 TMA pipeline, 4 lines/thread) */
     int64_t winding_certified; /* exact winding decisions settled by the cluster bound */
     int64_t winding_summed;    /* ... and by the triangle-by-triangle sum */
     int64_t reserved[3];

@@ -90,8 +90,10 @@ struct Job {
     cudaStream_t st = nullptr;
     GridMap map_a{}, map_b{};  // TMA descriptors of A and B
     Fwn fwn{};                 // clusters of the hierarchical winding evaluation
-    int xsched = kXAuto;       // sweep schedules (a tuned class's winners, else the defaults)
-    int wsched = kWAuto;
+    int xsched = kXAuto;       // sweep schedules of the first round (a tuned class's winners,
+    int wsched = kWAuto;       // else the defaults) ...
+    int xsched1 = kXAuto;      // ... and of the later rounds
+    int wsched1 = kWAuto;
 };
 
 // Carves aligned sub-buffers out of one allocation: a sizing pass, then a placing pass.
@@ -227,7 +229,7 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
         for (int axis = 0; axis < 3; ++axis)
             for (int dir = 1; dir >= -1; dir -= 2) {
                 launch_sweep(0, axis, dir, r, src, dst, L, j.ds, st, src == j.A ? &j.map_a : &j.map_b,
-                             j.xsched, j.wsched);
+                             r == 0 ? j.xsched : j.xsched1, r == 0 ? j.wsched : j.wsched1);
                 std::swap(src, dst);
             }
         launch_end_round(r, r, kMaxRounds, j.ds, st);
@@ -279,12 +281,15 @@ int plan(gbsdf_batch& b, BErr& e) {
             place_phase1(j, p1);
             encode_grid_map(j.map_a, j.A, j.L);
             encode_grid_map(j.map_b, j.B, j.L);
-            const SweepPlan plan = tuned_sweep_plan(b.device, j.L, j.A, j.B, &j.map_a, j.ds, b.origin, false);
+            const SweepPlan plan = tuned_sweep_plan(b.device, j.L, j.A, j.B, &j.map_a, j.ds, b.origin, false, 0);
+            const SweepPlan plan1 = tuned_sweep_plan(b.device, j.L, j.A, j.B, &j.map_a, j.ds, b.origin, false, 1);
             j.xsched = plan.x;
             j.wsched = plan.w;
+            j.xsched1 = plan1.x;
+            j.wsched1 = plan1.w;
             const int xs_opt = b.sweep_schedule % 10, ws_opt = b.sweep_schedule / 10;
-            if (xs_opt >= kXCpAsync && xs_opt <= kXTmaPipe) j.xsched = xs_opt;
-            if (ws_opt == kWCpAsync || ws_opt == kWTmaPipe) j.wsched = ws_opt;
+            if (xs_opt >= kXCpAsync && xs_opt <= kXTmaPipe) j.xsched = j.xsched1 = xs_opt;
+            if (ws_opt >= kWCpAsync && ws_opt <= kWTmaVec) j.wsched = j.wsched1 = ws_opt;
         }
     // counting pass
     for (Job& j : b.jobs) {
@@ -395,8 +400,8 @@ void fill_stats(const Job& j, int status, float ms, unsigned long long launches,
     s->csr_entries = (long long)h.csr_entries;
     s->winding_certified = (long long)h.fwn_certified;
     s->winding_summed = (long long)h.fwn_fallback_total;
-    s->sweep_schedule = (j.map_a.valid ? (j.xsched == kXAuto ? kXTmaPipe : j.xsched) : kXCpAsync) +
-                        10 * (j.map_a.walk_valid ? (j.wsched == kWAuto ? kWTmaPipe : j.wsched) : kWCpAsync);
+    s->sweep_schedule = (j.map_a.valid ? (j.xsched1 == kXAuto ? kXTmaPipe : j.xsched1) : kXCpAsync) +
+                        10 * (j.map_a.walk_valid ? (j.wsched1 == kWAuto ? kWTmaPipe : j.wsched1) : kWCpAsync);
 }
 
 int run_once(gbsdf_batch& b, bool& any_overflow, float& ms, BErr& e) {

@@ -350,17 +350,26 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     encode_grid_map(map_a, P<float>(w.A), L);
     encode_grid_map(map_b, P<float>(w.B), L);
     auto map_of = [&](const float* p) { return p == P<float>(w.A) ? &map_a : &map_b; };
-    // sweep_schedule: 0 autotuned; else x schedule + 10 x walk schedule (a 0 digit: tuned)
+    // sweep_schedule: 0 autotuned; else x schedule + 10 x walk schedule (a 0 digit: tuned).
+    // The first round and the later ones have their own tuned plans (phase 0 / 1).
     const int xs_opt = o.sweep_schedule % 10, ws_opt = o.sweep_schedule / 10;
-    SweepPlan plan = tuned_sweep_plan(w.device, L, src, dst, &map_a, w.ds, st, xs_opt == 0 || ws_opt == 0);
-    if (xs_opt >= kXCpAsync && xs_opt <= kXTmaPipe) plan.x = xs_opt;
-    if (ws_opt == kWCpAsync || ws_opt == kWTmaPipe) plan.w = ws_opt;
-    const int xsched = plan.x, wsched = plan.w;
+    const bool tune = xs_opt == 0 || ws_opt == 0;
+    SweepPlan plan;
+    auto set_plan = [&](int phase) -> int {
+        plan = tuned_sweep_plan(w.device, L, src, dst, map_of(src), w.ds, st, tune, phase);
+        if (xs_opt >= kXCpAsync && xs_opt <= kXTmaPipe) plan.x = xs_opt;
+        if (ws_opt >= kWCpAsync && ws_opt <= kWTmaVec) plan.w = ws_opt;
+        GB_CK(cudaGetLastError());
+        return (int)GBSDF_OK;
+    };
+    if (int rcp = set_plan(0)) return rcp;
     if (ref_eikonal) {
         for (int r = 0; r < kMaxRounds; ++r) {
+            if (r == 1)
+                if (int rcp = set_plan(1)) return rcp;
             for (int axis = 0; axis < 3; ++axis)
                 for (int dir = 1; dir >= -1; dir -= 2) {
-                    launch_sweep(rule, axis, dir, r, src, dst, L, w.ds, st, map_of(src), xsched, wsched);
+                    launch_sweep(rule, axis, dir, r, src, dst, L, w.ds, st, map_of(src), plan.x, plan.w);
                     std::swap(src, dst);
                 }
             launch_end_round(r, r, kMaxRounds, w.ds, st);
@@ -370,10 +379,12 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         const int batch = 4;
         for (int r0 = 0; r0 < cap; r0 += batch) {
             for (int r = r0; r < std::min(cap, r0 + batch); ++r) {
+                if (r == 1)
+                    if (int rcp = set_plan(1)) return rcp;
                 GB_CK(cudaMemsetAsync(&w.ds->changed[r % 64], 0, sizeof(int), st));
                 for (int axis = 0; axis < 3; ++axis)
                     for (int dir = 1; dir >= -1; dir -= 2) {
-                        launch_sweep(rule, axis, dir, r % 64, src, dst, L, w.ds, st, map_of(src), xsched, wsched);
+                        launch_sweep(rule, axis, dir, r % 64, src, dst, L, w.ds, st, map_of(src), plan.x, plan.w);
                         std::swap(src, dst);
                     }
                 launch_end_round(r % 64, r, cap, w.ds, st);
@@ -510,8 +521,9 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         stats->proposed = (long long)h.proposed;
         stats->winding_certified = (long long)h.fwn_certified;
         stats->winding_summed = (long long)h.fwn_fallback_total;
-        // x schedule + 10 x walk schedule of what ran
-        stats->sweep_schedule = (map_a.valid ? xsched : kXCpAsync) + 10 * (map_a.walk_valid ? wsched : kWCpAsync);
+        // x schedule + 10 x walk schedule of the last round's sweeps
+        stats->sweep_schedule = (map_a.valid ? (plan.x == kXAuto ? kXTmaPipe : plan.x) : kXCpAsync) +
+                                10 * (map_a.walk_valid ? (plan.w == kWAuto ? kWTmaPipe : plan.w) : kWCpAsync);
     }
     return status;
 }

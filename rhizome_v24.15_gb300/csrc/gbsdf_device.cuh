@@ -165,6 +165,28 @@ __device__ __forceinline__ float godunov_ref(float ax, float ay, float az, float
     return updated;
 }
 
+// godunov_ref with the 1D, 2D and 3D candidates all formed and the reference's branch
+// conditions selecting among them (same operands, same roundings). Past the first sweeps
+// more than 95% of warp steps hold a lane that needs the 2D update and most hold one that
+// needs the 3D update, so branching saves little; without branches the updates of a
+// thread's independent lines interleave. A square root whose candidate is not selected
+// takes 1 in place of a negative discriminant.
+__device__ __forceinline__ float godunov_ref_sel(float ax, float ay, float az, float h) {
+    const float s0 = fminf(ax, fminf(ay, az));
+    const float s2 = fmaxf(ax, fmaxf(ay, az));
+    const float s1 = ax + ay + az - s0 - s2;
+    const float u1 = s0 + h;
+    const float d10 = (s1 - s0) * (s1 - s0);
+    const float disc = 2.0f * h * h - d10;
+    const float disc3 = 3.0f * h * h - (d10 + (s2 - s1) * (s2 - s1) + (s2 - s0) * (s2 - s0)) * 0.5f;
+    const bool ok2 = disc >= 0.0f, ok3 = disc3 >= 0.0f;
+    const float u2 = (s0 + s1 + sqrtf(ok2 ? disc : 1.0f)) * 0.5f;
+    const float u3 = div3_rn(s0 + s1 + s2 + sqrtf(ok3 ? disc3 : 1.0f));
+    const bool take2 = (u1 > s1) && ok2;
+    const bool take3 = take2 && (u2 > s2) && ok3;
+    return take3 ? u3 : (take2 ? u2 : u1);
+}
+
 // Corrected, monotone Godunov update (the engine's exact mode): sorted minima,
 // true 3D discriminant 3h^2 - sum_{i<j}(s_i - s_j)^2, increments formed from
 // differences and added to the smallest neighbour once.
@@ -192,6 +214,13 @@ __device__ __forceinline__ float godunov_exact(float a, float b, float c, float 
 template <int RULE>
 __device__ __forceinline__ float godunov(float ax, float ay, float az, float h) {
     if constexpr (RULE == 0) return godunov_ref(ax, ay, az, h);
+    else return godunov_exact(ax, ay, az, h);
+}
+
+// The same updates for kernels that interleave several lines per thread.
+template <int RULE>
+__device__ __forceinline__ float godunov_sel(float ax, float ay, float az, float h) {
+    if constexpr (RULE == 0) return godunov_ref_sel(ax, ay, az, h);
     else return godunov_exact(ax, ay, az, h);
 }
 

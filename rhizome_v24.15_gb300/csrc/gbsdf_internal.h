@@ -214,21 +214,23 @@ bool encode_grid_map(GridMap& m, const float* base, const Lattice& L);
 // pipeline. 0 picks the pipeline when a TMA
 // descriptor is valid.
 enum XSchedule : int { kXAuto = 0, kXCpAsync = 1, kXTmaRing = 2, kXTmaPipe = 3 };
-// Schedules of the y and z walks: cp.async slice ring, or TMA batches on a
-// warp-specialised mbarrier pipeline. 0 picks the pipeline when its descriptors are valid.
-enum WSchedule : int { kWAuto = 0, kWCpAsync = 1, kWTmaPipe = 2 };
+// Schedules of the y and z walks: cp.async slice ring, TMA batches on a warp-specialised
+// mbarrier pipeline (one line per thread in two rows, or four adjacent lines per thread).
+// 0 picks the pipeline when its descriptors are valid.
+enum WSchedule : int { kWAuto = 0, kWCpAsync = 1, kWTmaPipe = 2, kWTmaVec = 3 };
 // `src_map`: the descriptor of `src` (or null); `x_schedule`: an XSchedule.
 void launch_sweep(int rule, int axis, int dir, int round, const float* src, float* dst, const Lattice& L,
                   DevState* ds, cudaStream_t st, const GridMap* src_map = nullptr, int x_schedule = kXAuto,
                   int w_schedule = kWAuto);
-// The sweep schedules for this lattice class: the remembered winners, else (measure)
-// each candidate timed on src -> dst (writes dst and changed[63]), else the pipelines.
+// The sweep schedules for this lattice class and phase (0: the first round, 1: later
+// rounds): the remembered winners, else (measure) each candidate timed on src -> dst
+// (writes dst and changed[63]), else the pipelines.
 struct SweepPlan {
     int x;  // XSchedule
     int w;  // WSchedule
 };
 SweepPlan tuned_sweep_plan(int device, const Lattice& L, const float* src, float* dst, const GridMap* src_map,
-                           DevState* ds, cudaStream_t st, bool measure);
+                           DevState* ds, cudaStream_t st, bool measure, int phase);
 // Layout check of the x sweep's TMA tile (swizzled rows, out-of-lattice fill): writes the
 // number of mismatching elements to *mism.
 int selftest_tma_tile(unsigned long long* mism);

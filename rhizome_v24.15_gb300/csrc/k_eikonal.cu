@@ -659,7 +659,7 @@ constexpr int kWPX = 40;                               // box columns
 constexpr int kWPB = 4;                                // slices per batch
 constexpr int kWPS = 4;                                // ring slots
 constexpr int kWPBox = kWPX * kWHR * kWPB;             // floats per batch (2880)
-constexpr int kWPSlotBytes = 12288;                    // batch bytes rounded up to 1 KB
+constexpr int kWPSlotBytes = (kWPBox * 4 + 1023) / 1024 * 1024;  // batch bytes rounded up to 1 KB
 constexpr int kWPThreads = kWThreads + 32;             // 8 consumer warps + 1 producer warp
 constexpr size_t kWPSmem = (size_t)kWPS * kWPSlotBytes + 128 + 1024;
 
@@ -787,6 +787,136 @@ __global__ void __launch_bounds__(kWPThreads) sweep_walk_pipe_kernel(const __gri
     mark_changed(ch, &ds->changed[round]);
 }
 
+// ---- y and z walks, TMA batches, four adjacent lines per thread ----------------------
+// sweep_walk_pipe_kernel's tile (32 x 16 lines), boxes and barriers with 4 consumer warps
+// and a 3-slot ring (more CTAs per SM): a thread walks the lines of 4 adjacent x in one
+// row, so a slice costs it one 16-byte shared load of the next slice, two of the
+// neighbouring rows, two scalar loads of the x neighbours at the quad's ends and one
+// 16-byte global store -- 1.5 memory instructions per voxel where one line per thread
+// issues 6 -- and the four branch-free updates interleave. Needs dim x a multiple of 4
+// (as the TMA boxes do) and a 16-byte aligned destination, so quads are all in or all out.
+constexpr int kWVConsumers = 128;
+constexpr int kWVThreads = kWVConsumers + 32;
+constexpr int kWVS = 3;                                // ring slots
+constexpr size_t kWVSmem = (size_t)kWVS * kWPSlotBytes + 128 + 1024;
+
+template <int AXIS, int RULE, int DIR>
+__global__ void __launch_bounds__(kWVThreads) sweep_walk_vec_kernel(const __grid_constant__ CUtensorMap tm,
+                                                                     float* __restrict__ dst, Lattice L,
+                                                                     int round, DevState* ds) {
+    if (ds->stop) return;
+    extern __shared__ unsigned char tsm_raw[];
+    unsigned char* tsm = align1k(tsm_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kWVS * kWPSlotBytes);
+    uint64_t* empty = full + kWVS;
+    const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
+    const size_t plane = (size_t)dx * dy;
+    const int n_walk = (AXIS == 2) ? dz : dy;
+    const int n_rows = (AXIS == 2) ? dy : dz;
+    const size_t step_stride = (AXIS == 2) ? plane : (size_t)dx;
+    const size_t row_stride = (AXIS == 2) ? (size_t)dx : plane;
+    constexpr int kSliceS = (AXIS == 2) ? kWHR * kWPX : kWPX;
+    constexpr int kRowS = (AXIS == 2) ? kWPX : kWPB * kWPX;
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * kWX, r0 = blockIdx.y * kWR;
+    const int nbatches = (n_walk + kWPB - 1) / kWPB;
+    if (tid == 0) {
+        for (int s = 0; s < kWVS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kWVConsumers / 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    if (tid >= kWVConsumers) {
+        if (tid != kWVConsumers) return;
+        int b = 0;
+        for (; b < nbatches; ++b) {
+            const int s = b % kWVS;
+            if (b >= kWVS && !mbar_wait(&empty[s], ((b / kWVS) - 1) & 1)) break;
+            const int sl0 = (DIR > 0) ? b * kWPB : n_walk - kWPB - b * kWPB;
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            mbar_expect_tx(&full[s], kWPBox * 4);
+            if (AXIS == 2) tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, r0 - 1, sl0, &full[s]);
+            else tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, sl0, r0 - 1, &full[s]);
+        }
+        if (b < nbatches) {
+            for (int k = max(0, b - kWVS); k < b; ++k) mbar_wait(&full[k % kWVS], (k / kWVS) & 1);
+            atomicAdd(&ds->wait_timeouts, 1ull);
+        }
+        return;
+    }
+    const int cx = tid & 7, tr = tid >> 3;       // quad of x, row
+    const int x = x0 + 4 * cx, r = r0 + tr;
+    const bool act = (x < dx) && (r < n_rows);  // dim x is a multiple of 4: the quad is all in
+    const float h = L.h;
+    const int m = (tr + 1) * kRowS + 4 * cx + 4;  // 16-byte aligned: kRowS, kSliceS are multiples of 4
+    auto slice_ptr = [&](int s) -> const float* {
+        const int b = s / kWPB, q = s - b * kWPB;
+        const int qb = (DIR > 0) ? q : (kWPB - 1 - q);
+        return reinterpret_cast<const float*>(tsm + (b % kWVS) * kWPSlotBytes) + qb * kSliceS;
+    };
+    float prev[4] = {kFarSentinel, kFarSentinel, kFarSentinel, kFarSentinel};
+    float cur[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    bool ch = false;
+    const long long sstep = (DIR > 0) ? (long long)step_stride : -(long long)step_stride;
+    float* p = dst + (size_t)((DIR > 0) ? 0 : n_walk - 1) * step_stride + (size_t)r * row_stride + x;
+#pragma unroll 1
+    for (int b = 0; b < nbatches; ++b) {
+        bool ok = mbar_wait(&full[b % kWVS], (b / kWVS) & 1);
+        if (ok && b + 1 < nbatches) ok = mbar_wait(&full[(b + 1) % kWVS], ((b + 1) / kWVS) & 1);
+        if (!__all_sync(0xffffffffu, ok)) {
+            if ((tid & 31) == 0) atomicAdd(&ds->wait_timeouts, 1ull);
+            return;
+        }
+        if (b == 0) {
+            const float4 c = *reinterpret_cast<const float4*>(slice_ptr(0) + m);
+            cur[0] = c.x; cur[1] = c.y; cur[2] = c.z; cur[3] = c.w;
+        }
+#pragma unroll
+        for (int q = 0; q < kWPB; ++q) {
+            const int s = b * kWPB + q;
+            if (s >= n_walk) break;
+            const float* cs = slice_ptr(s);
+            float nxt[4] = {kFarSentinel, kFarSentinel, kFarSentinel, kFarSentinel};
+            if (s + 1 < n_walk) {
+                const float4 n4 = *reinterpret_cast<const float4*>(slice_ptr(s + 1) + m);
+                nxt[0] = n4.x; nxt[1] = n4.y; nxt[2] = n4.z; nxt[3] = n4.w;
+            }
+            if (act) {
+                const float4 rm = *reinterpret_cast<const float4*>(cs + m - kRowS);
+                const float4 rp = *reinterpret_cast<const float4*>(cs + m + kRowS);
+                const float xl = cs[m - 1], xr = cs[m + 4];
+                const float rmv[4] = {rm.x, rm.y, rm.z, rm.w}, rpv[4] = {rp.x, rp.y, rp.z, rp.w};
+                float out[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float left = (j == 0) ? xl : cur[j - 1];
+                    const float right = (j == 3) ? xr : cur[j + 1];
+                    const float ax = fminf(fminf(left, right), kFarSentinel);
+                    const float ar = fminf(fminf(rmv[j], rpv[j]), kFarSentinel);
+                    const float al = fminf(prev[j], nxt[j]);
+                    const float u = (AXIS == 2) ? godunov_sel<RULE>(ax, ar, al, h)
+                                                : godunov_sel<RULE>(ax, al, ar, h);
+                    out[j] = cur[j];
+                    if (u < cur[j]) {
+                        out[j] = u;
+                        ch = true;
+                    }
+                    prev[j] = out[j];
+                }
+                *reinterpret_cast<float4*>(p) = make_float4(out[0], out[1], out[2], out[3]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) cur[j] = nxt[j];
+            p += sstep;
+        }
+        __syncwarp();
+        if ((tid & 31) == 0) mbar_arrive(&empty[b % kWVS]);
+    }
+    mark_changed(ch, &ds->changed[round]);
+}
+
 // Layout check of the staged tile: one CTA loads the box at (x, y, z) of a grid whose
 // cells hold their own linear index, and every thread compares elements (scalar reads
 // through tsw, vector reads through tvec) with the expected value or NaN outside.
@@ -909,7 +1039,23 @@ void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lat
     if (!wtma) wsched = kWCpAsync;
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
     GBSDF_COUNT_LAUNCH();
-    if (axis != 0 && wsched == kWTmaPipe) {
+    // four lines per thread: 16-byte stores need an aligned destination (rows already are)
+    if (wsched == kWTmaVec && (reinterpret_cast<uintptr_t>(dst) & 15)) wsched = kWTmaPipe;
+    if (axis != 0 && wsched == kWTmaVec) {
+        const int n_rows = (axis == 2) ? dy : dz;
+        dim3 grid((dx + kWX - 1) / kWX, (n_rows + kWR - 1) / kWR);
+        if (axis == 2) {
+            cudaFuncSetAttribute(sweep_walk_vec_kernel<2, RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kWVSmem);
+            sweep_walk_vec_kernel<2, RULE, DIR><<<grid, kWVThreads, kWVSmem, st>>>(src_map->zmap, dst, L, round,
+                                                                                 ds);
+        } else {
+            cudaFuncSetAttribute(sweep_walk_vec_kernel<1, RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kWVSmem);
+            sweep_walk_vec_kernel<1, RULE, DIR><<<grid, kWVThreads, kWVSmem, st>>>(src_map->ymap, dst, L, round,
+                                                                                 ds);
+        }
+    } else if (axis != 0 && wsched == kWTmaPipe) {
         const int n_rows = (axis == 2) ? dy : dz;
         dim3 grid((dx + kWX - 1) / kWX, (n_rows + kWR - 1) / kWR);
         if (axis == 2) {

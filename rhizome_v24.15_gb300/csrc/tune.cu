@@ -1,14 +1,16 @@
 // tune.cu — the sweep-schedule autotuner.
 //
-// The x sweep has three schedules and the y / z walks two, all with identical results
+// The x sweep has three schedules and the y / z walks three, all with identical results
 // (internal header, XSchedule / WSchedule). Which is fastest depends on the lattice (row
-// length, CTAs per wave) and the device, so the first build of a lattice class times each
-// candidate on that build's own buffers -- the band field about to be swept, one warm-up
-// and two timed launches each (x sweeps for the x schedules, z walks for the walk
-// schedules), CUDA events on the build's stream -- and remembers the winners.
-// A class is (device, row pitch a multiple of 16 bytes, round(log2 voxels), round(log2
-// row length)). Timing writes only the destination copy and one change-flag slot, both
-// rewritten by the eikonal stage that follows.
+// length, CTAs per wave), the device and the field: the first round sweeps a band in a far
+// field, where most updates are one-dimensional, later rounds a field where most warps
+// need the 2D and 3D updates. So the first build of a lattice class times each candidate
+// twice on that build's own buffers -- phase 0 on the band field about to be swept, phase 1
+// on the field after the first round -- one warm-up and two timed launches each (x sweeps
+// for the x schedules, z walks for the walk schedules), CUDA events on the build's stream,
+// and remembers the winners per phase. A class is (device, row pitch a multiple of 16
+// bytes, round(log2 voxels), round(log2 row length)). Timing writes only the destination
+// copy, which the next sweep rewrites whole, and one change-flag slot.
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -20,23 +22,23 @@
 namespace gbsdf {
 namespace {
 
-using Key = std::tuple<int, int, int, int>;
+using Key = std::tuple<int, int, int, int, int>;
 std::mutex g_tune_mu;
 std::map<Key, SweepPlan> g_tuned;
 
-Key key_of(int device, const Lattice& L) {
+Key key_of(int device, const Lattice& L, int phase) {
     return Key{device, (L.dims[0] & 3) == 0 ? 1 : 0, (int)std::lround(std::log2((double)L.N)),
-               (int)std::lround(std::log2((double)L.dims[0]))};
+               (int)std::lround(std::log2((double)L.dims[0])), phase};
 }
 
 }  // namespace
 
 SweepPlan tuned_sweep_plan(int device, const Lattice& L, const float* src, float* dst, const GridMap* src_map,
-                           DevState* ds, cudaStream_t st, bool measure) {
+                           DevState* ds, cudaStream_t st, bool measure, int phase) {
     SweepPlan plan{kXCpAsync, kWCpAsync};
     const bool tma = src_map && src_map->valid, wtma = src_map && src_map->walk_valid;
     if (!tma && !wtma) return plan;
-    const Key k = key_of(device, L);
+    const Key k = key_of(device, L, phase);
     {
         std::lock_guard<std::mutex> g(g_tune_mu);
         auto it = g_tuned.find(k);
@@ -80,7 +82,7 @@ SweepPlan tuned_sweep_plan(int device, const Lattice& L, const float* src, float
     }
     if (wtma) {
         float best = 1e30f;
-        for (int cand : {kWCpAsync, kWTmaPipe}) {
+        for (int cand : {kWCpAsync, kWTmaPipe, kWTmaVec}) {
             const float ms = time_it(2, plan.x, cand);
             if (ms >= 0.0f && ms < best) {
                 best = ms;
