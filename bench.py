@@ -182,9 +182,10 @@ def run_batched(gbsdf, torch, dev, mode, steps, warmup, local):
 
 def run_decode(gbsdf, steps):
     """The wire-format decoders on the bench mug (179,840 triangles): binary STL (decode +
-    weld) and OBJ text, through the public API (host bytes in, host arrays out, device
-    allocation per call as in the reference), against the oracle's single-threaded CPU
-    restatement of the reference's decoders. Host wall-clock per call, median of K."""
+    weld), ASCII STL (tokens, numbers, weld) and OBJ text, through the public API (host
+    bytes in, host arrays out, device allocation per call as in the reference), against the
+    oracle's single-threaded CPU restatement of the reference's decoders. Host wall-clock
+    per call, median of K."""
     from gbsdf import meshgen
     from oracle import oracle as O
 
@@ -193,8 +194,10 @@ def run_decode(gbsdf, steps):
     v, f = meshgen.mug(**kw)
     stl = meshgen.to_binary_stl(v, f)
     obj = meshgen.to_obj_text(v, f, fancy=False)
+    astl = meshgen.to_ascii_stl(v, f, fancy=False)
     res = {}
     for name, data, gpu, cpu in (("binary_stl", stl, gbsdf.parse_binary_stl, O.parse_binary_stl),
+                                 ("ascii_stl", astl, gbsdf.parse_ascii_stl, O.parse_ascii_stl),
                                  ("obj", obj, gbsdf.parse_obj, O.parse_obj)):
         gpu(data)  # warm-up (context, module load)
         ts = []

@@ -240,8 +240,8 @@ int gbsdf_mlp_backward(const float* params_dev, const float* features_dev, const
 int gbsdf_mlp_adam(float* params_dev, const float* grad_dev, float* m_dev, float* v_dev, float lr, float beta1,
                    float beta2, float eps, float grad_scale, int32_t step, int32_t device, char* err, size_t errlen);
 
-/* Mesh wire formats. Both decode on the GPU of `device` and
- * write host arrays; vertices are x, y, z floats, indices 3 per triangle.
+/* Mesh wire formats. Each decodes on the GPU of `device` and writes host arrays;
+ * vertices are x, y, z floats, indices 3 per triangle.
  *
  * Replaces CudaRasterizer::parse_binary_stl_gpu (cuda_mesh_io.cu:592-722, record decode
  * :524-590): 80-byte header, uint32 triangle count, 50-byte records. Vertices are welded
@@ -263,6 +263,21 @@ int gbsdf_parse_binary_stl(const uint8_t* bytes, size_t n_bytes, float* out_vert
 int gbsdf_parse_obj(const char* text, size_t n_bytes, float* out_vertices, int64_t vertex_capacity,
                     uint32_t* out_indices, int64_t index_capacity, int64_t* n_vertices, int64_t* n_indices,
                     int32_t device, char* err, size_t errlen);
+
+/* Replaces CudaRasterizer::parse_ascii_stl_gpu (cuda_mesh_io.cu:1201-1325, token finder
+ * :1094-1118, weld :1146-1186), the decoder StlParser::parse (stl_parser.cpp:43-57) runs
+ * when the header's triangle count does not fit the file: "vertex" tokens (at the text
+ * start or after a space, tab, CR or LF, followed by a space or tab) in file order, at
+ * most gbsdf_ascii_stl_capacity(n_bytes) of them, cut to whole facets; three numbers
+ * after each token (the OBJ number rule); corners welded on the reference's 64-bit hash
+ * of round(coordinate * 10000) and every corner kept. Vertices are numbered in order of
+ * first occurrence with the first corner's coordinates (the reference's numbering follows
+ * its threads' timing). out_vertices / out_indices must hold the capacity's count.
+ * GBSDF_EINVAL when the text is shorter than 15 bytes or holds no whole facet. */
+int gbsdf_ascii_stl_capacity(size_t n_bytes, int64_t* vertex_capacity);
+int gbsdf_parse_ascii_stl(const char* text, size_t n_bytes, float* out_vertices, int64_t vertex_capacity,
+                          uint32_t* out_indices, int64_t index_capacity, int64_t* n_vertices, int64_t* n_indices,
+                          int32_t device, char* err, size_t errlen);
 
 /* Replaces CudaRasterizer::orient_mesh_gpu (cuda_mesh_topology.cu:707-842), the pre-pass
  * the reference's OBJ loader runs after decoding: makes the winding of `indices` (host,

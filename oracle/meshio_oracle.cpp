@@ -13,6 +13,16 @@
 //   starting "v " / "f " in file order (at most text_length / 10 + 1024 of each), three
 //   numbers per vertex, up to four 1-based (or negative, relative) indices per face, quads
 //   split (0,1,2) (0,2,3).
+// * ASCII STL: CudaRasterizer::parse_ascii_stl_gpu (cuda_mesh_io.cu:1201-1325) with
+//   gpu_find_ascii_stl_vertices_kernel (:1094-1118), the OBJ number parser and
+//   gpu_weld_raw_vertices_kernel (:1146-1186): "vertex" tokens (at the text start or after
+//   a space, tab, CR or LF, followed by a space or tab, ending before the last 7 bytes) in
+//   file order, at most the reference's offset capacity, the count cut to whole facets;
+//   three numbers after each token; corners welded on the reference's 64-bit hash of
+//   round(coordinate * 10000) (dev_quantize_vec3_key, :1146-1156), every corner kept. The
+//   reference numbers vertices in the order its threads win the table slots and keeps the
+//   winner's coordinates; this restatement numbers them in order of first occurrence and
+//   keeps the first corner's coordinates (the engine does the same).
 // Every expression is restated as written in the reference source, each operation rounded
 // once (compile with -ffp-contract=off; oracle.py does), the same convention as the engine
 // (-fmad=false). A build of the reference that fuses multiply-adds can differ from this by
@@ -235,6 +245,61 @@ int orc_parse_obj(const char* text_in, size_t n, float* verts, uint32_t* idx, in
     if (I == 0) return 1;
     *nv = V;
     *ni = I;
+    return 0;
+}
+
+// Returns 0 on success, 1 when the text is shorter than 15 bytes or holds no whole facet.
+// verts must hold 3 * cap floats and idx cap indices, cap = ascii_stl_capacity(n).
+int64_t orc_ascii_stl_capacity(size_t n) {
+    const size_t max_verts = n / 12 + 1024;
+    size_t cap = 1024;
+    while (cap < max_verts && cap < ((size_t)1 << 26)) cap <<= 1;
+    return (int64_t)cap;
+}
+
+int orc_parse_ascii_stl(const char* text_in, size_t n, float* verts, uint32_t* idx, int64_t* nv, int64_t* ni) {
+    *nv = 0;
+    *ni = 0;
+    if (!text_in || n < 15) return 1;
+    std::vector<char> text(text_in, text_in + n);
+    text.push_back('\0');
+    const size_t cap = (size_t)orc_ascii_stl_capacity(n);
+    std::vector<size_t> vo;
+    for (size_t i = 0; i + 7 < n; ++i) {
+        const bool start = (i == 0) || text[i - 1] == ' ' || text[i - 1] == '\t' || text[i - 1] == '\n' ||
+                           text[i - 1] == '\r';
+        if (!start) continue;
+        if (std::memcmp(text.data() + i, "vertex", 6) == 0 && (text[i + 6] == ' ' || text[i + 6] == '\t')) {
+            if (vo.size() < cap) vo.push_back(i + 6);
+        }
+    }
+    const size_t m = vo.size() - vo.size() % 3;
+    if (m == 0) return 1;
+    std::unordered_map<uint64_t, uint32_t> ids;
+    int64_t V = 0;
+    for (size_t k = 0; k < m; ++k) {
+        const char* p = text.data() + vo[k];
+        const float x = fast_atof(p);
+        const float y = fast_atof(p);
+        const float z = fast_atof(p);
+        // dev_quantize_vec3_key (cuda_mesh_io.cu:1146-1156)
+        const uint64_t ux = (uint64_t)(uint32_t)quant(x), uy = (uint64_t)(uint32_t)quant(y),
+                       uz = (uint64_t)(uint32_t)quant(z);
+        uint64_t key = (ux * 73856093ull) ^ (uy * 19349663ull) ^ (uz * 83492791ull) ^ ((ux & 0xFFFFFull) << 42) ^
+                       ((uy & 0xFFFFFull) << 21) ^ (uz & 0x1FFFFFull);
+        if (key == 0) key = 1;
+        auto it = ids.find(key);
+        if (it == ids.end()) {
+            it = ids.emplace(key, (uint32_t)V).first;
+            verts[3 * V] = x;
+            verts[3 * V + 1] = y;
+            verts[3 * V + 2] = z;
+            ++V;
+        }
+        idx[k] = it->second;
+    }
+    *nv = V;
+    *ni = (int64_t)m;
     return 0;
 }
 

@@ -288,6 +288,21 @@ def parse_obj(text: bytes):
     return st, verts[:nv.value], idx[:ni.value]
 
 
+def parse_ascii_stl(text: bytes):
+    """ASCII STL decode (cuda_mesh_io.cu:1094-1325). Returns (status, vertices (V,3), indices (I,))."""
+    n = len(text)
+    L = lib()
+    L.orc_ascii_stl_capacity.restype = C.c_int64
+    cap = int(L.orc_ascii_stl_capacity(C.c_size_t(n)))
+    buf = np.frombuffer(text, np.uint8) if n else np.zeros(1, np.uint8)
+    verts = np.zeros((cap, 3), np.float32)
+    idx = np.zeros(cap, np.uint32)
+    nv, ni = C.c_int64(0), C.c_int64(0)
+    L.orc_parse_ascii_stl.restype = C.c_int
+    st = L.orc_parse_ascii_stl(_p(buf), C.c_size_t(n), _p(verts), _p(idx), C.byref(nv), C.byref(ni))
+    return st, verts[:nv.value], idx[:ni.value]
+
+
 def orient_mesh(vertices, indices):
     """Orientation pre-pass (cuda_mesh_topology.cu:707-842). Returns (indices oriented,
     orientable, had_inconsistent_winding, was_inverted, signed volume)."""

@@ -17,6 +17,12 @@
 //   3. first flags (corner == its key's smallest corner), an exclusive scan numbers the
 //      first corners in file order, every corner takes its first corner's number;
 //   4. a scan over the kept triangles compacts the index list in order.
+// ASCII STL (CudaRasterizer::parse_ascii_stl_gpu, cuda_mesh_io.cu:1201-1325): the reference
+// collects "vertex" token offsets with atomics and bitonic-sorts them, then welds on the
+// GPU with slots claimed in thread order, so its vertex numbering varies from run to run.
+// Here a scan over per-byte token flags gives the file order, the corners go through the
+// same order-independent weld as binary STL, keyed on the reference's 64-bit hash of the
+// quantised coordinates, and vertices are numbered in order of first occurrence.
 // OBJ: the reference finds "v " / "f " line starts with atomics and sorts the offsets on
 // the host; here a scan over per-byte flags gives the file order directly. Faces are
 // counted (0, 1 or 2 triangles), scanned and written in file order (the reference's
@@ -53,6 +59,16 @@ __device__ __forceinline__ uint32_t key_hash(int3 k) {
 }
 
 __device__ __forceinline__ bool key_eq(int3 a, int3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+
+__device__ __forceinline__ uint32_t key_hash(unsigned long long k) {
+    uint64_t h = k * 0x9E3779B97F4A7C15ull;
+    h ^= h >> 29;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 32;
+    return (uint32_t)h;
+}
+
+__device__ __forceinline__ bool key_eq(unsigned long long a, unsigned long long b) { return a == b; }
 
 // 1. decode (gpu_decode_binary_stl_kernel, cuda_mesh_io.cu:524-590)
 __global__ void stl_decode_kernel(const uint8_t* __restrict__ payload, long long T, float* __restrict__ raw,
@@ -102,11 +118,12 @@ __global__ void stl_decode_kernel(const uint8_t* __restrict__ payload, long long
 }
 
 // 2. insert every corner; equal keys keep their smallest corner index
-__global__ void weld_insert_kernel(const int3* __restrict__ keys, long long n, uint32_t* __restrict__ table,
+template <class K>
+__global__ void weld_insert_kernel(const K* __restrict__ keys, long long n, uint32_t* __restrict__ table,
                                    uint32_t mask) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int3 k = keys[i];
+    const K k = keys[i];
     uint32_t h = key_hash(k) & mask;
     for (uint32_t probe = 0; probe <= mask; ++probe) {
         uint32_t cur = table[h];
@@ -124,11 +141,12 @@ __global__ void weld_insert_kernel(const int3* __restrict__ keys, long long n, u
 }
 
 // 3a. first-occurrence flags and each corner's first corner
-__global__ void weld_first_kernel(const int3* __restrict__ keys, long long n, const uint32_t* __restrict__ table,
+template <class K>
+__global__ void weld_first_kernel(const K* __restrict__ keys, long long n, const uint32_t* __restrict__ table,
                                   uint32_t mask, unsigned* __restrict__ first, uint32_t* __restrict__ rep) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int3 k = keys[i];
+    const K k = keys[i];
     uint32_t h = key_hash(k) & mask;
     uint32_t r = (uint32_t)i;
     for (uint32_t probe = 0; probe <= mask; ++probe) {
@@ -347,6 +365,43 @@ struct Scratch {
     }
 };
 
+// ---- ASCII STL ----------------------------------------------------------------------
+// "vertex" token flags (gpu_find_ascii_stl_vertices_kernel, cuda_mesh_io.cu:1094-1118): at
+// the text start or after a space, tab, CR or LF, followed by a space or tab, and starting
+// before the last 7 bytes.
+__global__ void stla_flags_kernel(const char* __restrict__ text, long long n, unsigned* __restrict__ fl) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned f = 0;
+    if (i + 7 < n) {
+        const char b = (i == 0) ? ' ' : text[i - 1];
+        const bool start = b == ' ' || b == '\t' || b == '\n' || b == '\r';
+        f = start && text[i] == 'v' && text[i + 1] == 'e' && text[i + 2] == 'r' && text[i + 3] == 't' &&
+            text[i + 4] == 'e' && text[i + 5] == 'x' && (text[i + 6] == ' ' || text[i + 6] == '\t');
+    }
+    fl[i] = f;
+}
+
+__global__ void stla_offsets_kernel(long long n, const unsigned* __restrict__ fl,
+                                    const unsigned long long* __restrict__ pos, long long cap,
+                                    long long* __restrict__ vo) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (fl[i] && (long long)pos[i] < cap) vo[pos[i]] = i + 6;
+}
+
+// the reference's weld key (dev_quantize_vec3_key, cuda_mesh_io.cu:1146-1156): a 64-bit
+// mix of the round(coordinate * 10000) integers; corners with equal keys are one vertex
+__global__ void stla_keys_kernel(const float* __restrict__ raw, long long n, unsigned long long* __restrict__ keys) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long ux = (uint32_t)quant(raw[3 * i]), uy = (uint32_t)quant(raw[3 * i + 1]),
+                             uz = (uint32_t)quant(raw[3 * i + 2]);
+    unsigned long long h = (ux * 73856093ull) ^ (uy * 19349663ull) ^ (uz * 83492791ull) ^ ((ux & 0xFFFFFull) << 42) ^
+                           ((uy & 0xFFFFFull) << 21) ^ (uz & 0x1FFFFFull);
+    keys[i] = h ? h : 1ull;
+}
+
 unsigned blocks_for(long long n, int threads = 256) { return (unsigned)((n + threads - 1) / threads); }
 
 int set_device(int32_t device, IErr& e) {
@@ -419,9 +474,9 @@ int gbsdf_parse_binary_stl(const uint8_t* bytes, size_t n_bytes, float* out_vert
     GBSDF_COUNT_LAUNCH();
     stl_decode_kernel<<<blocks_for(T), 256, 0, st>>>(d_payload, T, d_raw, d_norm, d_keys);
     GBSDF_COUNT_LAUNCH();
-    weld_insert_kernel<<<blocks_for(n), 256, 0, st>>>(d_keys, n, d_table, cap - 1);
+    weld_insert_kernel<int3><<<blocks_for(n), 256, 0, st>>>(d_keys, n, d_table, cap - 1);
     GBSDF_COUNT_LAUNCH();
-    weld_first_kernel<<<blocks_for(n), 256, 0, st>>>(d_keys, n, d_table, cap - 1, d_first, d_rep);
+    weld_first_kernel<int3><<<blocks_for(n), 256, 0, st>>>(d_keys, n, d_table, cap - 1, d_first, d_rep);
     launch_exclusive_scan(d_first, d_fpos, n, d_scan, 0, st);
     GBSDF_COUNT_LAUNCH();
     weld_assign_kernel<<<blocks_for(n), 256, 0, st>>>(d_raw, n, d_rep, d_fpos, d_vid, d_outv);
@@ -534,6 +589,102 @@ int gbsdf_parse_obj(const char* text, size_t n_bytes, float* out_vertices, int64
     if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "OBJ download: %s", cudaGetErrorString(ce));
     *n_vertices = V;
     *n_indices = 3 * NT;
+    return GBSDF_OK;
+}
+
+int gbsdf_ascii_stl_capacity(size_t n_bytes, int64_t* vertex_capacity) {
+    if (!vertex_capacity) return GBSDF_EINVAL;
+    const size_t max_verts = n_bytes / 12 + 1024;
+    size_t cap = 1024;
+    while (cap < max_verts && cap < ((size_t)1 << 26)) cap <<= 1;
+    *vertex_capacity = (int64_t)cap;
+    return GBSDF_OK;
+}
+
+int gbsdf_parse_ascii_stl(const char* text, size_t n_bytes, float* out_vertices, int64_t vertex_capacity,
+                          uint32_t* out_indices, int64_t index_capacity, int64_t* n_vertices, int64_t* n_indices,
+                          int32_t device, char* err, size_t errlen) {
+    IErr e{err, errlen};
+    if (err && errlen) err[0] = 0;
+    if (!n_vertices || !n_indices) return e.set(GBSDF_EINVAL, "null count pointers");
+    *n_vertices = 0;
+    *n_indices = 0;
+    if (!text || n_bytes < 15) return e.set(GBSDF_EINVAL, "ASCII STL text shorter than 15 bytes");
+    int64_t cap = 0;
+    gbsdf_ascii_stl_capacity(n_bytes, &cap);
+    int rc = set_device(device, e);
+    if (rc != GBSDF_OK) return rc;
+    const long long n = (long long)n_bytes;
+    cudaError_t ce = cudaSuccess;
+    Scratch s;
+    char* d_text = s.get<char>((size_t)n + 1, ce);
+    unsigned* d_fl = s.get<unsigned>((size_t)n, ce);
+    unsigned long long* d_pos = s.get<unsigned long long>((size_t)n + 1, ce);
+    long long* d_vo = s.get<long long>((size_t)cap, ce);
+    unsigned long long* d_scan = s.get<unsigned long long>((size_t)scan_tmp_elems(n), ce);
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        return e.set(GBSDF_ENOMEM, "device allocation failed: %s", cudaGetErrorString(ce));
+    }
+    cudaStream_t st = 0;
+    cudaMemcpyAsync(d_text, text, (size_t)n, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(d_text + n, 0, 1, st);
+    GBSDF_COUNT_LAUNCH();
+    stla_flags_kernel<<<blocks_for(n), 256, 0, st>>>(d_text, n, d_fl);
+    launch_exclusive_scan(d_fl, d_pos, n, d_scan, 0, st);
+    GBSDF_COUNT_LAUNCH();
+    stla_offsets_kernel<<<blocks_for(n), 256, 0, st>>>(n, d_fl, d_pos, cap, d_vo);
+    unsigned long long pl = 0;
+    unsigned fl = 0;
+    cudaMemcpyAsync(&pl, d_pos + (n - 1), 8, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&fl, d_fl + (n - 1), 4, cudaMemcpyDeviceToHost, st);
+    ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "ASCII STL scan: %s", cudaGetErrorString(ce));
+    const long long tokens = std::min<long long>((long long)pl + fl, cap);
+    const long long m = tokens - tokens % 3;  // whole facets
+    if (m == 0) return e.set(GBSDF_EINVAL, "ASCII STL text holds no whole facet");
+    if (vertex_capacity < m || index_capacity < m || !out_vertices || !out_indices)
+        return e.set(GBSDF_EINVAL, "outputs must hold %lld vertices and indices", m);
+    uint32_t tcap = 1024;
+    while ((long long)tcap < 2 * m) tcap <<= 1;
+    float* d_raw = s.get<float>((size_t)m * 3, ce);
+    unsigned long long* d_keys = s.get<unsigned long long>((size_t)m, ce);
+    uint32_t* d_table = s.get<uint32_t>(tcap, ce);
+    unsigned* d_first = s.get<unsigned>((size_t)m, ce);
+    uint32_t* d_rep = s.get<uint32_t>((size_t)m, ce);
+    unsigned long long* d_fpos = s.get<unsigned long long>((size_t)m + 1, ce);
+    uint32_t* d_vid = s.get<uint32_t>((size_t)m, ce);
+    float* d_outv = s.get<float>((size_t)m * 3, ce);
+    unsigned long long* d_scan2 = s.get<unsigned long long>((size_t)scan_tmp_elems(m), ce);
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        return e.set(GBSDF_ENOMEM, "device allocation failed: %s", cudaGetErrorString(ce));
+    }
+    cudaMemsetAsync(d_table, 0xff, (size_t)tcap * 4, st);
+    GBSDF_COUNT_LAUNCH();
+    obj_vertices_kernel<<<blocks_for(m), 256, 0, st>>>(d_text, d_vo, m, d_raw);
+    GBSDF_COUNT_LAUNCH();
+    stla_keys_kernel<<<blocks_for(m), 256, 0, st>>>(d_raw, m, d_keys);
+    GBSDF_COUNT_LAUNCH();
+    weld_insert_kernel<unsigned long long><<<blocks_for(m), 256, 0, st>>>(d_keys, m, d_table, tcap - 1);
+    GBSDF_COUNT_LAUNCH();
+    weld_first_kernel<unsigned long long><<<blocks_for(m), 256, 0, st>>>(d_keys, m, d_table, tcap - 1, d_first,
+                                                                         d_rep);
+    launch_exclusive_scan(d_first, d_fpos, m, d_scan2, 0, st);
+    GBSDF_COUNT_LAUNCH();
+    weld_assign_kernel<<<blocks_for(m), 256, 0, st>>>(d_raw, m, d_rep, d_fpos, d_vid, d_outv);
+    unsigned long long vl = 0;
+    unsigned vlast = 0;
+    cudaMemcpyAsync(&vl, d_fpos + (m - 1), 8, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&vlast, d_first + (m - 1), 4, cudaMemcpyDeviceToHost, st);
+    ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "ASCII STL weld: %s", cudaGetErrorString(ce));
+    const long long V = (long long)vl + vlast;
+    ce = cudaMemcpy(out_vertices, d_outv, (size_t)V * 12, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(out_indices, d_vid, (size_t)m * 4, cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "ASCII STL download: %s", cudaGetErrorString(ce));
+    *n_vertices = V;
+    *n_indices = m;
     return GBSDF_OK;
 }
 

@@ -59,7 +59,7 @@ EXPORTS = ("gbsdf_default_options", "gbsdf_compute_mesh_sdf", "gbsdf_compute_mes
            "gbsdf_mesh_lattice", "gbsdf_build_from_mesh",
            "gbsdf_brick_features", "gbsdf_mlp_forward", "gbsdf_mlp_backward", "gbsdf_mlp_adam",
            "gbsdf_batch_create", "gbsdf_batch_run", "gbsdf_batch_destroy", "gbsdf_parse_binary_stl", "gbsdf_parse_obj",
-           "gbsdf_orient_mesh",
+           "gbsdf_ascii_stl_capacity", "gbsdf_parse_ascii_stl", "gbsdf_orient_mesh",
            "gbsdf_release_workspace", "gbsdf_legacy_sdf_noalloc", "gbsdf_selftest", "gbsdf_version")
 
 _lib = None
@@ -115,6 +115,11 @@ def load(path: Path | None = None):
     L.gbsdf_parse_obj.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, i64p, i64p,
                                   C.c_int32, C.c_char_p, C.c_size_t]
     L.gbsdf_parse_obj.restype = C.c_int
+    L.gbsdf_ascii_stl_capacity.argtypes = [C.c_size_t, i64p]
+    L.gbsdf_ascii_stl_capacity.restype = C.c_int
+    L.gbsdf_parse_ascii_stl.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, i64p,
+                                        i64p, C.c_int32, C.c_char_p, C.c_size_t]
+    L.gbsdf_parse_ascii_stl.restype = C.c_int
     L.gbsdf_orient_mesh.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, i32p, i32p, i32p,
                                     C.POINTER(C.c_double), C.c_int32, C.c_char_p, C.c_size_t]
     L.gbsdf_orient_mesh.restype = C.c_int

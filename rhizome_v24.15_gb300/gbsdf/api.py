@@ -295,6 +295,44 @@ def parse_obj(text: bytes, device=0):
     return verts[:nv.value], idx[:ni.value]
 
 
+def parse_ascii_stl(text: bytes, device=0):
+    """GPU decode + weld of ASCII STL text (gbsdf_parse_ascii_stl). Returns (vertices (V,3)
+    float32, indices (I,) uint32)."""
+    data = bytes(text)
+    L = _lib.load()
+    cap = C.c_int64(0)
+    L.gbsdf_ascii_stl_capacity(C.c_size_t(len(data)), C.byref(cap))
+    b = np.frombuffer(data, np.uint8) if data else np.zeros(1, np.uint8)
+    verts = np.empty((cap.value, 3), np.float32)
+    idx = np.empty(cap.value, np.uint32)
+    nv, ni = C.c_int64(0), C.c_int64(0)
+    err = C.create_string_buffer(512)
+    rc = L.gbsdf_parse_ascii_stl(b.ctypes.data, len(data), verts.ctypes.data, cap.value, idx.ctypes.data, cap.value,
+                                 C.byref(nv), C.byref(ni), int(device), err, len(err))
+    if rc != _lib.OK:
+        raise GbsdfError(rc, err.value.decode(errors="replace"))
+    return verts[:nv.value], idx[:ni.value]
+
+
+def parse_stl(data: bytes, device=0):
+    """StlParser::parse (stl_parser.cpp:9-66): a file of at least 84 bytes whose header
+    count T > 0 fits (84 + 50 T bytes) is binary, anything else ASCII; decoded on the GPU,
+    then oriented (orient_mesh). Returns (vertices, indices, orientable); raises GbsdfError
+    where the reference returns false (too small, undecodable, no triangle)."""
+    data = bytes(data)
+    if len(data) < 84:
+        raise GbsdfError(_lib.EINVAL, "STL file too small to be valid")
+    T = int(np.frombuffer(data[80:84], np.uint32)[0])
+    if T > 0 and len(data) >= 84 + 50 * T:
+        verts, idx = parse_binary_stl(data, device=device)
+    else:
+        verts, idx = parse_ascii_stl(data, device=device)
+    if len(idx) == 0:
+        raise GbsdfError(_lib.EINVAL, "STL contains no valid non-degenerate triangles")
+    idx, orientable, _, _, _ = orient_mesh(verts, idx, device=device)
+    return verts, idx, orientable
+
+
 def orient_mesh(vertices, indices, device=0):
     """GPU orientation pre-pass (gbsdf_orient_mesh). Returns (indices oriented (I,) uint32,
     orientable, had_inconsistent_winding, was_inverted, signed volume)."""

@@ -40,6 +40,7 @@ __all__ = [
     "to_triangles",
     "workload",
     "batch_workload",
+    "to_ascii_stl",
     "to_binary_stl",
     "to_obj_text",
     "WORKLOADS",
@@ -446,6 +447,33 @@ def to_binary_stl(verts, faces, normals=None, header: bytes = b"gbsdf binary STL
     rec["n"] = np.asarray(normals, np.float32)
     rec["v"] = tri
     return header[:80].ljust(80, b" ") + np.uint32(len(f)).tobytes() + rec.tobytes()
+
+
+def to_ascii_stl(verts, faces, seed: int = 0, fancy: bool = True) -> bytes:
+    """ASCII STL text of an indexed mesh (solid / facet normal / outer loop / vertex lines).
+    With ``fancy`` the writer varies the spellings the decoder must accept: indentation by
+    spaces or tabs, tabs between numbers, CRLF line ends, signs and exponents."""
+    rng = np.random.default_rng(seed)
+    v = np.asarray(verts, np.float32)
+    f = np.asarray(faces, np.int64).reshape(-1, 3)
+    tri = v[f]
+    nrm = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    out = ["solid gbsdf\n"]
+    for t in range(len(f)):
+        eol = "\r\n" if fancy and rng.random() < 0.1 else "\n"
+        out.append("  facet normal %.6e %.6e %.6e%s    outer loop%s" % (nrm[t, 0], nrm[t, 1], nrm[t, 2], eol, eol))
+        for k in range(3):
+            p = tri[t, k]
+            r = rng.random() if fancy else 1.0
+            if r < 0.1:
+                out.append("\tvertex\t%+.6e\t%.7g %.9g%s" % (p[0], p[1], p[2], eol))
+            elif r < 0.2:
+                out.append("      vertex %.8e %.8e %.8e%s" % (p[0], p[1], p[2], eol))
+            else:
+                out.append("      vertex %.6f %.6f %.6f%s" % (p[0], p[1], p[2], eol))
+        out.append("    endloop%s  endfacet%s" % (eol, eol))
+    out.append("endsolid gbsdf\n")
+    return "".join(out).encode()
 
 
 def to_obj_text(verts, faces, seed: int = 0, fancy: bool = True) -> bytes:

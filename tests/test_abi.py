@@ -50,6 +50,10 @@ def test_library_loads_and_binds(lib_path):
     for n in declared_functions():
         assert hasattr(L, n)
     assert set(_lib.EXPORTS) <= set(declared_functions())
+    # every bound entry point has its C signature (ctypes would pass 64-bit pointers and
+    # sizes as 32-bit ints otherwise)
+    unbound = [n for n in _lib.EXPORTS if getattr(L, n).argtypes is None]
+    assert not unbound, unbound
     assert b"sm_103a" in L.gbsdf_version()
 
 

@@ -112,3 +112,45 @@ def test_orientation_large_component(engine, oracle):
     gi, go, gc, gw, gv = engine.orient_mesh(v.astype(np.float32), g)
     assert go and gc and gv > 0
     assert np.array_equal(gi.reshape(-1, 3), f)
+
+
+def test_ascii_stl_matches_oracle(engine, oracle):
+    """ASCII STL: token finding, numbers and the 64-bit-key weld against the oracle (numbers
+    written with exponents within one ulp: powf on both sides), on the oracle's edge cases
+    and a ~160k-triangle sphere."""
+    from gbsdf import meshgen
+    from test_meshio_oracle import ascii_stl_cases
+
+    v3, f3 = meshgen.perturbed_sphere(seed=3, n_lat=200, n_lon=400)
+    cases = list(ascii_stl_cases()) + [meshgen.to_ascii_stl(v3, f3, seed=4)]
+    for k, text in enumerate(cases):
+        gv, gi = engine.parse_ascii_stl(text)
+        st, ov, oi = oracle.parse_ascii_stl(text)
+        assert st == 0
+        assert np.array_equal(gi, oi), k
+        assert _ulps(gv, ov).max() <= (0 if k == 0 else 1), k
+    with pytest.raises(engine.GbsdfError):
+        engine.parse_ascii_stl(b"vertex 1 2 3")
+    with pytest.raises(engine.GbsdfError):
+        engine.parse_ascii_stl(b"solid x\nvertex 1 2 3\nvertex 4 5 6\nendsolid x\n")
+
+
+def test_parse_stl_front_end(engine):
+    """StlParser::parse: binary when the header count fits the file, else ASCII; both
+    oriented; the two encodings of one mesh give the same triangles."""
+    from gbsdf import meshgen
+
+    v, f = meshgen.mug(segments=64, n_bottom=3, n_wall=6, n_rim=1, handle_path=16, handle_around=12)
+    v = v.astype(np.float32)
+    rng = np.random.default_rng(7)
+    g = f.copy()
+    fl = rng.random(len(g)) < 0.3
+    g[fl] = g[fl][:, [0, 2, 1]]  # scrambled winding: the front end orients it back
+    bv, bi, bo = engine.parse_stl(meshgen.to_binary_stl(v, g))
+    av, ai, ao = engine.parse_stl(meshgen.to_ascii_stl(v, g, fancy=False))
+    assert bo and ao
+    assert np.array_equal(bi, ai)  # same welding and orientation
+    assert np.allclose(bv, av, rtol=0, atol=2e-5)
+    assert np.array_equal(bv[bi.reshape(-1, 3)], v[f])  # the source's outward winding restored
+    with pytest.raises(engine.GbsdfError):
+        engine.parse_stl(b"solid tiny\n")

@@ -137,3 +137,119 @@ def test_orientation_oracle():
             assert inverted and not inconsistent
         if name == "mobius":
             assert not orientable and inconsistent
+
+
+# ---- ASCII STL ----------------------------------------------------------------------
+F32 = np.float32
+
+
+def _atof(b, p):
+    """device_fast_atof (cuda_mesh_io.cu:810-843) in float32 steps, each rounded once."""
+    while b[p] in (32, 9):
+        p += 1
+    sign = F32(1)
+    if b[p] == 45:
+        sign, p = F32(-1), p + 1
+    elif b[p] == 43:
+        p += 1
+    val = F32(0)
+    while 48 <= b[p] <= 57:
+        val = F32(F32(val * F32(10)) + F32(b[p] - 48))
+        p += 1
+    if b[p] == 46:
+        p += 1
+        factor = F32(0.1)
+        while 48 <= b[p] <= 57:
+            val = F32(val + F32(F32(b[p] - 48) * factor))
+            factor = F32(factor * F32(0.1))
+            p += 1
+    if b[p] in (101, 69):
+        p += 1
+        es = F32(1)
+        if b[p] == 45:
+            es, p = F32(-1), p + 1
+        elif b[p] == 43:
+            p += 1
+        ev = 0
+        while 48 <= b[p] <= 57:
+            ev = ev * 10 + (b[p] - 48)
+            p += 1
+        val = F32(val * F32(10.0 ** float(F32(es * F32(ev)))))
+    return F32(sign * val), p
+
+
+def _ascii_stl_python(text):
+    """The reference's ASCII STL rules as a plain Python program (tokens, numbers, 64-bit
+    weld key, first-occurrence numbering)."""
+    n = len(text)
+    if n < 15:
+        return None
+    b = text + b"\0"
+    cap = 1024
+    while cap < n // 12 + 1024 and cap < (1 << 26):
+        cap <<= 1
+    offs = []
+    i = text.find(b"vertex")
+    while i != -1:
+        if i + 7 < n and (i == 0 or b[i - 1] in b" \t\n\r") and b[i + 6] in b" \t" and len(offs) < cap:
+            offs.append(i + 6)
+        i = text.find(b"vertex", i + 1)
+    m = len(offs) - len(offs) % 3
+    if m == 0:
+        return None
+    raw = np.zeros((m, 3), np.float32)
+    for k in range(m):
+        p = offs[k]
+        for c in range(3):
+            raw[k, c], p = _atof(b, p)
+    x = (raw * F32(10000.0)).astype(np.float64)
+    q = (np.sign(x) * np.floor(np.abs(x) + 0.5)).astype(np.int64).astype(np.int32)
+    u = q.view(np.uint32).astype(np.uint64)
+    with np.errstate(over="ignore"):
+        key = ((u[:, 0] * np.uint64(73856093)) ^ (u[:, 1] * np.uint64(19349663)) ^ (u[:, 2] * np.uint64(83492791)) ^
+               ((u[:, 0] & np.uint64(0xFFFFF)) << np.uint64(42)) ^ ((u[:, 1] & np.uint64(0xFFFFF)) << np.uint64(21)) ^
+               (u[:, 2] & np.uint64(0x1FFFFF)))
+    key[key == 0] = 1
+    ids, verts, idx = {}, [], []
+    for k in range(m):
+        kk = int(key[k])
+        if kk not in ids:
+            ids[kk] = len(verts)
+            verts.append(raw[k])
+        idx.append(ids[kk])
+    return np.array(verts, np.float32).reshape(-1, 3), np.array(idx, np.uint32)
+
+
+def ascii_stl_cases():
+    from gbsdf import meshgen
+
+    v, f = meshgen.mug(segments=24, n_bottom=2, n_wall=3, n_rim=1, handle_path=8, handle_around=6)
+    yield meshgen.to_ascii_stl(v, f, fancy=False)
+    yield meshgen.to_ascii_stl(v, f, seed=1)
+    # near-duplicates inside one quantisation step (merged, first coordinates kept) and across one
+    v2 = np.concatenate([v, v[:20] + F32(2e-5), v[:20] + F32(3e-4)])
+    f2 = np.concatenate([f, f[:12] % 20 + len(v), f[:12] % 20 + len(v) + 20])
+    yield meshgen.to_ascii_stl(v2, f2, seed=2)
+    # token edge cases: a token at the text start, "endvertex" / "vertexx" / "xvertex" (not
+    # tokens), tab after the keyword, a dangling eighth corner (cut to whole facets), and a
+    # token in the last 7 bytes (ignored)
+    yield (b"vertex 1 2 3\nvertex\t4 5 6 endvertex 7 7 7\n vertexx 9 9 9 xvertex 8 8 8\r\nvertex -1e1 .5 +2\n"
+           b"\tvertex 1 2 3\n vertex 0 0 0\nvertex 3 2 1\nvertex 5 5 5\nvertex 6")
+
+
+def test_ascii_stl_oracle_matches_python_restatement():
+    for text in ascii_stl_cases():
+        st, ov, oi = O.parse_ascii_stl(text)
+        want = _ascii_stl_python(text)
+        assert st == 0 and want is not None
+        assert np.array_equal(ov.view(np.uint32), want[0].view(np.uint32))
+        assert np.array_equal(oi, want[1])
+    st, ov, oi = O.parse_ascii_stl(next(iter(ascii_stl_cases())))
+    from gbsdf import meshgen
+
+    v, f = meshgen.mug(segments=24, n_bottom=2, n_wall=3, n_rim=1, handle_path=8, handle_around=6)
+    # every corner kept, one vertex per source vertex, positions as written (6 decimals)
+    assert len(ov) == len(v) and len(oi) == 3 * len(f)
+    assert np.allclose(ov[oi].reshape(-1, 3, 3), v.astype(np.float32)[f], rtol=0, atol=2e-5)
+    assert O.parse_ascii_stl(b"vertex 1 2 3")[0] == 1  # shorter than 15 bytes
+    assert O.parse_ascii_stl(b"solid x\nvertex 1 2 3\nvertex 4 5 6\nendsolid x\n")[0] == 1  # no whole facet
