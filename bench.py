@@ -276,6 +276,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-mode pass (profiling runs)")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-mesh batched workload")
+    ap.add_argument("--sweep-schedule", type=int, default=0,
+                    help="force the eikonal sweep schedules, x + 10 w (profiling runs; 0 = autotuned)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -319,7 +321,7 @@ def main():
 
     def step_device(m=mode):
         _, res = gbsdf.compute_mesh_sdf(tris_dev, h, mn, mx, out=out_dev, mode=m, path=gbsdf.PATH_FAST,
-                                        device=local, mlp_params=mlp)
+                                        device=local, mlp_params=mlp, sweep_schedule=args.sweep_schedule)
         return res
 
     def barrier():
@@ -408,10 +410,12 @@ def main():
                        "l2": "inputs larger than L2 (2.6 GB grid per step)"},
             "e2e": None if e2e is None else {"value": e2e, "unit": UNIT, "ms_per_step": e2e_ms,
                                              "h2d_bytes_per_step": int(T * 48), "d2h_bytes_per_step": int(N * 4)},
-            "roofline": {"kernel": "eikonal directional sweep (sweep_x_pipe / sweep_walk_pipe, autotuned)", "bound": "hbm", "achieved": achieved,
-                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes,
-                         "launch_ms": per_launch_ms},
+            "roofline": {"kernel": "eikonal directional sweep (sweep_x_pipe / sweep_walk_vec, autotuned)",
+                         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "alg_bytes_per_launch": alg_bytes, "launch_ms": per_launch_ms,
+                         "note": "issue-bound below the HBM roof: 66-81 instructions per voxel at 70-77% "
+                                 "issue-active (profiles/sweeps_vec_mug_600x608x608.md)"},
             "stages_ms": {k: round(float(np.mean([s[k] for s in stats])), 3)
                           for k in ("ms_prep", "ms_splat", "ms_parity", "ms_fixup", "ms_eikonal", "ms_verify",
                                     "ms_apply")},
