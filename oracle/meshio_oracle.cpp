@@ -1,6 +1,6 @@
 // meshio_oracle.cpp — TEST INFRASTRUCTURE ONLY: CPU restatement of the reference's mesh
-// decoders (native/src/engine/io/cuda_mesh_io.cu), the checker of the engine's GPU
-// decoders (rhizome_v24.15_gb300/csrc/k_io.cu). Never linked into the product.
+// decoders (native/src/engine/io/cuda_mesh_io.cu); the tests compare the engine's GPU
+// decoders (rhizome_v24.15_gb300/csrc/k_io.cu) with it. Never linked into the product.
 //
 // * binary STL: CudaRasterizer::parse_binary_stl_gpu (cuda_mesh_io.cu:592-722) with the
 //   record decode of gpu_decode_binary_stl_kernel (:524-590): 80-byte header, uint32

@@ -1,6 +1,6 @@
 """Generate golden vectors for the geometry primitives from the reference's OWN code.
 
-Runs only where the reference tree exists (this builder container): it compiles
+Runs only where the reference tree exists: it compiles
 native/src/core/math_utils.cuh (point_triangle_distance_sq, MATH:43-106;
 triangle_solid_angle, MATH:109-132) with a glm stand-in into oracle/_ref (see
 oracle/build_ref.sh), evaluates both primitives on seeded inputs that cover every

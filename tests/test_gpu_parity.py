@@ -1,6 +1,6 @@
 """GPU parity: the CUDA engine through its C ABI against the CPU oracle.
 
-Tolerances (the benchmark spec): signs bit-exact; band distances (|d| <= 8h) within 1e-5
+Tolerances: signs bit-exact; band distances (|d| <= 8h) within 1e-5
 voxel; far field within 1e-4 voxel. In reference mode the engine and the oracle run
 the same arithmetic in the same (lockstep) schedule, so the grids are expected to be
 bit-identical; the tests assert the tolerances and report the bit-exact fraction.
