@@ -216,6 +216,33 @@ def run_decode(gbsdf, steps):
     return res
 
 
+def run_iso(gbsdf, out_dev, dims, h, mn, steps):
+    """The device-resident hand-off: marching cubes of the build's SDF read in place on the
+    device (gbsdf_extract_iso_surface with a device grid, mesh left on the device), against
+    the reference's route -- the grid taken to the host and uploaded again by the extractor
+    (cuda_marching_cubes.cu:864-866) -- with the mesh returned to the host. Host wall-clock
+    per call (both calls: count query, then emit), median of K."""
+    import torch
+
+    origin = mn.astype(np.float32) * np.float32(h)
+    host = out_dev.cpu().numpy()
+    res = {}
+    for name, fn in (("device_grid", lambda: gbsdf.extract_iso_surface(out_dev, dims, h, origin, 0.0,
+                                                                        outputs_on_device=True)),
+                     ("host_grid", lambda: gbsdf.extract_iso_surface(host, dims, h, origin, 0.0))):
+        fn()
+        ts = []
+        for _ in range(max(3, steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            v, i = fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        res[name] = {"ms": float(np.median(ts)) * 1e3, "vertices": int(len(v)), "triangles": int(len(i) // 3)}
+    res["grid_gvox_s"] = float(np.prod(dims)) / (res["device_grid"]["ms"] * 1e-3) / 1e9
+    return res
+
+
 def cpu_baseline(tris, mn, mx, h, z_slab=64, threads=None):
     """The oracle's restatement of the reference path (CPU), bounded to a z-slab of
     the lattice through the middle of the mug. Returns (Gvox/s, seconds, sample desc)."""
@@ -429,6 +456,7 @@ def main():
         line["pipeline"]["proposed_bricks"] = s0["proposed"]
     if rank == 0 and not args.no_batch:
         line["decode"] = run_decode(gbsdf, args.steps)
+        line["iso_surface"] = run_iso(gbsdf, out_dev, dims, h, mn, args.steps)
     if not args.no_batch and mode in (gbsdf.MODE_REFERENCE, gbsdf.MODE_EXACT_SIGNS):
         line["batched"] = run_batched(gbsdf, torch, dev, mode, args.steps, args.warmup, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

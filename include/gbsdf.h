@@ -291,8 +291,38 @@ int gbsdf_orient_mesh(const float* vertices, int64_t n_vertices, uint32_t* indic
                       int32_t* is_orientable, int32_t* had_inconsistent_winding, int32_t* was_inverted,
                       double* signed_volume, int32_t device, char* err, size_t errlen);
 
-/* Releases the cached device workspace of `device` (buffers are otherwise reused
- * across calls on the same device). */
+/* Iso-surface of a grid (marching cubes), the consumer of a device-resident SDF.
+ * Replaces CudaRasterizer::extract_iso_surface (cuda_marching_cubes.cu:829-951): the
+ * reference uploads a host grid; here `grid` may also be a device pointer
+ * (grid_on_device = 1, e.g. the output of gbsdf_compute_mesh_sdf) and is read in place,
+ * never written. Same rules: boundary voxels read below iso + h read as iso + h; a corner
+ * is inside when value - iso <= 0; one vertex per crossing grid edge at the reference's
+ * clamped linear interpolation, origin + index * h; triangles outward. Vertices are numbered
+ * in voxel order (x, y, z edges of a voxel in turn) and triangles in cube order (the
+ * reference's atomic counters give a run-dependent order). The triangle table is generated
+ * by one face rule (inside corners on an ambiguous face are cut off separately), which
+ * closes the surface for any grid; on ambiguous cubes it may connect the vertices
+ * differently from the reference's hand-written table. dims < 2 on any axis: an empty mesh.
+ * Outputs on the host, or on the device with outputs_on_device = 1. When an output is too
+ * small (capacities 0 to query) GBSDF_EINVAL is returned with *n_vertices / *n_indices set
+ * to the counts needed. */
+int gbsdf_extract_iso_surface(const float* grid, int32_t grid_on_device, const int32_t dims[3], float voxel_size,
+                              const float origin[3], float iso_value, float* out_vertices, int64_t vertex_capacity,
+                              uint32_t* out_indices, int64_t index_capacity, int32_t outputs_on_device,
+                              int64_t* n_vertices, int64_t* n_indices, int32_t device, char* err, size_t errlen);
+/* The same with the mesh left on the device in library-owned buffers (one call, no size
+ * query): *vertices_dev / *indices_dev stay valid until the next extraction on `device` or
+ * gbsdf_release_workspace(device). */
+int gbsdf_extract_iso_surface_device(const float* grid, int32_t grid_on_device, const int32_t dims[3],
+                                     float voxel_size, const float origin[3], float iso_value, float** vertices_dev,
+                                     uint32_t** indices_dev, int64_t* n_vertices, int64_t* n_indices, int32_t device,
+                                     char* err, size_t errlen);
+/* The generated triangle table: 256 cases x 16 edge numbers (3 per triangle, -1 ends).
+ * Needs no GPU. */
+int gbsdf_iso_surface_table(int8_t* out_table);
+
+/* Releases the cached device workspaces of `device` -- the SDF builder's and the
+ * iso-surface extractor's (buffers are otherwise reused across calls on the same device). */
 void gbsdf_release_workspace(int32_t device);
 
 /* The exact (legacy-kernel) SDF of gbsdf_compute_mesh_sdf with GBSDF_PATH_LEGACY, for

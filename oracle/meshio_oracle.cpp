@@ -23,6 +23,13 @@
 //   reference numbers vertices in the order its threads win the table slots and keeps the
 //   winner's coordinates; this restatement numbers them in order of first occurrence and
 //   keeps the first corner's coordinates (the engine does the same).
+// * iso-surface: CudaRasterizer::extract_iso_surface (cuda_marching_cubes.cu:829-951): border
+//   seal to iso + h (:312-332), inside when value - iso <= 0 (:334-360), one vertex per
+//   crossing grid edge at the clamped linear interpolation (:415-489), triangles from a
+//   256 x 16 edge table passed in (the engine's generated table: the reference's own
+//   table is hand-written and its atomic counters order the output by thread timing);
+//   vertices numbered in voxel order (x, y, z edges of a voxel in turn), triangles in cube
+//   order.
 // Every expression is restated as written in the reference source, each operation rounded
 // once (compile with -ffp-contract=off; oracle.py does), the same convention as the engine
 // (-fmad=false). A build of the reference that fuses multiply-adds can differ from this by
@@ -243,6 +250,74 @@ int orc_parse_obj(const char* text_in, size_t n, float* verts, uint32_t* idx, in
         }
     }
     if (I == 0) return 1;
+    *nv = V;
+    *ni = I;
+    return 0;
+}
+
+// Counts (out pointers NULL) or extracts the iso-surface; returns 0.
+int orc_extract_iso_surface(const float* g, const int32_t* dims, float h, const float* origin, float iso,
+                            const int8_t* table, float* verts, uint32_t* idx, int64_t* nv, int64_t* ni) {
+    const int dx = dims[0], dy = dims[1], dz = dims[2];
+    *nv = 0;
+    *ni = 0;
+    if (dx < 2 || dy < 2 || dz < 2) return 0;
+    const float seal = iso + h;
+    auto val = [&](int x, int y, int z) {
+        float v = g[((size_t)z * dy + y) * dx + x];
+        if ((x == 0 || x == dx - 1 || y == 0 || y == dy - 1 || z == 0 || z == dz - 1) && v < seal) v = seal;
+        return v - iso;
+    };
+    const size_t N = (size_t)dx * dy * dz;
+    std::vector<uint32_t> vbase(N);
+    std::vector<uint8_t> mask(N);
+    int64_t V = 0;
+    for (int z = 0; z < dz; ++z)
+        for (int y = 0; y < dy; ++y)
+            for (int x = 0; x < dx; ++x) {
+                const size_t i = ((size_t)z * dy + y) * dx + x;
+                const float v0 = val(x, y, z);
+                const bool s0 = v0 <= 0.0f;
+                const float px = origin[0] + (float)x * h, py = origin[1] + (float)y * h, pz = origin[2] + (float)z * h;
+                vbase[i] = (uint32_t)V;
+                uint8_t m = 0;
+                for (int a = 0; a < 3; ++a) {
+                    const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
+                    if (x1 >= dx || y1 >= dy || z1 >= dz) continue;
+                    const float v1 = val(x1, y1, z1);
+                    if (s0 == (v1 <= 0.0f)) continue;
+                    m |= (uint8_t)(1 << a);
+                    if (verts) {
+                        const float den = v0 - v1;
+                        const float t = (std::fabs(den) > 1e-7f) ? std::fmin(std::fmax(v0 / den, 0.001f), 0.999f) : 0.5f;
+                        verts[3 * V] = (a == 0) ? px + t * h : px;
+                        verts[3 * V + 1] = (a == 1) ? py + t * h : py;
+                        verts[3 * V + 2] = (a == 2) ? pz + t * h : pz;
+                    }
+                    ++V;
+                }
+                mask[i] = m;
+            }
+    static const int own[12][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 0}, {0, 0, 1}, {1, 0, 1},
+                                   {0, 1, 1}, {0, 0, 1}, {0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}};
+    static const int axis[12] = {0, 1, 0, 1, 0, 1, 0, 1, 2, 2, 2, 2};
+    static const int corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+    int64_t I = 0;
+    for (int z = 0; z + 1 < dz; ++z)
+        for (int y = 0; y + 1 < dy; ++y)
+            for (int x = 0; x + 1 < dx; ++x) {
+                int cs = 0;
+                for (int c = 0; c < 8; ++c)
+                    if (val(x + corner[c][0], y + corner[c][1], z + corner[c][2]) <= 0.0f) cs |= 1 << c;
+                for (int k = 0; k < 15 && table[16 * cs + k] >= 0; ++k) {
+                    const int e = table[16 * cs + k];
+                    const size_t w = ((size_t)(z + own[e][2]) * dy + (y + own[e][1])) * dx + (x + own[e][0]);
+                    const int a = axis[e];
+                    const uint32_t rank = (a == 0) ? 0u : (a == 1) ? (mask[w] & 1u) : (uint32_t)((mask[w] & 1u) + ((mask[w] >> 1) & 1u));
+                    if (idx) idx[I] = vbase[w] + rank;
+                    ++I;
+                }
+            }
     *nv = V;
     *ni = I;
     return 0;

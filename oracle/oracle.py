@@ -303,6 +303,25 @@ def parse_ascii_stl(text: bytes):
     return st, verts[:nv.value], idx[:ni.value]
 
 
+def extract_iso_surface(grid, dims, voxel_size, origin, iso, table):
+    """Marching cubes (cuda_marching_cubes.cu:829-951) with the edge table `table`
+    (256 x 16 int8). Returns (vertices (V,3), indices (I,))."""
+    g = np.ascontiguousarray(grid, np.float32).ravel()
+    d = np.asarray(dims, np.int32)
+    o = np.asarray(origin, np.float32)
+    t = np.ascontiguousarray(table, np.int8).ravel()
+    nv, ni = C.c_int64(0), C.c_int64(0)
+    L = lib()
+    L.orc_extract_iso_surface.restype = C.c_int
+    L.orc_extract_iso_surface(_p(g), _p(d), C.c_float(voxel_size), _p(o), C.c_float(iso), _p(t), None, None,
+                              C.byref(nv), C.byref(ni))
+    verts = np.zeros((max(nv.value, 1), 3), np.float32)
+    idx = np.zeros(max(ni.value, 1), np.uint32)
+    L.orc_extract_iso_surface(_p(g), _p(d), C.c_float(voxel_size), _p(o), C.c_float(iso), _p(t), _p(verts), _p(idx),
+                              C.byref(nv), C.byref(ni))
+    return verts[:nv.value], idx[:ni.value]
+
+
 def orient_mesh(vertices, indices):
     """Orientation pre-pass (cuda_mesh_topology.cu:707-842). Returns (indices oriented,
     orientable, had_inconsistent_winding, was_inverted, signed volume)."""

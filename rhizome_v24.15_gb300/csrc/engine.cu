@@ -907,6 +907,7 @@ void gbsdf_release_workspace(int32_t device) {
     std::lock_guard<std::mutex> g(g_ws_mu);
     std::lock_guard<std::mutex> lk(g_ws[device].mu);
     free_ws(g_ws[device]);
+    release_iso_workspace(device);
 }
 
 int gbsdf_selftest(int32_t which, int32_t device, uint64_t* result, char* err, size_t errlen) {

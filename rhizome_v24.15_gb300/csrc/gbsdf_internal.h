@@ -105,6 +105,8 @@ void launch_prep(const float* tris12, long long T, const Lattice& L, SplatTri* s
 void launch_exclusive_scan(const unsigned* in, unsigned long long* out, long long n, unsigned long long* tmp,
                            long long tmp_elems, cudaStream_t st);
 long long scan_tmp_elems(long long n);
+// Frees the iso-surface extractor's cached scratch of `device` (k_iso.cu).
+void release_iso_workspace(int device);
 // With `ds`, the pair lists are known to hold `cap_b` / `cap_s` entries: when the counts
 // of this build exceed them the fill writes nothing and sets ds->overflow (the splat and
 // parity passes then skip the build).

@@ -60,6 +60,7 @@ EXPORTS = ("gbsdf_default_options", "gbsdf_compute_mesh_sdf", "gbsdf_compute_mes
            "gbsdf_brick_features", "gbsdf_mlp_forward", "gbsdf_mlp_backward", "gbsdf_mlp_adam",
            "gbsdf_batch_create", "gbsdf_batch_run", "gbsdf_batch_destroy", "gbsdf_parse_binary_stl", "gbsdf_parse_obj",
            "gbsdf_ascii_stl_capacity", "gbsdf_parse_ascii_stl", "gbsdf_orient_mesh",
+           "gbsdf_extract_iso_surface", "gbsdf_extract_iso_surface_device", "gbsdf_iso_surface_table",
            "gbsdf_release_workspace", "gbsdf_legacy_sdf_noalloc", "gbsdf_selftest", "gbsdf_version")
 
 _lib = None
@@ -123,6 +124,16 @@ def load(path: Path | None = None):
     L.gbsdf_orient_mesh.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, i32p, i32p, i32p,
                                     C.POINTER(C.c_double), C.c_int32, C.c_char_p, C.c_size_t]
     L.gbsdf_orient_mesh.restype = C.c_int
+    L.gbsdf_extract_iso_surface.argtypes = [C.c_void_p, C.c_int32, i32p, C.c_float, C.POINTER(C.c_float), C.c_float,
+                                            C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, i64p, i64p,
+                                            C.c_int32, C.c_char_p, C.c_size_t]
+    L.gbsdf_extract_iso_surface.restype = C.c_int
+    L.gbsdf_extract_iso_surface_device.argtypes = [C.c_void_p, C.c_int32, i32p, C.c_float, C.POINTER(C.c_float),
+                                                   C.c_float, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), i64p, i64p,
+                                                   C.c_int32, C.c_char_p, C.c_size_t]
+    L.gbsdf_extract_iso_surface_device.restype = C.c_int
+    L.gbsdf_iso_surface_table.argtypes = [C.c_void_p]
+    L.gbsdf_iso_surface_table.restype = C.c_int
     L.gbsdf_release_workspace.argtypes = [C.c_int32]
     L.gbsdf_release_workspace.restype = None
     L.gbsdf_legacy_sdf_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_float, i32p, i32p, C.c_void_p, C.c_int32,

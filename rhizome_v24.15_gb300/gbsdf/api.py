@@ -333,6 +333,67 @@ def parse_stl(data: bytes, device=0):
     return verts, idx, orientable
 
 
+class _DeviceArray:
+    """A device buffer described by __cuda_array_interface__ (for torch.as_tensor)."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"data": (int(ptr), False), "shape": tuple(shape), "typestr": typestr,
+                                         "version": 2}
+
+
+def extract_iso_surface(grid, dims, voxel_size, origin, iso_value=0.0, device=0, outputs_on_device=False):
+    """Marching cubes of a grid (gbsdf_extract_iso_surface). ``grid``: N floats, x fastest --
+    a numpy array (uploaded, as the reference does) or a CUDA tensor read in place (e.g. the
+    ``out`` of compute_mesh_sdf). Returns (vertices (V,3) float32, indices (I,) uint32), numpy
+    arrays, or CUDA tensors (indices int32) with ``outputs_on_device`` (one call through
+    gbsdf_extract_iso_surface_device)."""
+    d = _i3(dims)
+    o = (C.c_float * 3)(*[float(x) for x in np.asarray(origin, np.float64).reshape(3)])
+    on_dev = bool(getattr(grid, "is_cuda", False))
+    if on_dev:
+        import torch
+
+        if grid.dtype != torch.float32 or not grid.is_contiguous():
+            raise GbsdfError(_lib.EINVAL, "the device grid must be a contiguous float32 tensor")
+        gptr = grid.data_ptr()
+    else:
+        grid = np.ascontiguousarray(grid, np.float32).ravel()
+        gptr = grid.ctypes.data
+    if int(np.prod(np.asarray(dims, np.int64))) > (grid.numel() if on_dev else grid.size):
+        raise GbsdfError(_lib.EINVAL, "the grid holds fewer voxels than dims")
+    L = _lib.load()
+    nv, ni = C.c_int64(0), C.c_int64(0)
+    err = C.create_string_buffer(512)
+    if outputs_on_device:  # one call; copies of the library-owned device mesh
+        import torch
+
+        pv, pi = C.c_void_p(0), C.c_void_p(0)
+        rc = L.gbsdf_extract_iso_surface_device(gptr, int(on_dev), d, float(voxel_size), o, float(iso_value),
+                                                C.byref(pv), C.byref(pi), C.byref(nv), C.byref(ni), int(device), err,
+                                                len(err))
+        if rc != _lib.OK:
+            raise GbsdfError(rc, err.value.decode(errors="replace"))
+        dev = torch.device("cuda", int(device))
+        if nv.value == 0:
+            return torch.empty((0, 3), dtype=torch.float32, device=dev), torch.empty(0, dtype=torch.int32, device=dev)
+        return (torch.as_tensor(_DeviceArray(pv.value, (nv.value, 3), "<f4"), device=dev).clone(),
+                torch.as_tensor(_DeviceArray(pi.value, (ni.value,), "<i4"), device=dev).clone())
+    rc = L.gbsdf_extract_iso_surface(gptr, int(on_dev), d, float(voxel_size), o, float(iso_value), None, 0, None, 0,
+                                     0, C.byref(nv), C.byref(ni), int(device), err, len(err))
+    if rc != _lib.OK and (nv.value == 0 and ni.value == 0 or rc != _lib.EINVAL):
+        raise GbsdfError(rc, err.value.decode(errors="replace"))
+    V, I = nv.value, ni.value
+    verts = np.empty((max(V, 1), 3), np.float32)
+    idx = np.empty(max(I, 1), np.uint32)
+    vp, ip = verts.ctypes.data, idx.ctypes.data
+    if V and I:
+        rc = L.gbsdf_extract_iso_surface(gptr, int(on_dev), d, float(voxel_size), o, float(iso_value), vp, V, ip, I,
+                                         0, C.byref(nv), C.byref(ni), int(device), err, len(err))
+        if rc != _lib.OK:
+            raise GbsdfError(rc, err.value.decode(errors="replace"))
+    return verts[:nv.value], idx[:ni.value]
+
+
 def orient_mesh(vertices, indices, device=0):
     """GPU orientation pre-pass (gbsdf_orient_mesh). Returns (indices oriented (I,) uint32,
     orientable, had_inconsistent_winding, was_inverted, signed volume)."""
@@ -419,6 +480,25 @@ class CudaRasterizer:
         if not res.ok:
             return False, out_distances, res.stats.get("ms_total", 0.0)
         return True, buf, res.stats["ms_total"]
+
+    @staticmethod
+    def extract_iso_surface(grid, dims=None, voxel_size=None, origin=None, iso_value=0.0):
+        """cuda_marching_cubes.cu:829-962: (distance_grid, dims, voxel_size, origin, iso) or
+        (CudaVolumeGrid, iso) -> (ok, (vertices, indices), out_time_ms); dims < 2 gives an
+        empty mesh."""
+        import time as _time
+
+        if isinstance(grid, CudaVolumeGrid):
+            vol = grid
+            iso_value = 0.0 if dims is None else float(dims)
+            grid, dims, voxel_size = vol.data, vol.dims, vol.voxel_size
+            origin = np.asarray(vol.min_coord, np.float32) * np.float32(vol.voxel_size)
+        t0 = _time.perf_counter()
+        try:
+            mesh = extract_iso_surface(grid, dims, voxel_size, origin, iso_value)
+        except GbsdfError:
+            return False, (np.zeros((0, 3), np.float32), np.zeros(0, np.uint32)), 0.0
+        return True, mesh, (_time.perf_counter() - t0) * 1e3
 
     @staticmethod
     def build_from_mesh(vertices, indices, voxel_size):

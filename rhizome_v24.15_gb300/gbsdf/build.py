@@ -21,7 +21,7 @@ INCLUDE = ROOT.parent / "include"
 BUILD = ROOT / "_build"
 LIB = PKG / "libgbsdf.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "k_splat.cu", "k_parity.cu", "k_gwn.cu", "k_eikonal.cu", "k_misc.cu", "noalloc.cu", "k_learn.cu", "batch.cu", "tune.cu", "k_io.cu", "k_orient.cu"]
+SOURCES = ["engine.cu", "k_splat.cu", "k_parity.cu", "k_gwn.cu", "k_eikonal.cu", "k_misc.cu", "noalloc.cu", "k_learn.cu", "batch.cu", "tune.cu", "k_io.cu", "k_orient.cu", "k_iso.cu"]
 
 
 def nvcc() -> str:
