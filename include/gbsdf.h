@@ -317,6 +317,23 @@ int gbsdf_extract_iso_surface_device(const float* grid, int32_t grid_on_device, 
                                      float voxel_size, const float origin[3], float iso_value, float** vertices_dev,
                                      uint32_t** indices_dev, int64_t* n_vertices, int64_t* n_indices, int32_t device,
                                      char* err, size_t errlen);
+/* Interior volume of an SDF grid: the voxels with value <= 0 times h^3. Replaces
+ * CudaRasterizer::compute_sdf_interior_volume_gpu (cuda_viewport_gl.cu:702-741); `grid`
+ * (n_voxels floats) on the host (uploaded, as the reference does) or on the device
+ * (grid_on_device = 1, read in place). GBSDF_EINVAL for an empty grid (the reference
+ * returns false). */
+int gbsdf_interior_volume(const float* grid, int32_t grid_on_device, int64_t n_voxels, float voxel_size,
+                          float* out_volume_mm3, int64_t* out_inside_voxels, int32_t device, char* err,
+                          size_t errlen);
+/* Default growth seed inside an SDF grid. Replaces CudaRasterizer::find_default_seed_gpu
+ * (cuda_viewport_packers.cu:304-384): the seed starts at (centre x, centre y, min_p.z + 2h)
+ * of the box (min_p, max_p); with m the grid minimum (at most 1e30), the voxels with value
+ * <= (m < 0 ? max(desired_margin, 0.65 m) : m + h) compete on 10 max(0, z - min_p.z) +
+ * 0.5 |xy - centre xy| (ties: the lower index), and the winner's lattice point
+ * ((min_coord + i) h) is the seed. Same grid placement as gbsdf_interior_volume. */
+int gbsdf_find_default_seed(const float* grid, int32_t grid_on_device, const int32_t dims[3],
+                            const int32_t min_coord[3], float voxel_size, const float min_p[3], const float max_p[3],
+                            float desired_margin, float out_seed[3], int32_t device, char* err, size_t errlen);
 /* The generated triangle table: 256 cases x 16 edge numbers (3 per triangle, -1 ends).
  * Needs no GPU. */
 int gbsdf_iso_surface_table(int8_t* out_table);

@@ -322,6 +322,48 @@ def extract_iso_surface(grid, dims, voxel_size, origin, iso, table):
     return verts[:nv.value], idx[:ni.value]
 
 
+def interior_volume(grid, voxel_size):
+    """compute_sdf_interior_volume_gpu (cuda_viewport_gl.cu:702-741, kernel :84-112):
+    (float32(count) * float32(h h h), count) over the voxels with value <= 0."""
+    g = np.asarray(grid, np.float32).ravel()
+    c = int(np.count_nonzero(g <= np.float32(0)))
+    h = np.float32(voxel_size)
+    return np.float32(np.float32(c) * np.float32(np.float32(h * h) * h)), c
+
+
+def find_default_seed(grid, dims, min_coord, voxel_size, min_p, max_p, desired_margin):
+    """find_default_seed_gpu (cuda_viewport_packers.cu:304-384, kernel :235-276), float32
+    step by step: grid minimum (values below 1e30), margin, score 10 z_height + 0.5 xy
+    distance, lowest (score, index)."""
+    F = np.float32
+    g = np.asarray(grid, np.float32).ravel()
+    h = F(voxel_size)
+    mnp, mxp = np.asarray(min_p, np.float32), np.asarray(max_p, np.float32)
+    cx, cy = F((mnp[0] + mxp[0]) * F(0.5)), F((mnp[1] + mxp[1]) * F(0.5))
+    seed = np.array([cx, cy, F(mnp[2] + F(F(2.0) * h))], np.float32)
+    finite = g[g < F(1e30)]
+    m = F(finite.min()) if finite.size else F(1e30)
+    margin = F(max(F(desired_margin), F(m * F(0.65)))) if m < 0 else F(m + h)
+    idx = np.nonzero(g <= margin)[0]
+    if idx.size == 0:
+        return seed
+    dx, dy = int(dims[0]), int(dims[1])
+    x, y, z = idx % dx, (idx // dx) % dy, idx // (dx * dy)
+    px = ((np.asarray(min_coord[0]) + x).astype(np.float32) * h).astype(np.float32)
+    py = ((np.asarray(min_coord[1]) + y).astype(np.float32) * h).astype(np.float32)
+    pz = ((np.asarray(min_coord[2]) + z).astype(np.float32) * h).astype(np.float32)
+    ex, ey = (px - cx).astype(np.float32), (py - cy).astype(np.float32)
+    xy = np.sqrt((ex * ex).astype(np.float32) + (ey * ey).astype(np.float32)).astype(np.float32)
+    zh = np.maximum(F(0), (pz - mnp[2]).astype(np.float32))
+    score = ((zh * F(10)).astype(np.float32) + (xy * F(0.5)).astype(np.float32)).astype(np.float32)
+    u = score.view(np.uint32)
+    key = np.where(u & 0x80000000, ~u, u | 0x80000000).astype(np.uint64) << np.uint64(32)
+    key |= (idx.astype(np.uint64) & np.uint64(0xffffffff))
+    b = int(idx[np.argmin(key)])
+    x, y, z = b % dx, (b // dx) % dy, b // (dx * dy)
+    return np.array([F(F(min_coord[0] + x) * h), F(F(min_coord[1] + y) * h), F(F(min_coord[2] + z) * h)], np.float32)
+
+
 def orient_mesh(vertices, indices):
     """Orientation pre-pass (cuda_mesh_topology.cu:707-842). Returns (indices oriented,
     orientable, had_inconsistent_winding, was_inverted, signed volume)."""

@@ -442,6 +442,61 @@ __global__ void __launch_bounds__(kIsoThreads) iso_triangle_kernel(const float* 
     }
 }
 
+// ---- other consumers of the SDF: interior volume, default seed -----------------------
+// CudaRasterizer::compute_sdf_interior_volume_gpu (cuda_viewport_gl.cu:702-741, kernel
+// :84-112) and find_default_seed_gpu (cuda_viewport_packers.cu:304-384, kernel :235-276,
+// min reduce cuda_rasterizer.cu:1632-1665): both read the grid in place here. Counts and
+// minima are integer atomics, so the results do not depend on the launch.
+__device__ __forceinline__ unsigned ordered_u32(float f) {  // order-preserving float key
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void sdf_inside_min_kernel(const float* __restrict__ g, long long n,
+                                      unsigned long long* __restrict__ inside, unsigned* __restrict__ min_key) {
+    unsigned long long c = 0;
+    float mn = 1e30f;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float v = __ldg(&g[i]);
+        c += (v <= 0.0f);
+        if (v < mn) mn = v;
+    }
+    unsigned k = ordered_u32(mn);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        c += __shfl_down_sync(0xffffffffu, c, o);
+        k = min(k, __shfl_down_sync(0xffffffffu, k, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (c) atomicAdd(inside, c);
+        atomicMin(min_key, k);
+    }
+}
+
+__global__ void sdf_seed_kernel(const float* __restrict__ g, int dx, int dy, int dz, int mx, int my, int mz, float h,
+                                float minpz, float cx, float cy, float margin, unsigned long long* __restrict__ best) {
+    const long long n = (long long)dx * dy * dz;
+    unsigned long long b = ~0ull;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float d = __ldg(&g[i]);
+        if (d > margin) continue;
+        const int x = (int)(i % dx), y = (int)((i / dx) % dy), z = (int)(i / ((long long)dx * dy));
+        const float px = (float)(mx + x) * h, py = (float)(my + y) * h, pz = (float)(mz + z) * h;
+        const float ex = px - cx, ey = py - cy;
+        const float xy = sqrtf(ex * ex + ey * ey);
+        const float zh = fmaxf(0.0f, pz - minpz);
+        const float score = zh * 10.0f + xy * 0.5f;
+        const unsigned long long key = ((unsigned long long)ordered_u32(score) << 32) | (unsigned long long)(i & 0xffffffffLL);
+        b = key < b ? key : b;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_down_sync(0xffffffffu, b, o);
+        b = t < b ? t : b;
+    }
+    if ((threadIdx.x & 31) == 0 && b != ~0ull) atomicMin(best, b);
+}
+
 struct IsoErr {
     char* buf;
     size_t len;
@@ -700,6 +755,116 @@ int gbsdf_extract_iso_surface_device(const float* grid, int32_t grid_on_device, 
     *indices_dev = nullptr;
     return extract_iso(grid, grid_on_device, dims, voxel_size, origin, iso_value, nullptr, 0, nullptr, 0, 2,
                        vertices_dev, indices_dev, n_vertices, n_indices, device, err, errlen);
+}
+
+// shared set-up of the two reductions: device, grid on the device, a small result block
+struct SdfReduce {
+    float* dgrid = nullptr;
+    unsigned long long* res = nullptr;  // [0] inside count, [1] min key (low 32), [2] best seed key
+    ~SdfReduce() {
+        if (dgrid) cudaFree(dgrid);
+        if (res) cudaFree(res);
+    }
+};
+
+static int sdf_reduce_setup(const float* grid, int32_t on_dev, long long n, int32_t device, IsoErr& e,
+                            SdfReduce& r, const float** g) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        return e.set(GBSDF_ENODEV, "no CUDA device available");
+    }
+    if (device < 0 || device >= ndev) return e.set(GBSDF_ENODEV, "device %d out of range", device);
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return e.set(GBSDF_ECUDA, "cudaSetDevice failed");
+    }
+    cudaError_t ce = cudaMalloc(&r.res, 3 * sizeof(unsigned long long));
+    if (ce == cudaSuccess && !on_dev) {  // the reference's path: the host grid is uploaded
+        ce = cudaMalloc(&r.dgrid, (size_t)n * 4);
+        if (ce == cudaSuccess) ce = cudaMemcpy(r.dgrid, grid, (size_t)n * 4, cudaMemcpyHostToDevice);
+    }
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        return e.set(ce == cudaErrorMemoryAllocation ? GBSDF_ENOMEM : GBSDF_ECUDA, "device set-up: %s",
+                     cudaGetErrorString(ce));
+    }
+    *g = on_dev ? grid : r.dgrid;
+    const unsigned long long init[3] = {0ull, 0xffffffffull, ~0ull};
+    ce = cudaMemcpy(r.res, init, sizeof(init), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "device set-up: %s", cudaGetErrorString(ce));
+    GBSDF_COUNT_LAUNCH();
+    sdf_inside_min_kernel<<<152 * 8, 256>>>(*g, n, &r.res[0], reinterpret_cast<unsigned*>(&r.res[1]));
+    return GBSDF_OK;
+}
+
+static float ordered_to_float(unsigned k) {
+    const unsigned u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+int gbsdf_interior_volume(const float* grid, int32_t grid_on_device, int64_t n_voxels, float voxel_size,
+                          float* out_volume_mm3, int64_t* out_inside_voxels, int32_t device, char* err,
+                          size_t errlen) {
+    IsoErr e{err, errlen};
+    if (err && errlen) err[0] = 0;
+    if (!out_volume_mm3) return e.set(GBSDF_EINVAL, "null output");
+    *out_volume_mm3 = 0.0f;
+    if (out_inside_voxels) *out_inside_voxels = 0;
+    if (!grid || n_voxels <= 0) return e.set(GBSDF_EINVAL, "empty grid");  // the reference returns false
+    SdfReduce r;
+    const float* g = nullptr;
+    int rc = sdf_reduce_setup(grid, grid_on_device, n_voxels, device, e, r, &g);
+    if (rc != GBSDF_OK) return rc;
+    unsigned long long cnt = 0;
+    const cudaError_t ce = cudaMemcpy(&cnt, &r.res[0], 8, cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "interior volume: %s", cudaGetErrorString(ce));
+    const float vox = voxel_size * voxel_size * voxel_size;
+    *out_volume_mm3 = (float)cnt * vox;
+    if (out_inside_voxels) *out_inside_voxels = (int64_t)cnt;
+    return GBSDF_OK;
+}
+
+int gbsdf_find_default_seed(const float* grid, int32_t grid_on_device, const int32_t dims[3],
+                            const int32_t min_coord[3], float voxel_size, const float min_p[3], const float max_p[3],
+                            float desired_margin, float out_seed[3], int32_t device, char* err, size_t errlen) {
+    IsoErr e{err, errlen};
+    if (err && errlen) err[0] = 0;
+    if (!dims || !min_coord || !min_p || !max_p || !out_seed) return e.set(GBSDF_EINVAL, "null argument");
+    const float cx = (min_p[0] + max_p[0]) * 0.5f, cy = (min_p[1] + max_p[1]) * 0.5f;
+    out_seed[0] = cx;
+    out_seed[1] = cy;
+    out_seed[2] = min_p[2] + 2.0f * voxel_size;
+    const long long n = (long long)dims[0] * dims[1] * dims[2];
+    if (!grid || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return e.set(GBSDF_EINVAL, "empty grid");
+    SdfReduce r;
+    const float* g = nullptr;
+    int rc = sdf_reduce_setup(grid, grid_on_device, n, device, e, r, &g);
+    if (rc != GBSDF_OK) return rc;
+    unsigned long long mk = 0;
+    cudaError_t ce = cudaMemcpy(&mk, &r.res[1], 8, cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "default seed: %s", cudaGetErrorString(ce));
+    const float mn = std::min(1e30f, ordered_to_float((unsigned)mk));
+    const float margin = (mn < 0.0f) ? std::max(desired_margin, mn * 0.65f) : (mn + voxel_size);
+    GBSDF_COUNT_LAUNCH();
+    sdf_seed_kernel<<<152 * 8, 256>>>(g, dims[0], dims[1], dims[2], min_coord[0], min_coord[1], min_coord[2],
+                                      voxel_size, min_p[2], cx, cy, margin, &r.res[2]);
+    unsigned long long best = ~0ull;
+    ce = cudaMemcpy(&best, &r.res[2], 8, cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "default seed: %s", cudaGetErrorString(ce));
+    if (best != ~0ull) {
+        const long long i = (long long)(best & 0xffffffffull);
+        if (i < n) {
+            const int x = (int)(i % dims[0]), y = (int)((i / dims[0]) % dims[1]),
+                      z = (int)(i / ((long long)dims[0] * dims[1]));
+            out_seed[0] = (float)(min_coord[0] + x) * voxel_size;
+            out_seed[1] = (float)(min_coord[1] + y) * voxel_size;
+            out_seed[2] = (float)(min_coord[2] + z) * voxel_size;
+        }
+    }
+    return GBSDF_OK;
 }
 
 }  // extern "C"

@@ -8,10 +8,10 @@ from . import meshgen
 from ._lib import LIB_PATH, load
 from .api import (MODE_EXACT, MODE_EXACT_SIGNS, MODE_LEARNED, MODE_REFERENCE, PATH_AUTO, PATH_FAST, PATH_LEGACY, Batch,
                   CudaRasterizer, CudaVolumeGrid, GbsdfError, Result, build_from_mesh, compute_mesh_sdf,
-                  compute_mesh_sdf_batch, extract_iso_surface, mesh_lattice, orient_mesh, parse_ascii_stl, parse_binary_stl, parse_obj,
+                  compute_mesh_sdf_batch, extract_iso_surface, find_default_seed, interior_volume, mesh_lattice, orient_mesh, parse_ascii_stl, parse_binary_stl, parse_obj,
                   parse_stl)
 
 __all__ = ["meshgen", "LIB_PATH", "load", "MODE_EXACT", "MODE_EXACT_SIGNS", "MODE_LEARNED", "MODE_REFERENCE",
            "PATH_AUTO", "PATH_FAST", "PATH_LEGACY", "Batch", "CudaRasterizer", "CudaVolumeGrid", "GbsdfError", "Result",
-           "build_from_mesh", "compute_mesh_sdf", "compute_mesh_sdf_batch", "extract_iso_surface", "mesh_lattice", "orient_mesh",
+           "build_from_mesh", "compute_mesh_sdf", "compute_mesh_sdf_batch", "extract_iso_surface", "find_default_seed", "interior_volume", "mesh_lattice", "orient_mesh",
            "parse_ascii_stl", "parse_binary_stl", "parse_obj", "parse_stl"]

@@ -61,6 +61,7 @@ EXPORTS = ("gbsdf_default_options", "gbsdf_compute_mesh_sdf", "gbsdf_compute_mes
            "gbsdf_batch_create", "gbsdf_batch_run", "gbsdf_batch_destroy", "gbsdf_parse_binary_stl", "gbsdf_parse_obj",
            "gbsdf_ascii_stl_capacity", "gbsdf_parse_ascii_stl", "gbsdf_orient_mesh",
            "gbsdf_extract_iso_surface", "gbsdf_extract_iso_surface_device", "gbsdf_iso_surface_table",
+           "gbsdf_interior_volume", "gbsdf_find_default_seed",
            "gbsdf_release_workspace", "gbsdf_legacy_sdf_noalloc", "gbsdf_selftest", "gbsdf_version")
 
 _lib = None
@@ -132,6 +133,13 @@ def load(path: Path | None = None):
                                                    C.c_float, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), i64p, i64p,
                                                    C.c_int32, C.c_char_p, C.c_size_t]
     L.gbsdf_extract_iso_surface_device.restype = C.c_int
+    f3p = C.POINTER(C.c_float)
+    L.gbsdf_interior_volume.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_float, f3p, i64p, C.c_int32,
+                                        C.c_char_p, C.c_size_t]
+    L.gbsdf_interior_volume.restype = C.c_int
+    L.gbsdf_find_default_seed.argtypes = [C.c_void_p, C.c_int32, i32p, i32p, C.c_float, f3p, f3p, C.c_float, f3p,
+                                          C.c_int32, C.c_char_p, C.c_size_t]
+    L.gbsdf_find_default_seed.restype = C.c_int
     L.gbsdf_iso_surface_table.argtypes = [C.c_void_p]
     L.gbsdf_iso_surface_table.restype = C.c_int
     L.gbsdf_release_workspace.argtypes = [C.c_int32]

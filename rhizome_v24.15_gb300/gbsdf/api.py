@@ -394,6 +394,43 @@ def extract_iso_surface(grid, dims, voxel_size, origin, iso_value=0.0, device=0,
     return verts[:nv.value], idx[:ni.value]
 
 
+def _grid_ptr(grid):
+    if bool(getattr(grid, "is_cuda", False)):
+        import torch
+
+        if grid.dtype != torch.float32 or not grid.is_contiguous():
+            raise GbsdfError(_lib.EINVAL, "the device grid must be a contiguous float32 tensor")
+        return grid.data_ptr(), 1, grid, int(grid.numel())
+    g = np.ascontiguousarray(grid, np.float32).ravel()
+    return g.ctypes.data, 0, g, int(g.size)
+
+
+def interior_volume(grid, voxel_size, device=0):
+    """Interior volume (gbsdf_interior_volume): (volume mm^3 as float32, inside voxels).
+    ``grid``: numpy array (uploaded) or CUDA tensor (read in place)."""
+    ptr, on_dev, keep, n = _grid_ptr(grid)
+    vol, cnt = C.c_float(0.0), C.c_int64(0)
+    err = C.create_string_buffer(256)
+    rc = _lib.load().gbsdf_interior_volume(ptr, on_dev, n, float(voxel_size), C.byref(vol), C.byref(cnt), int(device),
+                                           err, len(err))
+    if rc != _lib.OK:
+        raise GbsdfError(rc, err.value.decode(errors="replace"))
+    return np.float32(vol.value), cnt.value
+
+
+def find_default_seed(grid, dims, min_coord, voxel_size, min_p, max_p, desired_margin, device=0):
+    """Default growth seed (gbsdf_find_default_seed): a float32 (3,) point."""
+    ptr, on_dev, keep, n = _grid_ptr(grid)
+    f3 = lambda v: (C.c_float * 3)(*[float(x) for x in np.asarray(v, np.float32).reshape(3)])
+    out = (C.c_float * 3)()
+    err = C.create_string_buffer(256)
+    rc = _lib.load().gbsdf_find_default_seed(ptr, on_dev, _i3(dims), _i3(min_coord), float(voxel_size), f3(min_p),
+                                             f3(max_p), float(desired_margin), out, int(device), err, len(err))
+    if rc != _lib.OK:
+        raise GbsdfError(rc, err.value.decode(errors="replace"))
+    return np.array(list(out), np.float32)
+
+
 def orient_mesh(vertices, indices, device=0):
     """GPU orientation pre-pass (gbsdf_orient_mesh). Returns (indices oriented (I,) uint32,
     orientable, had_inconsistent_winding, was_inverted, signed volume)."""

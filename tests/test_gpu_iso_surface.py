@@ -77,3 +77,32 @@ def test_iso_surface_edges(engine):
     assert len(e[1]) == 0  # nothing inside
     with pytest.raises(engine.GbsdfError):
         engine.extract_iso_surface(np.zeros(8, np.float32), (2, 2, 2), 0.0, (0, 0, 0))  # bad voxel size
+
+
+def test_volume_and_seed(engine, oracle):
+    """gbsdf_interior_volume / gbsdf_find_default_seed against the oracle, host and device
+    grids, on a sphere's field and on the engine's own mug SDF."""
+    import torch
+
+    from gbsdf import meshgen
+
+    rng = np.random.default_rng(5)
+    n, h = 70, 0.1
+    ax = (np.arange(n) - 35) * h
+    z, y, x = np.meshgrid(ax, ax, ax, indexing="ij")
+    g = (np.sqrt(x * x + y * y + (z - 0.3) ** 2) - 2.5).astype(np.float32)
+    v, f = meshgen.mug(segments=48, n_bottom=3, n_wall=5, n_rim=1, handle_path=12, handle_around=10)
+    out, mn, mx, _ = engine.build_from_mesh(v.astype(np.float32), f.astype(np.uint32).ravel(), 1.5)
+    cases = [(g, (n, n, n), (-35, -35, -35), h, (-3.0, -2.5, -2.0), (3.0, 3.5, 2.0), -0.4),
+             (g + rng.normal(0, 1e-3, g.shape).astype(np.float32), (n, n, n), (-35, -35, -35), h, (-3, -3, -3),
+              (3, 3, 3), -9.0),
+             (out, mx - mn + 1, mn, 1.5, v.min(0), v.max(0), -4.0)]
+    for grid, dims, mc, hh, lo, hi, margin in cases:
+        for dev in (False, True):
+            gg = torch.from_numpy(grid).cuda() if dev else grid
+            vol, cnt = engine.interior_volume(gg, hh)
+            ovol, ocnt = oracle.interior_volume(grid, hh)
+            assert cnt == ocnt and vol == ovol
+            s = engine.find_default_seed(gg, dims, mc, hh, lo, hi, margin)
+            os_ = oracle.find_default_seed(grid, dims, mc, hh, lo, hi, margin)
+            assert np.array_equal(s, os_), (s, os_)

@@ -89,3 +89,22 @@ def test_sphere_surface(table):
     # outward: the signed volume is positive
     a, b, c = v[tri[:, 0]].astype(np.float64), v[tri[:, 1]].astype(np.float64), v[tri[:, 2]].astype(np.float64)
     assert np.einsum("ij,ij->i", a, np.cross(b, c)).sum() / 6 > 0
+
+
+def test_volume_and_seed_oracle():
+    """Interior volume and default seed (the other consumers of the SDF) on a sphere's
+    distance field: the volume of the voxels inside, the seed at the bottom of the ball shrunk
+    by the margin, on the vertical through the box centre."""
+    n, h, r = 60, 0.1, 2.2
+    ax = (np.arange(n) - 30) * h  # lattice points (min + i) h, min = -30
+    z, y, x = np.meshgrid(ax, ax, ax, indexing="ij")
+    g = (np.sqrt(x * x + y * y + z * z) - r).astype(np.float32)
+    vol, cnt = O.interior_volume(g, h)
+    assert cnt == int((g <= 0).sum()) and abs(vol - 4 / 3 * np.pi * r ** 3) < 0.02 * 4 / 3 * np.pi * r ** 3
+    seed = O.find_default_seed(g, (n, n, n), (-30, -30, -30), h, (-3.0, -3.0, -3.0), (3.0, 3.0, 3.0), -0.5)
+    assert abs(seed[0]) < 1e-6 and abs(seed[1]) < 1e-6
+    assert -r + 0.5 - h <= seed[2] <= -r + 0.5 + h  # lowest voxel with value <= -0.5
+    # nothing inside: the margin becomes min + h, the seed is still the lowest central voxel
+    seed = O.find_default_seed(g + np.float32(10), (n, n, n), (-30, -30, -30), h, (-3.0, -3.0, -3.0),
+                               (3.0, 3.0, 3.0), -0.5)
+    assert abs(seed[0]) < 1e-6 and abs(seed[1]) < 1e-6
