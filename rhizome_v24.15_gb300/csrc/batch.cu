@@ -451,11 +451,12 @@ int check_member(const gbsdf_mesh_desc& m, int mode, BErr& e) {
         d[k] = (long long)m.max_coord[k] - m.min_coord[k] + 1;
         if (d[k] <= 0 || d[k] > (1 << 30)) return e.set(GBSDF_EINVAL, "empty or oversized lattice");
     }
-    // the reference's int-range guards (cuda_rasterizer.cu:816-820)
+    // the reference's int-range guards (cuda_rasterizer.cu:816-820), reference mode only
+    // (the engine indexes in 64 bits; exact-signs batches serve such lattices)
     const long long G = 2000000000LL, N = d[0] * d[1] * d[2];
-    if (N > G || m.n_tris * d[2] > G || d[0] * d[1] > G || d[0] * d[2] > G || d[1] * d[2] > G)
+    if (mode == GBSDF_MODE_REFERENCE &&
+        (N > G || m.n_tris * d[2] > G || d[0] * d[1] > G || d[0] * d[2] > G || d[1] * d[2] > G))
         return e.set(GBSDF_EGUARD, "reference int-range guard declines the fast path");
-    (void)mode;
     return GBSDF_OK;
 }
 

@@ -612,8 +612,9 @@ int compute(const float* tris12, long long T, bool tris_dev, float h, const int3
     const long long N = dims[0] * dims[1] * dims[2];
     int path = o.path;
     if (path == GBSDF_PATH_AUTO) path = ((unsigned long long)N >= kFastMinVoxels) ? GBSDF_PATH_FAST : GBSDF_PATH_LEGACY;
-    // the reference's int-range guards (cuda_rasterizer.cu:816-820), reference mode only
-    if (path == GBSDF_PATH_FAST && o.mode != GBSDF_MODE_EXACT) {
+    // the reference's int-range guards (cuda_rasterizer.cu:816-820): reference and learned
+    // modes (the engine indexes in 64 bits; exact-signs and exact modes serve such lattices)
+    if (path == GBSDF_PATH_FAST && (o.mode == GBSDF_MODE_REFERENCE || o.mode == GBSDF_MODE_LEARNED)) {
         const long long G = 2000000000LL;
         if (N > G || T * dims[2] > G || dims[0] * dims[1] > G || dims[0] * dims[2] > G || dims[1] * dims[2] > G) {
             if (o.path != GBSDF_PATH_AUTO)
