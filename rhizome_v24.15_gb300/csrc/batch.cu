@@ -171,6 +171,8 @@ void place_phase1(Job& j, Carver& c) {
     j.fwn.scan = c.take<unsigned long long>((size_t)fwn_scan_elems(j.fwn.g) * 8);
     j.fwn.fb = c.take<long long>((size_t)j.list_cap * 8);
     j.fwn.fb_cap = j.list_cap;
+    void* sup = c.take<char>(fwn_super_bytes(j.fwn.g, T, j.list_cap));
+    if (sup) fwn_super_carve(j.fwn, sup, T, j.list_cap);
 }
 
 void place_phase2(Job& j, Carver& c) {

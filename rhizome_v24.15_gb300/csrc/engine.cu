@@ -65,7 +65,7 @@ struct Workspace {
     std::mutex mu;
     Buf A, B, S, U, t12, t9, stt, ptt, bcount, bcur, boff, active, blist, scount, scur, soff, slist, scan, list,
         recheck, hb, verts, idx, flags, fpos, S2, U2, fbase, fX, logits, opencnt, ekeys, ecnt, mparts, mlossp, phist, E, fwc, fwt, fwo, fwn, fwu, fwf, fwoff,
-        fwci, fwscan, fwfb;
+        fwci, fwscan, fwfb, fws;
     DevState* ds = nullptr;
     DevState* hs = nullptr;  // pinned host mirror
 };
@@ -141,7 +141,7 @@ void free_ws(Workspace& w) {
                    &w.active, &w.blist, &w.scount, &w.scur, &w.soff, &w.slist, &w.scan, &w.list, &w.recheck,
                    &w.hb, &w.verts, &w.idx, &w.flags, &w.fpos, &w.S2, &w.U2, &w.fbase, &w.fX, &w.logits,
                    &w.opencnt, &w.ekeys, &w.ecnt, &w.mparts, &w.mlossp, &w.phist, &w.E,
-                   &w.fwc, &w.fwt, &w.fwo, &w.fwn, &w.fwu, &w.fwf, &w.fwoff, &w.fwci, &w.fwscan, &w.fwfb};
+                   &w.fwc, &w.fwt, &w.fwo, &w.fwn, &w.fwu, &w.fwf, &w.fwoff, &w.fwci, &w.fwscan, &w.fwfb, &w.fws};
     for (Buf* b : bufs) {
         if (b->p) cudaFree(b->p);
         *b = Buf{};
@@ -189,6 +189,8 @@ int build_fwn(Workspace& w, const Lattice& L, long long T, Fwn& f, Err& e) {
     f = Fwn{g, P<FwnCell>(w.fwc), P<unsigned>(w.fwt), P<unsigned>(w.fwo), P<unsigned>(w.fwn), P<unsigned>(w.fwu),
             P<unsigned>(w.fwf), P<unsigned long long>(w.fwoff), P<unsigned long long>(w.fwci),
             P<unsigned long long>(w.fwscan), P<long long>(w.fwfb), kListCap};
+    GB_CK(ensure(w.fws, fwn_super_bytes(g, T, kListCap)));
+    fwn_super_carve(f, w.fws.p, T, kListCap);
     launch_fwn_build(P<float>(w.t9), T, L, f, w.ds, st);
     GB_CK(cudaGetLastError());
     return GBSDF_OK;

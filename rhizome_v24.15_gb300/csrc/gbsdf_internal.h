@@ -69,6 +69,8 @@ struct DevState {
     unsigned long long fwn_certified;  // voxels whose side the cluster bound decided
     unsigned long long fwn_fallback;   // voxels handed to the exact sum (current pass)
     unsigned long long fwn_fallback_total;
+    unsigned long long fwn_supers;     // super-clusters (4^3 cluster cubes) of the first stage
+    unsigned long long fwn_fallback2;  // voxels the super-cluster stage left to the cluster stage
     int changed[64];                   // per eikonal round
     int stop;                          // eikonal converged flag
     int rounds;
@@ -180,8 +182,26 @@ struct Fwn {
     unsigned long long* scan; // scan scratch
     long long* fb;            // voxels left to the exact sum
     long long fb_cap;
+    // super-clusters: the clusters of each cube of 4^3 cluster cubes, with aggregated
+    // moments; a first query stage uses them for far super-clusters and hands the voxels
+    // it cannot decide to the cluster stage (fb2)
+    long long scells = 0;            // super grid cubes
+    int sn[3] = {0, 0, 0};
+    FwnCell* supers = nullptr;       // capacity: min(super cubes, clusters)
+    unsigned* sup_of = nullptr;      // per cluster: its super cube
+    unsigned* sup_counts = nullptr;  // per super cube
+    unsigned* sup_cursor = nullptr;
+    unsigned* sup_flag = nullptr;
+    unsigned long long* sup_off = nullptr;
+    unsigned long long* sup_cidx = nullptr;
+    unsigned* sup_child = nullptr;   // clusters by super cube, ascending within a cube
+    long long* fb2 = nullptr;        // voxels left to the cluster stage (capacity fb_cap)
 };
 long long fwn_scan_elems(const FwnGrid& g);
+// Bytes of the super-cluster arrays of `g` (T triangles, list capacity `cap`), and their
+// carving from one 256-byte aligned allocation into f (sets scells, sn and the pointers).
+size_t fwn_super_bytes(const FwnGrid& g, long long T, long long cap);
+void fwn_super_carve(Fwn& f, void* base, long long T, long long cap);
 // Builds the clusters of the packed triangles (device only, no host round trip).
 void launch_fwn_build(const float* tri9, long long T, const Lattice& L, const Fwn& f, DevState* ds, cudaStream_t st);
 // Decides the listed voxels (as launch_gwn does) by the cluster bound, then sums the rest

@@ -172,6 +172,8 @@ __global__ void __launch_bounds__(kGwnThreads) gwn_kernel(const float* __restric
 #define GBSDF_FWN_BETA 4.0f
 #endif
 constexpr float kFwnBeta = GBSDF_FWN_BETA;  // a cluster is far when d > beta r
+constexpr float kFwnBetaFine = 16.0f;       // the refining stage's threshold
+constexpr long long kFwnFineMinTris = 1000000;  // meshes that get the refining stage
 constexpr float kFwnSlackRel = 1e-5f;  // rounding slack per unit of summed |terms|
 constexpr float kFwnSlackAbs = 1e-5f;  // rounding slack in w
 
@@ -221,13 +223,18 @@ __device__ __forceinline__ double warp_sum_d(double x) {
 __global__ void fwn_stats_kernel(const float* __restrict__ t9, long long ncg, const unsigned* __restrict__ counts,
                                  const unsigned long long* __restrict__ off, const unsigned* __restrict__ flag,
                                  const unsigned long long* __restrict__ cidx, const unsigned* __restrict__ tri,
-                                 FwnCell* __restrict__ cells, DevState* ds) {
+                                 FwnCell* __restrict__ cells, DevState* ds, FwnGrid g, int snx, int sny,
+                                 unsigned* __restrict__ sup_of) {
     const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (b >= ncg) return;
     if (b == ncg - 1 && lane == 0) ds->fwn_cells = cidx[b] + flag[b];
     const unsigned n = counts[b];
     if (!n) return;
+    if (lane == 0) {  // the super cube of this cluster (4^3 cluster cubes)
+        const long long bx = b % g.n[0], by = (b / g.n[0]) % g.n[1], bz = b / ((long long)g.n[0] * g.n[1]);
+        sup_of[cidx[b]] = (unsigned)(((bz >> 2) * sny + (by >> 2)) * snx + (bx >> 2));
+    }
     const unsigned long long o = off[b];
     double A = 0.0, D[3] = {0, 0, 0}, G[3] = {0, 0, 0}, mean[3] = {0, 0, 0};
     double M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // sum_t D_t g_t^T; shifted to c below
@@ -294,13 +301,134 @@ __global__ void fwn_stats_kernel(const float* __restrict__ t9, long long ncg, co
     cells[cidx[b]] = c;
 }
 
+// ---- super-clusters ---------------------------------------------------------------
+__global__ void fwn_sup_count_kernel(const DevState* ds, const unsigned* __restrict__ sup_of,
+                                     unsigned* __restrict__ sup_counts) {
+    const long long n = (long long)ds->fwn_cells;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        atomicAdd(&sup_counts[sup_of[k]], 1u);
+}
+
+__global__ void fwn_sup_fill_kernel(const DevState* ds, const unsigned* __restrict__ sup_of,
+                                    const unsigned long long* __restrict__ sup_off, unsigned* __restrict__ cursor,
+                                    unsigned* __restrict__ child) {
+    const long long n = (long long)ds->fwn_cells;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const unsigned s = sup_of[k];
+        child[sup_off[s] + atomicAdd(&cursor[s], 1u)] = (unsigned)k;
+    }
+}
+
+// One warp per super cube: its children sorted ascending (the fill's order is the atomics'),
+// then the aggregated moments in FP64: area A = sum A_c, area vector D = sum D_c, centroid
+// C = sum A_c c_c / A, first moment about C, M = sum (M_c + D_c (c_c - C)^T) (the moments
+// of the triangles themselves, shifted), radius R = max (|c_c - C| + r_c): every triangle
+// point lies within R of C, so the cluster bound holds with (C, R, A).
+__global__ void fwn_sup_stats_kernel(long long nsc, const unsigned* __restrict__ counts,
+                                     const unsigned long long* __restrict__ off, const unsigned* __restrict__ flag,
+                                     const unsigned long long* __restrict__ cidx, unsigned* __restrict__ child,
+                                     const FwnCell* __restrict__ cells, FwnCell* __restrict__ supers,
+                                     DevState* ds) {
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (b >= nsc) return;
+    if (b == nsc - 1 && lane == 0) ds->fwn_supers = cidx[b] + flag[b];
+    const unsigned n = counts[b];
+    if (!n) return;
+    unsigned* ch = child + off[b];
+    // n <= 64: two per lane; rank = number of smaller children
+    const unsigned a0 = (lane < (int)n) ? ch[lane] : 0xffffffffu;
+    const unsigned a1 = (lane + 32 < (int)n) ? ch[lane + 32] : 0xffffffffu;
+    unsigned r0 = 0, r1 = 0;
+    for (int i = 0; i < 64; ++i) {
+        const unsigned v = __shfl_sync(0xffffffffu, i < 32 ? a0 : a1, i & 31);
+        r0 += v < a0;
+        r1 += v < a1;
+    }
+    __syncwarp();
+    if (lane < (int)n) ch[r0] = a0;
+    if (lane + 32 < (int)n) ch[r1] = a1;
+    __syncwarp();
+    double A = 0.0, D[3] = {0, 0, 0}, G[3] = {0, 0, 0}, mean[3] = {0, 0, 0};
+    for (unsigned k = lane; k < n; k += 32) {
+        const FwnCell c = cells[ch[k]];
+        A += c.area;
+        const double cc[3] = {c.cx, c.cy, c.cz}, dd[3] = {c.ax, c.ay, c.az};
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            D[i] += dd[i];
+            G[i] += (double)c.area * cc[i];
+            mean[i] += cc[i];
+        }
+    }
+    A = warp_sum_d(A);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        D[i] = warp_sum_d(D[i]);
+        G[i] = warp_sum_d(G[i]);
+        mean[i] = warp_sum_d(mean[i]);
+    }
+    double C[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) C[i] = (A > 0.0) ? G[i] / A : mean[i] / n;
+    const float fc[3] = {(float)C[0], (float)C[1], (float)C[2]};
+    double M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, R = 0.0;
+    for (unsigned k = lane; k < n; k += 32) {
+        const FwnCell c = cells[ch[k]];
+        const double sh[3] = {(double)c.cx - fc[0], (double)c.cy - fc[1], (double)c.cz - fc[2]};
+        const double dd[3] = {c.ax, c.ay, c.az};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) M[3 * i + j] += (double)c.m[3 * i + j] + dd[i] * sh[j];
+        R = fmax(R, sqrt(sh[0] * sh[0] + sh[1] * sh[1] + sh[2] * sh[2]) + (double)c.r);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) M[i] = warp_sum_d(M[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) R = fmax(R, __shfl_xor_sync(0xffffffffu, R, o));
+    if (lane != 0) return;
+    FwnCell S;
+    S.cx = fc[0];
+    S.cy = fc[1];
+    S.cz = fc[2];
+    S.r = (float)(R * (1.0 + 1e-6)) + 1e-30f;
+    S.ax = (float)D[0];
+    S.ay = (float)D[1];
+    S.az = (float)D[2];
+    S.area = (float)(A * (1.0 + 1e-6));
+    for (int i = 0; i < 9; ++i) S.m[i] = (float)M[i];
+    S.off = (unsigned)off[b];
+    S.cnt = n;
+    S.pad0 = 0;
+    supers[cidx[b]] = S;
+}
+
+// far-field term of a cluster (or super-cluster) seen from p, with its truncation bound
+__device__ __forceinline__ void fwn_far(const FwnCell& cl, float dx, float dy, float dz, float d2, float d, float& s,
+                                        float& c, float& mag, float& err) {
+    const float inv3 = 1.0f / (d2 * d);
+    const float dip = (cl.ax * dx + cl.ay * dy + cl.az * dz) * inv3;
+    const float tr = cl.m[0] + cl.m[4] + cl.m[8];
+    const float my0 = cl.m[0] * dx + cl.m[1] * dy + cl.m[2] * dz;
+    const float my1 = cl.m[3] * dx + cl.m[4] * dy + cl.m[5] * dz;
+    const float my2 = cl.m[6] * dx + cl.m[7] * dy + cl.m[8] * dz;
+    const float yMy = dx * my0 + dy * my1 + dz * my2;
+    const float quad = (tr - 3.0f * yMy / d2) * inv3;
+    kahan_add(s, c, dip + quad);
+    mag += fabsf(dip) + fabsf(quad);
+    const float e = (d - cl.r) * 0.99999f;
+    err += 3.0f * cl.r * cl.r * cl.area / (e * e * e * e);
+}
+
 // One warp per listed voxel: far clusters by their dipole with the error bound, near
 // clusters triangle by triangle; lane 0 decides or hands the voxel to the exact sum.
 __global__ void __launch_bounds__(kGwnThreads) fwn_query_kernel(
     const float* __restrict__ t9, const FwnCell* __restrict__ cells, const unsigned* __restrict__ tri, Lattice L,
     const long long* __restrict__ list, long long cap, int consumer, int only_if, uint32_t* __restrict__ sbits,
     const float* __restrict__ dist, int dist_sq, float surf_tol_vox, DevState* ds, long long* __restrict__ fb,
-    long long fb_cap) {
+    long long fb_cap, float beta, unsigned long long* __restrict__ fb_n, int last) {
     if (only_if && !ds->patching) return;
     const float tau = surf_tol_vox * L.h;
     const long long n = min((long long)ds->listed, cap);
@@ -329,7 +457,7 @@ __global__ void __launch_bounds__(kGwnThreads) fwn_query_kernel(
             const float dx = cl.cx - p.x, dy = cl.cy - p.y, dz = cl.cz - p.z;
             const float d2 = dx * dx + dy * dy + dz * dz;
             const float d = sqrtf(d2);
-            if (d > kFwnBeta * cl.r) {
+            if (d > beta * cl.r) {
                 // y = c - q: K(c) = -y / d^3 seen from the centroid's side; grad K(c) =
                 // (I - 3 yy^T / d^2) / d^3 contracted with M (sign: the kernel is x - q)
                 const float inv3 = 1.0f / (d2 * d);
@@ -373,7 +501,7 @@ __global__ void __launch_bounds__(kGwnThreads) fwn_query_kernel(
                 consume(L, v, false, consumer, sbits, ds);
                 ++certified;
             } else {
-                const unsigned long long k = atomicAdd(&ds->fwn_fallback, 1ull);
+                const unsigned long long k = atomicAdd(fb_n, 1ull);
                 if ((long long)k < fb_cap) fb[k] = v;
                 ++handed;
             }
@@ -381,15 +509,127 @@ __global__ void __launch_bounds__(kGwnThreads) fwn_query_kernel(
     }
     if (lane == 0) {
         if (certified) atomicAdd(&ds->fwn_certified, certified);
-        if (handed) atomicAdd(&ds->fwn_fallback_total, handed);
+        if (handed && last) atomicAdd(&ds->fwn_fallback_total, handed);
     }
 }
 
-// the exact sum takes the fallback list as its list
-__global__ void fwn_handoff_kernel(DevState* ds, int only_if, long long fb_cap) {
+constexpr int kNearCap = 256;  // near super-clusters listed per voxel (the rest expand in-lane)
+
+// First stage: one warp per listed voxel over the super-clusters -- far ones by their
+// moments and bound, near ones cluster by cluster (far clusters by moments, near ones
+// triangle by triangle); lane 0 decides or hands the voxel to the cluster stage (fb2),
+// whose tighter bounds decide most of what is left.
+__global__ void __launch_bounds__(kGwnThreads) fwn_query_sup_kernel(
+    const float* __restrict__ t9, const FwnCell* __restrict__ cells, const unsigned* __restrict__ tri,
+    const FwnCell* __restrict__ supers, const unsigned* __restrict__ child, Lattice L,
+    const long long* __restrict__ list, long long cap, int consumer, int only_if, uint32_t* __restrict__ sbits,
+    const float* __restrict__ dist, int dist_sq, float surf_tol_vox, DevState* ds, long long* __restrict__ fb2,
+    long long fb_cap) {
     if (only_if && !ds->patching) return;
-    ds->listed = min(ds->fwn_fallback, (unsigned long long)fb_cap);
-    ds->fwn_fallback = 0ull;
+    const float tau = surf_tol_vox * L.h;
+    const long long n = min((long long)ds->listed, cap);
+    const long long nsup = (long long)ds->fwn_supers;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    __shared__ unsigned near_list[kGwnThreads / 32][kNearCap];
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    unsigned long long certified = 0;
+    for (long long j = warp; j < n; j += nwarps) {
+        const long long v = list[j];
+        if (v < 0) continue;
+        int x, y, z;
+        voxel_coords(L, v, x, y, z);
+        const f3 p = lattice_point(L.mn[0], L.mn[1], L.mn[2], x, y, z, L.h);
+        if (dist) {
+            const float d = dist[v];
+            if (dist_sq ? (d <= tau * tau) : (d <= tau)) {  // on the surface: inside
+                if (lane == 0) consume(L, v, true, consumer, sbits, ds);
+                continue;
+            }
+        }
+        float s = 0.0f, c = 0.0f, err = 0.0f, mag = 0.0f;
+        bool amb = false;
+        // a near cluster: its moments when far enough, else its triangles
+        auto near_cluster = [&](const FwnCell& cl) {
+            const float ex = cl.cx - p.x, ey = cl.cy - p.y, ez = cl.cz - p.z;
+            const float e2 = ex * ex + ey * ey + ez * ez;
+            const float e = sqrtf(e2);
+            if (e > kFwnBeta * cl.r) {
+                fwn_far(cl, ex, ey, ez, e2, e, s, c, mag, err);
+            } else {
+                for (unsigned t = 0; t < cl.cnt; ++t) {
+                    const float* tv = t9 + 9ull * tri[cl.off + t];
+                    const float term = solid_angle_fast(p, mk(tv[0], tv[1], tv[2]), mk(tv[3], tv[4], tv[5]),
+                                                        mk(tv[6], tv[7], tv[8]), amb);
+                    kahan_add(s, c, term);
+                    mag += fabsf(term);
+                }
+            }
+        };
+        // far super-clusters by their moments; near ones listed (in super-cluster order,
+        // slots from a ballot) and their children then split across the lanes
+        int nn = 0;
+        for (long long base = 0; base < nsup; base += 32) {
+            const long long k = base + lane;
+            bool nearby = false;
+            if (k < nsup) {
+                const FwnCell S = supers[k];
+                const float dx = S.cx - p.x, dy = S.cy - p.y, dz = S.cz - p.z;
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                const float d = sqrtf(d2);
+                if (d > kFwnBeta * S.r) fwn_far(S, dx, dy, dz, d2, d, s, c, mag, err);
+                else nearby = true;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, nearby);
+            if (nearby) {
+                const int slot = nn + __popc(bal & ((1u << lane) - 1u));
+                if (slot < kNearCap) {
+                    near_list[wib][slot] = (unsigned)k;
+                } else {  // list full: this lane expands it itself
+                    const FwnCell S = supers[k];
+                    for (unsigned q = 0; q < S.cnt; ++q) near_cluster(cells[child[S.off + q]]);
+                }
+            }
+            nn += __popc(bal);
+        }
+        __syncwarp();
+        nn = min(nn, kNearCap);
+        for (int i = 0; i < nn; ++i) {
+            const FwnCell S = supers[near_list[wib][i]];
+            for (unsigned q = lane; q < S.cnt; q += 32) near_cluster(cells[child[S.off + q]]);
+        }
+        __syncwarp();
+        float tot = s - c;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            tot += __shfl_xor_sync(0xffffffffu, tot, o);
+            err += __shfl_xor_sync(0xffffffffu, err, o);
+            mag += __shfl_xor_sync(0xffffffffu, mag, o);
+        }
+        amb = __any_sync(0xffffffffu, amb);
+        if (lane == 0) {
+            const float w = fabsf(tot * kInv4Pi);
+            const float E = (err + kFwnSlackRel * mag) * kInv4Pi + kFwnSlackAbs;
+            if (!amb && w - E >= 0.5f) {
+                consume(L, v, true, consumer, sbits, ds);
+                ++certified;
+            } else if (!amb && w + E < 0.5f) {
+                consume(L, v, false, consumer, sbits, ds);
+                ++certified;
+            } else {
+                const unsigned long long k = atomicAdd(&ds->fwn_fallback2, 1ull);
+                if ((long long)k < fb_cap) fb2[k] = v;
+            }
+        }
+    }
+    if (lane == 0 && certified) atomicAdd(&ds->fwn_certified, certified);
+}
+
+// the next stage takes the leftovers of the last as its list
+__global__ void fwn_handoff_kernel(DevState* ds, int only_if, long long fb_cap, unsigned long long* fb_n) {
+    if (only_if && !ds->patching) return;
+    ds->listed = min(*fb_n, (unsigned long long)fb_cap);
+    *fb_n = 0ull;
 }
 
 constexpr int kRecheckThreads = 256;
@@ -565,7 +805,58 @@ void launch_fwn_build(const float* tri9, long long T, const Lattice& L, const Fw
     fwn_fill_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(T, f.cell_of, f.off, f.cursor, f.tri);
     GBSDF_COUNT_LAUNCH();
     fwn_stats_kernel<<<(unsigned)((nc * 32 + 255) / 256), 256, 0, st>>>(tri9, nc, f.counts, f.off, f.flag, f.cidx,
-                                                                        f.tri, f.cells, ds);
+                                                                        f.tri, f.cells, ds, f.g, f.sn[0], f.sn[1],
+                                                                        f.sup_of);
+    if (!f.supers) return;
+    const long long ns = f.scells;
+    cudaMemsetAsync(f.sup_counts, 0, (size_t)ns * 4, st);
+    cudaMemsetAsync(f.sup_cursor, 0, (size_t)ns * 4, st);
+    GBSDF_COUNT_LAUNCH();
+    fwn_sup_count_kernel<<<152 * 4, 256, 0, st>>>(ds, f.sup_of, f.sup_counts);
+    launch_exclusive_scan(f.sup_counts, f.sup_off, ns, f.scan, 0, st);
+    GBSDF_COUNT_LAUNCH();
+    fwn_flag_kernel<<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(f.sup_counts, ns, f.sup_flag);
+    launch_exclusive_scan(f.sup_flag, f.sup_cidx, ns, f.scan, 0, st);
+    GBSDF_COUNT_LAUNCH();
+    fwn_sup_fill_kernel<<<152 * 4, 256, 0, st>>>(ds, f.sup_of, f.sup_off, f.sup_cursor, f.sup_child);
+    GBSDF_COUNT_LAUNCH();
+    fwn_sup_stats_kernel<<<(unsigned)((ns * 32 + 255) / 256), 256, 0, st>>>(
+        ns, f.sup_counts, f.sup_off, f.sup_flag, f.sup_cidx, f.sup_child, f.cells, f.supers, ds);
+}
+
+size_t fwn_super_bytes(const FwnGrid& g, long long T, long long cap) {
+    long long ns = 1;
+    for (int k = 0; k < 3; ++k) ns *= (g.n[k] + 3) / 4;
+    const long long ncap = std::max<long long>(1, std::min<long long>(g.cells, T));
+    const long long scap = std::max<long long>(1, std::min<long long>(ns, ncap));
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    return al(scap * sizeof(FwnCell)) + al(ncap * 4) + 3 * al(ns * 4) + 2 * al(ns * 8) + al(ncap * 4) + al(cap * 8);
+}
+
+void fwn_super_carve(Fwn& f, void* base, long long T, long long cap) {
+    long long ns = 1;
+    for (int k = 0; k < 3; ++k) {
+        f.sn[k] = (f.g.n[k] + 3) / 4;
+        ns *= f.sn[k];
+    }
+    f.scells = ns;
+    const long long ncap = std::max<long long>(1, std::min<long long>(f.g.cells, T));
+    const long long scap = std::max<long long>(1, std::min<long long>(ns, ncap));
+    char* p = static_cast<char*>(base);
+    auto take = [&](size_t b) {
+        char* q = p;
+        p += (b + 255) & ~size_t(255);
+        return q;
+    };
+    f.supers = reinterpret_cast<FwnCell*>(take(scap * sizeof(FwnCell)));
+    f.sup_of = reinterpret_cast<unsigned*>(take(ncap * 4));
+    f.sup_counts = reinterpret_cast<unsigned*>(take(ns * 4));
+    f.sup_cursor = reinterpret_cast<unsigned*>(take(ns * 4));
+    f.sup_flag = reinterpret_cast<unsigned*>(take(ns * 4));
+    f.sup_off = reinterpret_cast<unsigned long long*>(take(ns * 8));
+    f.sup_cidx = reinterpret_cast<unsigned long long*>(take(ns * 8));
+    f.sup_child = reinterpret_cast<unsigned*>(take(ncap * 4));
+    f.fb2 = reinterpret_cast<long long*>(take(cap * 8));
 }
 
 void launch_winding(const Fwn* f, const float* tri9, long long T, const Lattice& L, const long long* list,
@@ -577,13 +868,41 @@ void launch_winding(const Fwn* f, const float* tri9, long long T, const Lattice&
                    surf_tol_vox, ds, num_sms, st);
         return;
     }
-    GBSDF_COUNT_LAUNCH();
-    fwn_query_kernel<<<(unsigned)(num_sms * 8), kGwnThreads, 0, st>>>(
-        tri9, f->cells, f->tri, L, list, list_cap, consumer, only_if, sbits, dist, dist_sq, surf_tol_vox, ds, f->fb,
-        f->fb_cap);
-    GBSDF_COUNT_LAUNCH();
-    fwn_handoff_kernel<<<1, 1, 0, st>>>(ds, only_if, f->fb_cap);
-    launch_gwn_team(tri9, T, L, f->fb, f->fb_cap, consumer, sbits, recheck, recheck_cap, dist, dist_sq, surf_tol_vox,
+    // stages, each taking the voxels the last could not decide: super-clusters (when built),
+    // clusters at beta, clusters at kFwnBetaFine (smaller truncation bounds, more triangles
+    // summed near the voxel), then the per-triangle sum
+    long long* bufs[2] = {f->fb2, f->fb};
+    int nb = 0;
+    if (f->supers) {
+        GBSDF_COUNT_LAUNCH();
+        fwn_query_sup_kernel<<<(unsigned)(num_sms * 8), kGwnThreads, 0, st>>>(
+            tri9, f->cells, f->tri, f->supers, f->sup_child, L, list, list_cap, consumer, only_if, sbits, dist,
+            dist_sq, surf_tol_vox, ds, bufs[0], f->fb_cap);
+        GBSDF_COUNT_LAUNCH();
+        fwn_handoff_kernel<<<1, 1, 0, st>>>(ds, only_if, f->fb_cap, &ds->fwn_fallback2);
+        list = bufs[0];
+        list_cap = f->fb_cap;
+        nb = 1;
+    }
+    const float betas[2] = {kFwnBeta, kFwnBetaFine};
+    // the refining stage pays off when the per-triangle sum it spares is long
+    const int stages = (T >= kFwnFineMinTris) ? 2 : 1;
+    for (int stg = 0; stg < stages; ++stg) {
+        long long* out = f->fb2 ? bufs[nb & 1] : f->fb;
+        unsigned long long* cnt = (nb & 1) ? &ds->fwn_fallback : &ds->fwn_fallback2;
+        if (!f->fb2) cnt = &ds->fwn_fallback;
+        GBSDF_COUNT_LAUNCH();
+        fwn_query_kernel<<<(unsigned)(num_sms * 8), kGwnThreads, 0, st>>>(
+            tri9, f->cells, f->tri, L, list, list_cap, consumer, only_if, sbits, dist, dist_sq, surf_tol_vox, ds, out,
+            f->fb_cap, betas[stg], cnt, stg == stages - 1 || !f->fb2);
+        GBSDF_COUNT_LAUNCH();
+        fwn_handoff_kernel<<<1, 1, 0, st>>>(ds, only_if, f->fb_cap, cnt);
+        list = out;
+        list_cap = f->fb_cap;
+        ++nb;
+        if (!f->fb2) break;  // one buffer: a single cluster stage
+    }
+    launch_gwn_team(tri9, T, L, list, f->fb_cap, consumer, sbits, recheck, recheck_cap, dist, dist_sq, surf_tol_vox,
                     ds, num_sms, st, only_if);
 }
 
