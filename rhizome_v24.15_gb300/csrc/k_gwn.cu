@@ -422,6 +422,49 @@ __device__ __forceinline__ void fwn_far(const FwnCell& cl, float dx, float dy, f
     err += 3.0f * cl.r * cl.r * cl.area / (e * e * e * e);
 }
 
+// Per-warp lists of a voxel's near clusters: their triangles are summed with the lanes
+// splitting the concatenated triangle ranges evenly (a lane per cluster would leave most
+// lanes idle while one walks a long cluster).
+constexpr int kNearClCap = 448;
+
+// exclusive prefix of n counts (cnt(i) for i < n) into pre[0..n]; returns the total
+template <class C>
+__device__ __forceinline__ unsigned warp_prefix(int n, unsigned* pre, int lane, C cnt) {
+    unsigned base = 0;
+    for (int b = 0; b < n; b += 32) {
+        const int i = b + lane;
+        const unsigned v = (i < n) ? cnt(i) : 0u;
+        unsigned inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (i < n) pre[i + 1] = base + inc;
+        base += __shfl_sync(0xffffffffu, inc, 31);
+    }
+    if (lane == 0) pre[0] = 0;
+    __syncwarp();
+    return base;
+}
+
+__device__ __forceinline__ void warp_near_triangles(const float* __restrict__ t9, const FwnCell* __restrict__ cells,
+                                                    const unsigned* __restrict__ tri, f3 p, const unsigned* ids,
+                                                    unsigned* pre, int nc, int lane, float& s, float& c, float& mag,
+                                                    bool& amb) {
+    const unsigned total = warp_prefix(nc, pre, lane, [&](int i) { return cells[ids[i]].cnt; });
+    int i = 0;
+    for (unsigned g = lane; g < total; g += 32) {
+        while (pre[i + 1] <= g) ++i;
+        const float* tv = t9 + 9ull * tri[cells[ids[i]].off + (g - pre[i])];
+        const float term =
+            solid_angle_fast(p, mk(tv[0], tv[1], tv[2]), mk(tv[3], tv[4], tv[5]), mk(tv[6], tv[7], tv[8]), amb);
+        kahan_add(s, c, term);
+        mag += fabsf(term);
+    }
+    __syncwarp();
+}
+
 // One warp per listed voxel: far clusters by their dipole with the error bound, near
 // clusters triangle by triangle; lane 0 decides or hands the voxel to the exact sum.
 __global__ void __launch_bounds__(kGwnThreads) fwn_query_kernel(
@@ -433,7 +476,9 @@ __global__ void __launch_bounds__(kGwnThreads) fwn_query_kernel(
     const float tau = surf_tol_vox * L.h;
     const long long n = min((long long)ds->listed, cap);
     const long long ncells = (long long)ds->fwn_cells;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    __shared__ unsigned cl_ids[kGwnThreads / 32][kNearClCap];
+    __shared__ unsigned cl_pre[kGwnThreads / 32][kNearClCap + 1];
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     unsigned long long certified = 0, handed = 0;
@@ -452,37 +497,40 @@ __global__ void __launch_bounds__(kGwnThreads) fwn_query_kernel(
         }
         float s = 0.0f, c = 0.0f, err = 0.0f, mag = 0.0f;
         bool amb = false;
-        for (long long k = lane; k < ncells; k += 32) {
-            const FwnCell cl = cells[k];
-            const float dx = cl.cx - p.x, dy = cl.cy - p.y, dz = cl.cz - p.z;
-            const float d2 = dx * dx + dy * dy + dz * dz;
-            const float d = sqrtf(d2);
-            if (d > beta * cl.r) {
-                // y = c - q: K(c) = -y / d^3 seen from the centroid's side; grad K(c) =
-                // (I - 3 yy^T / d^2) / d^3 contracted with M (sign: the kernel is x - q)
-                const float inv3 = 1.0f / (d2 * d);
-                const float dip = (cl.ax * dx + cl.ay * dy + cl.az * dz) * inv3;
-                const float tr = cl.m[0] + cl.m[4] + cl.m[8];
-                const float my0 = cl.m[0] * dx + cl.m[1] * dy + cl.m[2] * dz;
-                const float my1 = cl.m[3] * dx + cl.m[4] * dy + cl.m[5] * dz;
-                const float my2 = cl.m[6] * dx + cl.m[7] * dy + cl.m[8] * dz;
-                const float yMy = dx * my0 + dy * my1 + dz * my2;
-                const float quad = (tr - 3.0f * yMy / d2) * inv3;
-                const float term = dip + quad;
-                kahan_add(s, c, term);
-                mag += fabsf(dip) + fabsf(quad);
-                const float e = (d - cl.r) * 0.99999f;
-                err += 3.0f * cl.r * cl.r * cl.area / (e * e * e * e);
-            } else {
-                for (unsigned q = 0; q < cl.cnt; ++q) {
-                    const float* tv = t9 + 9ull * tri[cl.off + q];
-                    const float term =
-                        solid_angle_fast(p, mk(tv[0], tv[1], tv[2]), mk(tv[3], tv[4], tv[5]), mk(tv[6], tv[7], tv[8]), amb);
-                    kahan_add(s, c, term);
-                    mag += fabsf(term);
+        // far clusters by their moments; near ones listed (ballot slots, cluster order)
+        // and their triangles summed across the lanes
+        int ncl = 0;
+        for (long long base = 0; base < ncells; base += 32) {
+            const long long k = base + lane;
+            bool nearby = false;
+            if (k < ncells) {
+                const FwnCell cl = cells[k];
+                const float dx = cl.cx - p.x, dy = cl.cy - p.y, dz = cl.cz - p.z;
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                const float d = sqrtf(d2);
+                if (d > beta * cl.r) fwn_far(cl, dx, dy, dz, d2, d, s, c, mag, err);
+                else nearby = true;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, nearby);
+            if (nearby) {
+                const int slot = ncl + __popc(bal & ((1u << lane) - 1u));
+                if (slot < kNearClCap) {
+                    cl_ids[wib][slot] = (unsigned)k;
+                } else {  // list full: this lane sums the cluster itself
+                    const FwnCell cl = cells[k];
+                    for (unsigned q = 0; q < cl.cnt; ++q) {
+                        const float* tv = t9 + 9ull * tri[cl.off + q];
+                        const float term = solid_angle_fast(p, mk(tv[0], tv[1], tv[2]), mk(tv[3], tv[4], tv[5]),
+                                                            mk(tv[6], tv[7], tv[8]), amb);
+                        kahan_add(s, c, term);
+                        mag += fabsf(term);
+                    }
                 }
             }
+            ncl += __popc(bal);
         }
+        __syncwarp();
+        warp_near_triangles(t9, cells, tri, p, cl_ids[wib], cl_pre[wib], min(ncl, kNearClCap), lane, s, c, mag, amb);
         float tot = s - c;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -513,7 +561,7 @@ __global__ void __launch_bounds__(kGwnThreads) fwn_query_kernel(
     }
 }
 
-constexpr int kNearCap = 256;  // near super-clusters listed per voxel (the rest expand in-lane)
+constexpr int kNearCap = 192;  // near super-clusters listed per voxel (the rest expand in-lane)
 
 // First stage: one warp per listed voxel over the super-clusters -- far ones by their
 // moments and bound, near ones cluster by cluster (far clusters by moments, near ones
@@ -531,6 +579,9 @@ __global__ void __launch_bounds__(kGwnThreads) fwn_query_sup_kernel(
     const long long nsup = (long long)ds->fwn_supers;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     __shared__ unsigned near_list[kGwnThreads / 32][kNearCap];
+    __shared__ unsigned s_pre[kGwnThreads / 32][kNearCap + 1];
+    __shared__ unsigned cl_ids[kGwnThreads / 32][kNearClCap];
+    __shared__ unsigned cl_pre[kGwnThreads / 32][kNearClCap + 1];
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     unsigned long long certified = 0;
@@ -594,11 +645,35 @@ __global__ void __launch_bounds__(kGwnThreads) fwn_query_sup_kernel(
         }
         __syncwarp();
         nn = min(nn, kNearCap);
-        for (int i = 0; i < nn; ++i) {
-            const FwnCell S = supers[near_list[wib][i]];
-            for (unsigned q = lane; q < S.cnt; q += 32) near_cluster(cells[child[S.off + q]]);
+        // children of the near super-clusters, concatenated and split across the lanes: far
+        // ones by their moments, near ones listed for the triangle pass
+        const unsigned totalS =
+            warp_prefix(nn, s_pre[wib], lane, [&](int i) { return supers[near_list[wib][i]].cnt; });
+        int ncl = 0, si = 0;
+        for (unsigned gb = 0; gb < totalS; gb += 32) {
+            const unsigned g = gb + lane;
+            bool nearby = false;
+            unsigned cid = 0;
+            if (g < totalS) {
+                while (s_pre[wib][si + 1] <= g) ++si;
+                cid = child[supers[near_list[wib][si]].off + (g - s_pre[wib][si])];
+                const FwnCell cl = cells[cid];
+                const float ex = cl.cx - p.x, ey = cl.cy - p.y, ez = cl.cz - p.z;
+                const float e2 = ex * ex + ey * ey + ez * ez;
+                const float e = sqrtf(e2);
+                if (e > kFwnBeta * cl.r) fwn_far(cl, ex, ey, ez, e2, e, s, c, mag, err);
+                else nearby = true;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, nearby);
+            if (nearby) {
+                const int slot = ncl + __popc(bal & ((1u << lane) - 1u));
+                if (slot < kNearClCap) cl_ids[wib][slot] = cid;
+                else near_cluster(cells[cid]);  // list full: this lane sums it
+            }
+            ncl += __popc(bal);
         }
         __syncwarp();
+        warp_near_triangles(t9, cells, tri, p, cl_ids[wib], cl_pre[wib], min(ncl, kNearClCap), lane, s, c, mag, amb);
         float tot = s - c;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
