@@ -213,7 +213,7 @@ void launch_winding(const Fwn* f, const float* tri9, long long T, const Lattice&
 // Batches: decides on the device whether the build passed its checks (valid triangles,
 // the reference's CSR guard when `csr_guard`, no list overflow); sets ds->abort_ if not.
 void launch_batch_finalize(DevState* ds, int csr_guard, cudaStream_t st);
-void launch_gwn_recheck(const float* tri9, long long T, const Lattice& L, const long long* recheck,
+void launch_gwn_recheck(const float* tri9, long long T, const Lattice& L, long long* recheck,
                         long long recheck_cap, int consumer, uint32_t* sbits, DevState* ds, int num_sms,
                         cudaStream_t st);
 void launch_verify_prepare(const Lattice& L, int gen, const uint32_t* ubits, long long* list, DevState* ds,

@@ -709,20 +709,35 @@ __global__ void fwn_handoff_kernel(DevState* ds, int only_if, long long fb_cap, 
 
 constexpr int kRecheckThreads = 256;
 
+// FP64 re-checks: each listed voxel's winding number summed in FP64 over every triangle.
+// A short list (the usual case) would leave most SMs idle with one CTA per voxel, so each
+// voxel's triangles are cut into S fixed slices (S up to 32, as many as the list buffer
+// holds partial sums for: they go behind the n entries), one CTA per (voxel, slice), and a
+// second kernel adds each voxel's S partials in slice order -- the sums do not depend on
+// the launch. A long list runs one CTA per voxel.
+__device__ __forceinline__ int recheck_slices(long long n, long long cap) {
+    if (n <= 0) return 1;
+    const long long s = (cap - n) / n;
+    return (int)max(1LL, min(32LL, s));
+}
+
 __global__ void __launch_bounds__(kRecheckThreads) gwn_recheck_kernel(const float* __restrict__ tri9, long long T,
-                                                                      Lattice L,
-                                                                      const long long* __restrict__ recheck,
+                                                                      Lattice L, long long* __restrict__ recheck,
                                                                       long long cap, int consumer,
                                                                       uint32_t* __restrict__ sbits, DevState* ds) {
     __shared__ double red[kRecheckThreads];
     const long long n = min((long long)ds->recheck_n, cap);
-    for (long long e = blockIdx.x; e < n; e += gridDim.x) {
-        long long v = recheck[e];
+    const int S = recheck_slices(n, cap);
+    double* partial = reinterpret_cast<double*>(recheck + n);
+    for (long long e = blockIdx.x; e < n * S; e += gridDim.x) {
+        const long long v = recheck[e / S];
+        const long long sl = e % S;
+        const long long t0 = T * sl / S, t1 = T * (sl + 1) / S;
         int x, y, z;
         voxel_coords(L, v, x, y, z);
         f3 p = lattice_point(L.mn[0], L.mn[1], L.mn[2], x, y, z, L.h);
         double s = 0.0;
-        for (long long t = threadIdx.x; t < T; t += kRecheckThreads) {
+        for (long long t = t0 + threadIdx.x; t < t1; t += kRecheckThreads) {
             const float* q = tri9 + t * 9;
             s += solid_angle_f64(p, mk(q[0], q[1], q[2]), mk(q[3], q[4], q[5]), mk(q[6], q[7], q[8]));
         }
@@ -733,11 +748,30 @@ __global__ void __launch_bounds__(kRecheckThreads) gwn_recheck_kernel(const floa
             __syncthreads();
         }
         if (threadIdx.x == 0) {
-            double w = red[0] / (4.0 * 3.14159265358979323846);
-            consume(L, v, fabs(w) >= 0.5, consumer, sbits, ds);
-            atomicAdd(&ds->fp64_rechecks, 1ull);
+            if (S == 1) {
+                double w = red[0] / (4.0 * 3.14159265358979323846);
+                consume(L, v, fabs(w) >= 0.5, consumer, sbits, ds);
+                atomicAdd(&ds->fp64_rechecks, 1ull);
+            } else {
+                partial[e] = red[0];
+            }
         }
         __syncthreads();
+    }
+}
+
+__global__ void gwn_recheck_final_kernel(Lattice L, const long long* __restrict__ recheck, long long cap,
+                                         int consumer, uint32_t* __restrict__ sbits, DevState* ds) {
+    const long long n = min((long long)ds->recheck_n, cap);
+    const int S = recheck_slices(n, cap);
+    if (S == 1) return;
+    const double* partial = reinterpret_cast<const double*>(recheck + n);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int k = 0; k < S; ++k) s += partial[i * S + k];
+        const double w = s / (4.0 * 3.14159265358979323846);
+        consume(L, recheck[i], fabs(w) >= 0.5, consumer, sbits, ds);
+        atomicAdd(&ds->fp64_rechecks, 1ull);
     }
 }
 
@@ -990,12 +1024,14 @@ void launch_gwn_small(const float* tri9, long long T, const Lattice& L, const lo
                                                              recheck, recheck_cap, dist, dist_sq, surf_tol_vox, ds);
 }
 
-void launch_gwn_recheck(const float* tri9, long long T, const Lattice& L, const long long* recheck,
+void launch_gwn_recheck(const float* tri9, long long T, const Lattice& L, long long* recheck,
                         long long recheck_cap, int consumer, uint32_t* sbits, DevState* ds, int num_sms,
                         cudaStream_t st) {
     GBSDF_COUNT_LAUNCH();
     gwn_recheck_kernel<<<(unsigned)(num_sms * 4), kRecheckThreads, 0, st>>>(tri9, T, L, recheck, recheck_cap,
                                                                           consumer, sbits, ds);
+    GBSDF_COUNT_LAUNCH();
+    gwn_recheck_final_kernel<<<16, 256, 0, st>>>(L, recheck, recheck_cap, consumer, sbits, ds);
 }
 
 void launch_verify_prepare(const Lattice& L, int gen, const uint32_t* ubits, long long* list, DevState* ds,
