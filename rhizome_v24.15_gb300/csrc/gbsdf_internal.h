@@ -139,7 +139,7 @@ void launch_gwn(const float* tri9, long long T, const Lattice& L, const long lon
                 const float* dist, int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st);
 // Persistent exact-winding pass over a device-sized list, 32 threads per voxel (any list
 // length, no host round trip); `only_if`: skip unless a patch round is in flight.
-void launch_gwn_team(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
+void launch_gwn_team(const float* tri9, long long T, const Lattice& L, long long* list, long long list_cap,
                      int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, const float* dist,
                      int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st, int only_if = 0);
 

@@ -167,6 +167,121 @@ __global__ void __launch_bounds__(kGwnThreads) gwn_kernel(const float* __restric
     if (pairs) atomicAdd(&ds->gwn_pairs, pairs);
 }
 
+// The per-triangle sum for the voxels the cluster stages leave (launch_gwn_team): as
+// gwn_kernel<32>, but a short list (the usual case) cuts the triangles into S fixed slices
+// (S up to 32, as many as the list buffer holds partials for, behind its n entries), one CTA
+// per (8 voxels, slice); gwn_sliced_final_kernel adds each voxel's partials in slice order
+// and decides, so the result does not depend on the launch.
+__device__ __forceinline__ int team_slices(long long n, long long cap) {
+    if (n <= 0) return 1;
+    return (int)max(1LL, min(32LL, (cap - n) / n));
+}
+
+__global__ void __launch_bounds__(kGwnThreads) gwn_sliced_kernel(const float* __restrict__ tri9, long long T, Lattice L,
+                                                                 long long* __restrict__ list, long long cap,
+                                                                 int consumer, int only_if,
+                                                                 uint32_t* __restrict__ sbits,
+                                                                 long long* __restrict__ recheck,
+                                                                 long long recheck_cap, const float* __restrict__ dist,
+                                                                 int dist_sq, float surf_tol_vox, DevState* ds) {
+    if (only_if && !ds->patching) return;
+    const float tau = surf_tol_vox * L.h;
+    constexpr int VPB = kGwnThreads / 32;
+    __shared__ float s_tri[kGwnChunk * 9];
+    const long long n = min((long long)ds->listed, cap);
+    const int S = team_slices(n, cap);
+    float2* partial = reinterpret_cast<float2*>(list + n);
+    const int member = threadIdx.x & 31;
+    const int slot = threadIdx.x >> 5;
+    const long long ng = (n + VPB - 1) / VPB;
+    unsigned long long pairs = 0;
+    for (long long it = blockIdx.x; it < ng * S; it += gridDim.x) {
+        const long long grp = it / S;
+        const int sl = (int)(it - grp * S);
+        const long long j = grp * VPB + slot;
+        long long v = (j < n) ? list[j] : -1;
+        f3 p = mk(0.f, 0.f, 0.f);
+        if (v >= 0) {
+            int x, y, z;
+            voxel_coords(L, v, x, y, z);
+            p = lattice_point(L.mn[0], L.mn[1], L.mn[2], x, y, z, L.h);
+            if (dist) {
+                const float d = dist[v];
+                if (dist_sq ? (d <= tau * tau) : (d <= tau)) {  // on the surface: inside
+                    if (member == 0 && sl == 0) consume(L, v, true, consumer, sbits, ds);
+                    v = -2;
+                }
+            }
+        }
+        const long long t0 = T * sl / S, t1 = T * (sl + 1) / S;
+        float s = 0.0f, c = 0.0f;
+        bool amb = false;
+        for (long long c0 = t0; c0 < t1; c0 += kGwnChunk) {
+            const int m = (int)min((long long)kGwnChunk, t1 - c0);
+            __syncthreads();
+            for (int k = threadIdx.x; k < m * 9; k += kGwnThreads) s_tri[k] = __ldg(tri9 + c0 * 9 + k);
+            __syncthreads();
+            if (v >= 0) {
+                for (int i = member; i < m; i += 32) {
+                    const float* t = s_tri + i * 9;
+                    kahan_add(s, c, solid_angle_fast(p, mk(t[0], t[1], t[2]), mk(t[3], t[4], t[5]),
+                                                     mk(t[6], t[7], t[8]), amb));
+                }
+            }
+        }
+        float tot = s - c;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        amb = __any_sync(0xffffffffu, amb);
+        if (member == 0 && j < n) {
+            if (S > 1) {
+                partial[j * S + sl] = make_float2(tot, (v >= 0) ? (amb ? 1.0f : 0.0f) : 2.0f);
+            } else if (v >= 0) {
+                pairs += (unsigned long long)T;
+                const float aw = fabsf(tot * kInv4Pi);
+                if (amb || fabsf(aw - 0.5f) < kRecheckBand) {
+                    const unsigned long long r = atomicAdd(&ds->recheck_n, 1ull);
+                    if ((long long)r < recheck_cap) recheck[r] = v;
+                } else {
+                    consume(L, v, aw >= 0.5f, consumer, sbits, ds);
+                }
+            }
+        }
+    }
+    if (pairs) atomicAdd(&ds->gwn_pairs, pairs);
+}
+
+__global__ void gwn_sliced_final_kernel(long long T, Lattice L, const long long* __restrict__ list, long long cap,
+                                        int consumer, int only_if, uint32_t* __restrict__ sbits,
+                                        long long* __restrict__ recheck, long long recheck_cap, DevState* ds) {
+    if (only_if && !ds->patching) return;
+    const long long n = min((long long)ds->listed, cap);
+    const int S = team_slices(n, cap);
+    if (S == 1) return;
+    const float2* partial = reinterpret_cast<const float2*>(list + n);
+    unsigned long long pairs = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long v = list[i];
+        if (v < 0 || partial[i * S].y == 2.0f) continue;  // not listed, or decided on the surface
+        float tot = 0.0f;
+        bool amb = false;
+        for (int k = 0; k < S; ++k) {
+            const float2 q = partial[i * S + k];
+            tot += q.x;
+            amb |= q.y != 0.0f;
+        }
+        pairs += (unsigned long long)T;
+        const float aw = fabsf(tot * kInv4Pi);
+        if (amb || fabsf(aw - 0.5f) < kRecheckBand) {
+            const unsigned long long r = atomicAdd(&ds->recheck_n, 1ull);
+            if ((long long)r < recheck_cap) recheck[r] = v;
+        } else {
+            consume(L, v, aw >= 0.5f, consumer, sbits, ds);
+        }
+    }
+    if (pairs) atomicAdd(&ds->gwn_pairs, pairs);
+}
+
 // ---- hierarchical winding numbers (clusters of the 8^3 brick of each centroid) --------
 #ifndef GBSDF_FWN_BETA
 #define GBSDF_FWN_BETA 4.0f
@@ -873,13 +988,16 @@ void launch_gwn(const float* tri9, long long T, const Lattice& L, const long lon
     }
 }
 
-void launch_gwn_team(const float* tri9, long long T, const Lattice& L, const long long* list, long long list_cap,
+void launch_gwn_team(const float* tri9, long long T, const Lattice& L, long long* list, long long list_cap,
                      int consumer, uint32_t* sbits, long long* recheck, long long recheck_cap, const float* dist,
                      int dist_sq, float surf_tol_vox, DevState* ds, int num_sms, cudaStream_t st, int only_if) {
     GBSDF_COUNT_LAUNCH();
-    gwn_kernel<32><<<(unsigned)(num_sms * 8), kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, only_if,
-                                                                     sbits, recheck, recheck_cap, dist, dist_sq,
-                                                                     surf_tol_vox, ds);
+    gwn_sliced_kernel<<<(unsigned)(num_sms * 8), kGwnThreads, 0, st>>>(tri9, T, L, list, list_cap, consumer, only_if,
+                                                                         sbits, recheck, recheck_cap, dist, dist_sq,
+                                                                         surf_tol_vox, ds);
+    GBSDF_COUNT_LAUNCH();
+    gwn_sliced_final_kernel<<<16, 256, 0, st>>>(T, L, list, list_cap, consumer, only_if, sbits, recheck, recheck_cap,
+                                                ds);
 }
 
 FwnGrid fwn_grid(const Lattice& L, long long T) {
@@ -981,6 +1099,7 @@ void launch_winding(const Fwn* f, const float* tri9, long long T, const Lattice&
     // clusters at beta, clusters at kFwnBetaFine (smaller truncation bounds, more triangles
     // summed near the voxel), then the per-triangle sum
     long long* bufs[2] = {f->fb2, f->fb};
+    long long* left = nullptr;  // the last stage's leftovers
     int nb = 0;
     if (f->supers) {
         GBSDF_COUNT_LAUNCH();
@@ -1007,11 +1126,12 @@ void launch_winding(const Fwn* f, const float* tri9, long long T, const Lattice&
         GBSDF_COUNT_LAUNCH();
         fwn_handoff_kernel<<<1, 1, 0, st>>>(ds, only_if, f->fb_cap, cnt);
         list = out;
+        left = out;
         list_cap = f->fb_cap;
         ++nb;
         if (!f->fb2) break;  // one buffer: a single cluster stage
     }
-    launch_gwn_team(tri9, T, L, list, f->fb_cap, consumer, sbits, recheck, recheck_cap, dist, dist_sq, surf_tol_vox,
+    launch_gwn_team(tri9, T, L, left, f->fb_cap, consumer, sbits, recheck, recheck_cap, dist, dist_sq, surf_tol_vox,
                     ds, num_sms, st, only_if);
 }
 
