@@ -305,6 +305,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-mesh batched workload")
     ap.add_argument("--sweep-schedule", type=int, default=0,
                     help="force the eikonal sweep schedules, x + 10 w (profiling runs; 0 = autotuned)")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="only the planned 64-mesh batch in --mode, W + K runs (profiling runs)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -333,6 +335,27 @@ def main():
     modes = {"reference": gbsdf.MODE_REFERENCE, "exact-signs": gbsdf.MODE_EXACT_SIGNS, "exact": gbsdf.MODE_EXACT,
              "learned": gbsdf.MODE_LEARNED}
     mode = modes[args.mode]
+    if args.batch_only:
+        from gbsdf import meshgen
+
+        meshes = meshgen.batch_workload()
+        dm = [(torch.from_numpy(t).to(dev), hh, a, b) for t, hh, a, b in meshes]
+        outs = [torch.empty(int(np.prod(b.astype(np.int64) - a + 1)), dtype=torch.float32, device=dev)
+                for _, _, a, b in meshes]
+        vox = sum(int(o.numel()) for o in outs)
+        with gbsdf.Batch(dm, outs=outs, mode=mode, device=local) as bt:
+            for _ in range(args.warmup):
+                bt.run()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                bt.run()
+            torch.cuda.synchronize()
+            ms = (time.perf_counter() - t0) / args.steps * 1e3
+        if rank == 0:
+            print(json.dumps({"metric": "planned 64-mesh batch", "value": vox / (ms * 1e-3) / 1e9, "unit": UNIT,
+                              "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup, "mode": args.mode}))
+        return
     dims_override = tuple(int(x) for x in args.dims.split(",")) if args.dims else None
     tris, mn, mx, h = make_workload(dims_override, args.h, args.workload)
     mlp = None
