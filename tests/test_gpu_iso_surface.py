@@ -33,6 +33,9 @@ def test_random_and_sphere_grids(engine, oracle):
         g[rng.random(g.shape) < 0.05] = 0.0
         _check(engine, oracle, g, dims, 0.25, (-1.5, 2.0, 0.125), 0.0, table)
         _check(engine, oracle, g, dims, 0.25, (0.0, 0.0, 0.0), 0.3, table)
+        gn = g.copy()
+        gn[rng.random(g.shape) < 0.03] = np.nan  # NaN corners: outside, midpoint vertices
+        _check(engine, oracle, gn, dims, 0.25, (0.0, 0.0, 0.0), 0.0, table)
     n, h = 96, 0.05
     ax = (np.arange(n) - n / 2) * h
     z, y, x = np.meshgrid(ax, ax, ax, indexing="ij")

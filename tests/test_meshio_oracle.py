@@ -235,6 +235,10 @@ def ascii_stl_cases():
     # token in the last 7 bytes (ignored)
     yield (b"vertex 1 2 3\nvertex\t4 5 6 endvertex 7 7 7\n vertexx 9 9 9 xvertex 8 8 8\r\nvertex -1e1 .5 +2\n"
            b"\tvertex 1 2 3\n vertex 0 0 0\nvertex 3 2 1\nvertex 5 5 5\nvertex 6")
+    # a solid named "vertex ..." (the reference's rule reads it as a vertex token, its
+    # numbers as zeros), CR-only line ends, numbers with no digits and exponents (one underflowing to 0)
+    yield (b"solid vertex model\rfacet normal 0 0 1\r outer loop\r  vertex 1 2 3\r  vertex - + .\r"
+           b"  vertex 1e3 -2.5e-3 5e-324\r endloop\rendfacet\rendsolid vertex model\r")
 
 
 def test_ascii_stl_oracle_matches_python_restatement():
