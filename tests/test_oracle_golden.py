@@ -152,3 +152,68 @@ def test_dirty_mesh_gwn_open_box(oracle):
     w = oracle.gwn_points_f64(tris, pts.astype(np.float32))
     ok = np.where(inn, w >= 0.45, w < 0.35)
     assert ok.mean() >= 0.99
+
+
+def eikonal_fraction(grid, dims, mn, dx, R, seed=1337, n=55000, tol=0.02):
+    """The reference's eikonal property check, case (a) (harness_eikonal_cuda_tests.cpp:
+    55-129 with gpu_evaluate_eikonal_field_kernel, cuda_verification.cu:393-505, sample mode
+    0): n points on shells R + U(-3 dx, 3 dx) from the hash-seeded directions, the field
+    sampled trilinearly (dev_sample_sdf_trilinear, math_utils.cuh:344-389; 1000 outside),
+    central differences at dx / 2; returns the fraction with | |grad f| - 1 | <= tol."""
+    g = np.asarray(grid, np.float32).reshape(int(dims[2]), int(dims[1]), int(dims[0]))
+    i = np.arange(n, dtype=np.uint64)
+    s0 = (np.uint64(seed) + i * np.uint64(19997) + np.uint64(31)) & np.uint64(0xFFFFFFFF)
+    th = 2 * np.pi * _hash01(s0 + np.uint64(1))
+    cp = -1.0 + 2.0 * _hash01(s0 + np.uint64(2))
+    sp = np.sqrt(np.maximum(0.0, 1.0 - cp * cp))
+    r = R + (-3.0 * dx + 6.0 * dx * _hash01(s0 + np.uint64(3)))
+    p = np.stack([r * sp * np.cos(th), r * cp, r * sp * np.sin(th)], -1)
+    mn = np.asarray(mn, np.float64)
+
+    def f(q):
+        gq = q / dx - mn
+        i0 = np.floor(gq).astype(np.int64)
+        inside = np.all((i0 >= 0) & (i0 < np.asarray(dims)[None, :] - 1), axis=1)
+        i0c = np.clip(i0, 0, np.asarray(dims) - 2)
+        fr = gq - i0c
+        x0, y0, z0 = i0c[:, 0], i0c[:, 1], i0c[:, 2]
+        fx, fy, fz = fr[:, 0], fr[:, 1], fr[:, 2]
+        v = lambda a, b, c: g[z0 + c, y0 + b, x0 + a].astype(np.float64)
+        c00 = v(0, 0, 0) * (1 - fx) + v(1, 0, 0) * fx
+        c10 = v(0, 1, 0) * (1 - fx) + v(1, 1, 0) * fx
+        c01 = v(0, 0, 1) * (1 - fx) + v(1, 0, 1) * fx
+        c11 = v(0, 1, 1) * (1 - fx) + v(1, 1, 1) * fx
+        out = (c00 * (1 - fy) + c10 * fy) * (1 - fz) + (c01 * (1 - fy) + c11 * fy) * fz
+        return np.where(inside, out, 1000.0)
+
+    hh = 0.5 * dx
+    grad = []
+    for k in range(3):
+        e = np.zeros(3)
+        e[k] = hh
+        grad.append((f(p + e) - f(p - e)) / (2 * hh))
+    diff = np.abs(np.sqrt(grad[0] ** 2 + grad[1] ** 2 + grad[2] ** 2) - 1.0)
+    return float(np.mean(diff <= tol))
+
+
+def sphere_case(R=20.0, dx=0.35):
+    from gbsdf import meshgen
+
+    v, f = _sphere(R, 96, 96)
+    if meshgen.signed_volume(v, f) < 0:
+        f = f[:, [0, 2, 1]]
+    return v.astype(np.float32), f
+
+
+def test_eikonal_property_sphere(oracle):
+    """Harness case (a): sphere R = 20 mm (96 x 96 tessellation) at dx = 0.35 mm on the
+    build_from_mesh lattice; the reference passes it when at least 85% of the samples are
+    within 0.02 of |grad f| = 1. The oracle's reference-mode build does."""
+    from gbsdf import meshgen
+
+    v, f = sphere_case()
+    mn, mx = oracle.lattice(v, 0.35)
+    st, dist, _, _ = oracle.fast_sdf(meshgen.to_triangles(v, f), 0.35, mn, mx, fsm_mode=0, gwn_mode=1)
+    assert st == 0
+    frac = eikonal_fraction(dist, mx - mn + 1, mn, 0.35, 20.0)
+    assert frac >= 0.85, frac
