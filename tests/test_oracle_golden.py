@@ -154,6 +154,68 @@ def test_dirty_mesh_gwn_open_box(oracle):
     assert ok.mean() >= 0.99
 
 
+def _gwn_points(mode, seed):
+    """gpu_generate_gwn_test_points_kernel (cuda_verification.cu:209-263), modes 1 and 2."""
+    i = np.arange(10000, dtype=np.uint64)
+    s0 = (seed + i * 9973 + 17) & 0xFFFFFFFF
+    inn = i < 5000
+    pts = np.zeros((10000, 3))
+    if mode == 1:
+        r = np.where(inn, 13.5 * _hash01(s0 + 1), 16.5 + 18.5 * _hash01(s0 + 1))
+        u = -1.0 + 2.0 * _hash01(s0 + 2)
+        th = 2 * np.pi * _hash01(s0 + 3)
+        sq = np.sqrt(np.maximum(0.0, 1.0 - u * u))
+        pts = r[:, None] * np.stack([sq * np.cos(th), sq * np.sin(th), u], -1)
+        return pts, inn
+    pts[inn, 0] = -8.5 + 25.0 * _hash01(s0[inn] + 1)
+    pts[inn, 1] = -8.5 + 17.0 * _hash01(s0[inn] + 2)
+    pts[inn, 2] = -8.5 + 17.0 * _hash01(s0[inn] + 3)
+    for k in np.nonzero(~inn)[0]:
+        pts[k] = (28, 28, 28)
+        for att in range(64):
+            x = -35 + 70 * _hash01(s0[k] + att * 3 + 1)
+            y = -35 + 70 * _hash01(s0[k] + att * 3 + 2)
+            z = -35 + 70 * _hash01(s0[k] + att * 3 + 3)
+            if not (-12 <= x <= 20 and abs(y) <= 12 and abs(z) <= 12):
+                pts[k] = (x, y, z)
+                break
+    return pts, inn
+
+
+def test_dirty_mesh_gwn_inverted_sphere(oracle):
+    # harness_vessel_tests.cpp:77-83 + cuda_verification.cu:236-243, :266-281: a sphere
+    # (R 15, 48 x 48) with every winding flipped, oriented back by the orientation pre-pass;
+    # >= 99% of 10,000 points classified with in >= 0.50, out < 0.25
+    from gbsdf import meshgen
+
+    v, f = _sphere(15.0, 48, 48)
+    if meshgen.signed_volume(v, f) < 0:
+        f = f[:, [0, 2, 1]]
+    idx, orientable, inconsistent, inverted, vol = oracle.orient_mesh(v, f[:, [0, 2, 1]].astype(np.uint32))
+    assert orientable and inverted and vol > 0
+    pts, inn = _gwn_points(1, 1337)
+    w = oracle.gwn_points_f64(meshgen.to_triangles(v, idx.reshape(-1, 3)), pts.astype(np.float32))
+    ok = np.where(inn, w >= 0.50, w < 0.25)
+    assert ok.mean() >= 0.99
+
+
+def test_dirty_mesh_gwn_intersecting_cubes(oracle):
+    # harness_vessel_tests.cpp:85-102 + cuda_verification.cu:244-262, :266-281: two
+    # overlapping closed cubes; >= 99% of 10,000 points classified (in >= 0.45, out < 0.25)
+    from gbsdf import meshgen
+
+    c = np.array([[-10, -10, -10], [10, -10, -10], [10, 10, -10], [-10, 10, -10],
+                  [-10, -10, 10], [10, -10, 10], [10, 10, 10], [-10, 10, 10]], np.float32)
+    v = np.vstack([c, c + np.array([8, 0, 0], np.float32)])
+    q = np.array([0, 2, 1, 0, 3, 2, 4, 5, 6, 4, 6, 7, 0, 1, 5, 0, 5, 4,
+                  1, 2, 6, 1, 6, 5, 2, 3, 7, 2, 7, 6, 3, 0, 4, 3, 4, 7]).reshape(-1, 3)
+    f = np.vstack([q, q + 8])
+    pts, inn = _gwn_points(2, 9001)
+    w = oracle.gwn_points_f64(meshgen.to_triangles(v, f), pts.astype(np.float32))
+    ok = np.where(inn, w >= 0.45, w < 0.25)
+    assert ok.mean() >= 0.99
+
+
 def eikonal_fraction(grid, dims, mn, dx, R, seed=1337, n=55000, tol=0.02):
     """The reference's eikonal property check, case (a) (harness_eikonal_cuda_tests.cpp:
     55-129 with gpu_evaluate_eikonal_field_kernel, cuda_verification.cu:393-505, sample mode
