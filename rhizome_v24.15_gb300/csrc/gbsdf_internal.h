@@ -110,7 +110,7 @@ long long scan_tmp_elems(long long n);
 // Frees the iso-surface extractor's cached scratch of `device` (k_iso.cu).
 void release_iso_workspace(int device);
 // With `ds`, the pair lists are known to hold `cap_b` / `cap_s` entries: when the counts
-// of this build exceed them the fill writes nothing and sets ds->overflow (the splat and
+// of this SDF build exceed them the fill writes nothing and sets ds->overflow (the splat and
 // parity passes then skip the build).
 void launch_bin_fill(const SplatTri* stt, const ParTri* ptt, long long T, const Lattice& L,
                      const unsigned long long* brick_off, unsigned* brick_cur, unsigned* brick_list,
