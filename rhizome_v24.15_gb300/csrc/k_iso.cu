@@ -601,7 +601,8 @@ static int extract_iso(const float* grid, int32_t grid_on_device, const int32_t 
         cudaGetLastError();
         return e.set(GBSDF_ENODEV, "no CUDA device available");
     }
-    if (device < 0 || device >= ndev) return e.set(GBSDF_ENODEV, "device %d out of range", device);
+    if (device < 0 || device >= ndev || device >= 64)
+        return e.set(GBSDF_ENODEV, "device %d out of range", device);
     if (cudaSetDevice(device) != cudaSuccess) {
         cudaGetLastError();
         return e.set(GBSDF_ECUDA, "cudaSetDevice failed");
@@ -617,8 +618,8 @@ static int extract_iso(const float* grid, int32_t grid_on_device, const int32_t 
     if (groups > 0x7fffffffLL) return e.set(GBSDF_EINVAL, "lattice too large (%lld row groups)", groups);
     const IsoGeom G{dx, dy, dz, gpz, iso_value, iso_value + voxel_size};
     cudaError_t ce = cudaSuccess;
-    std::lock_guard<std::mutex> lock(g_iso[device & 63].mu);
-    IsoScratch s{g_iso[device & 63]};
+    std::lock_guard<std::mutex> lock(g_iso[device].mu);
+    IsoScratch s{g_iso[device]};
     // two passes over the same carving: sizing, then placing
     const float* g = grid;
     float* d_up = nullptr;
@@ -651,6 +652,8 @@ static int extract_iso(const float* grid, int32_t grid_on_device, const int32_t 
     iso_count_kernel<<<(unsigned)groups, kIsoThreads, 0, st>>>(g, G, d_mask, d_tv, d_tt);
     launch_exclusive_scan(d_tv, d_pv, tiles, d_scan, 0, st);
     launch_exclusive_scan(d_tt, d_pt, tiles, d_scan, 0, st);
+    ce = cudaGetLastError();  // launch errors are not reported by the synchronisation
+    if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "iso-surface count launch: %s", cudaGetErrorString(ce));
     unsigned long long pv = 0, pt = 0;
     unsigned lv = 0, lt = 0;
     cudaMemcpyAsync(&pv, d_pv + (tiles - 1), 8, cudaMemcpyDeviceToHost, st);
@@ -669,7 +672,7 @@ static int extract_iso(const float* grid, int32_t grid_on_device, const int32_t 
         return GBSDF_OK;
     }
     if (outputs == 2) {  // library-owned: grow the cache's mesh region
-        IsoCache& c = g_iso[device & 63];
+        IsoCache& c = g_iso[device];
         const size_t vb = ((size_t)V * 12 + 255) & ~size_t(255), need = vb + (size_t)T * 12;
         if (need > c.out_bytes) {
             if (c.out) cudaFree(c.out);
@@ -715,7 +718,8 @@ static int extract_iso(const float* grid, int32_t grid_on_device, const int32_t 
                                                                d_pv, d_vbase, d_v);
     GBSDF_COUNT_LAUNCH();
     iso_triangle_kernel<<<(unsigned)groups, kIsoThreads, 0, st>>>(g, G, d_mask, d_vbase, d_pt, d_i);
-    if (!outputs_on_device) {
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess && !outputs_on_device) {
         ce = cudaMemcpyAsync(out_vertices, d_v, (size_t)V * 12, cudaMemcpyDeviceToHost, st);
         if (ce == cudaSuccess) ce = cudaMemcpyAsync(out_indices, d_i, (size_t)T * 12, cudaMemcpyDeviceToHost, st);
     }
