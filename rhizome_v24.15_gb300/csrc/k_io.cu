@@ -492,7 +492,8 @@ int gbsdf_parse_binary_stl(const uint8_t* bytes, size_t n_bytes, float* out_vert
     cudaMemcpyAsync(&flast, d_first + (n - 1), 4, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&tl, d_tpos + (T - 1), 8, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&klast, d_keep + (T - 1), 4, cudaMemcpyDeviceToHost, st);
-    ce = cudaStreamSynchronize(st);
+    ce = cudaGetLastError();  // launch errors are not reported by the synchronisation
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "STL decode: %s", cudaGetErrorString(ce));
     const long long V = (long long)fl + flast, nt = (long long)tl + klast;
     ce = cudaMemcpy(out_vertices, d_outv, (size_t)V * 12, cudaMemcpyDeviceToHost);
@@ -546,7 +547,8 @@ int gbsdf_parse_obj(const char* text, size_t n_bytes, float* out_vertices, int64
     cudaMemcpyAsync(&pf, d_pf + (n - 1), 8, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&lv, d_fv + (n - 1), 4, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&lf, d_ff + (n - 1), 4, cudaMemcpyDeviceToHost, st);
-    ce = cudaStreamSynchronize(st);
+    ce = cudaGetLastError();  // launch errors are not reported by the synchronisation
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "OBJ scan: %s", cudaGetErrorString(ce));
     const long long V = std::min<long long>((long long)pv + lv, cap);
     const long long F = std::min<long long>((long long)pf + lf, cap);
@@ -571,7 +573,8 @@ int gbsdf_parse_obj(const char* text, size_t n_bytes, float* out_vertices, int64
     unsigned tlast = 0;
     cudaMemcpyAsync(&tl, d_tp + (F - 1), 8, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&tlast, d_nt + (F - 1), 4, cudaMemcpyDeviceToHost, st);
-    ce = cudaStreamSynchronize(st);
+    ce = cudaGetLastError();  // launch errors are not reported by the synchronisation
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "OBJ faces: %s", cudaGetErrorString(ce));
     const long long NT = (long long)tl + tlast;
     if (NT == 0) return e.set(GBSDF_EINVAL, "OBJ text holds no triangle or quad face");
@@ -584,7 +587,8 @@ int gbsdf_parse_obj(const char* text, size_t n_bytes, float* out_vertices, int64
     }
     GBSDF_COUNT_LAUNCH();
     obj_face_write_kernel<<<blocks_for(F), 256, 0, st>>>(d_text, d_fo, F, (int)V, d_tp, d_i);
-    ce = cudaMemcpy(out_vertices, d_v, (size_t)V * 12, cudaMemcpyDeviceToHost);
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaMemcpy(out_vertices, d_v, (size_t)V * 12, cudaMemcpyDeviceToHost);
     if (ce == cudaSuccess) ce = cudaMemcpy(out_indices, d_i, (size_t)NT * 12, cudaMemcpyDeviceToHost);
     if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "OBJ download: %s", cudaGetErrorString(ce));
     *n_vertices = V;
@@ -638,7 +642,8 @@ int gbsdf_parse_ascii_stl(const char* text, size_t n_bytes, float* out_vertices,
     unsigned fl = 0;
     cudaMemcpyAsync(&pl, d_pos + (n - 1), 8, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&fl, d_fl + (n - 1), 4, cudaMemcpyDeviceToHost, st);
-    ce = cudaStreamSynchronize(st);
+    ce = cudaGetLastError();  // launch errors are not reported by the synchronisation
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "ASCII STL scan: %s", cudaGetErrorString(ce));
     const long long tokens = std::min<long long>((long long)pl + fl, cap);
     const long long m = tokens - tokens % 3;  // whole facets
@@ -677,7 +682,8 @@ int gbsdf_parse_ascii_stl(const char* text, size_t n_bytes, float* out_vertices,
     unsigned vlast = 0;
     cudaMemcpyAsync(&vl, d_fpos + (m - 1), 8, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&vlast, d_first + (m - 1), 4, cudaMemcpyDeviceToHost, st);
-    ce = cudaStreamSynchronize(st);
+    ce = cudaGetLastError();  // launch errors are not reported by the synchronisation
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) return e.set(GBSDF_ECUDA, "ASCII STL weld: %s", cudaGetErrorString(ce));
     const long long V = (long long)vl + vlast;
     ce = cudaMemcpy(out_vertices, d_outv, (size_t)V * 12, cudaMemcpyDeviceToHost);
