@@ -4,7 +4,8 @@
 // of the jittered column ray from a host-built 4x4-supercell CSR, sorts them and
 // writes one byte per voxel with column-strided stores (cuda_rasterizer.cu:279-368,
 // CSR :824-882). Here one warp owns a strip of 32 adjacent columns of one row: the
-// strip's candidate list is walked uniformly by the warp, each lane keeps its own
+// strip's candidate list is filtered 32 entries at a time by the part of the test the
+// lanes share (the row), the survivors are walked uniformly by the warp, each lane keeps its own
 // crossings in shared memory, and the inside/outside state of the 32 lanes at each
 // z is packed into one 32-bit sign word with __ballot_sync -- one store per warp
 // per z, bit-packed signs (1 bit per voxel) instead of bytes.
@@ -57,28 +58,44 @@ __global__ void __launch_bounds__(kParWarps * 32) parity_kernel(const ParTri* __
     bool bad = false;
     const unsigned long long o = off[strip];
     const unsigned n = cnt[strip];
-    for (unsigned e = 0; e < n; ++e) {
-        const ParTri& p = ptt[list[o + e]];
-        if (!col || bad) continue;
-        if (supx < p.sx0 || supx > p.sx1 || supy < p.sy0 || supy > p.sy1) continue;
-        const float4 ab = *reinterpret_cast<const float4*>(p.xyab);
-        if (rx < ab.x || rx > ab.z || ry < ab.y || ry > ab.w) continue;
-        const float* v = p.v;
-        float d0 = (v[3] - v[0]) * (ry - v[1]) - (v[4] - v[1]) * (rx - v[0]);
-        float d1 = (v[6] - v[3]) * (ry - v[4]) - (v[7] - v[4]) * (rx - v[3]);
-        float d2 = (v[0] - v[6]) * (ry - v[7]) - (v[1] - v[7]) * (rx - v[6]);
-        bool pos = (d0 > 0.0f && d1 > 0.0f && d2 > 0.0f);
-        bool neg = (d0 < 0.0f && d1 < 0.0f && d2 < 0.0f);
-        if (!pos && !neg) continue;
-        float area2 = d0 + d1 + d2;
-        if (fabsf(area2) < 1e-12f) continue;
-        float zh = (d1 * v[2] + d2 * v[5] + d0 * v[8]) / area2;
-        if (nh < kParityMaxHits) {
-            hits[nh * 32 + lane] = zh;
-            if (SIGNED) hsg[nh * 32 + lane] = neg ? 1 : -1;
-            ++nh;
-        } else {
-            bad = true;
+    for (unsigned e0 = 0; e0 < n; e0 += 32) {
+        // The row part of the candidate test is the same for the 32 lanes (one row y): each
+        // lane tests one list entry, and the warp walks only the entries that pass, in list
+        // order. The test is the negated skip condition, so a NaN bound passes as before.
+        unsigned tri = 0;
+        bool row = false;
+        if (e0 + lane < n) {
+            tri = list[o + e0 + lane];
+            const int4 sr = *reinterpret_cast<const int4*>(&ptt[tri].sx0);
+            const float4 ab = *reinterpret_cast<const float4*>(ptt[tri].xyab);
+            row = !(supy < sr.z || supy > sr.w || ry < ab.y || ry > ab.w);
+        }
+        unsigned rows = __ballot_sync(0xffffffffu, row);
+        while (rows) {
+            const int src = __ffs(rows) - 1;
+            rows &= rows - 1;
+            const ParTri& p = ptt[__shfl_sync(0xffffffffu, tri, src)];
+            if (!col || bad) continue;
+            if (supx < p.sx0 || supx > p.sx1) continue;
+            const float4 ab = *reinterpret_cast<const float4*>(p.xyab);
+            if (rx < ab.x || rx > ab.z) continue;
+            const float* v = p.v;
+            float d0 = (v[3] - v[0]) * (ry - v[1]) - (v[4] - v[1]) * (rx - v[0]);
+            float d1 = (v[6] - v[3]) * (ry - v[4]) - (v[7] - v[4]) * (rx - v[3]);
+            float d2 = (v[0] - v[6]) * (ry - v[7]) - (v[1] - v[7]) * (rx - v[6]);
+            bool pos = (d0 > 0.0f && d1 > 0.0f && d2 > 0.0f);
+            bool neg = (d0 < 0.0f && d1 < 0.0f && d2 < 0.0f);
+            if (!pos && !neg) continue;
+            float area2 = d0 + d1 + d2;
+            if (fabsf(area2) < 1e-12f) continue;
+            float zh = (d1 * v[2] + d2 * v[5] + d0 * v[8]) / area2;
+            if (nh < kParityMaxHits) {
+                hits[nh * 32 + lane] = zh;
+                if (SIGNED) hsg[nh * 32 + lane] = neg ? 1 : -1;
+                ++nh;
+            } else {
+                bad = true;
+            }
         }
     }
     // insertion sort of this lane's crossings (with their signs)
