@@ -2,6 +2,7 @@
 against an independent numpy restatement, the OBJ decode against the source mesh, and --
 where the reference tree is present -- the reference's own mug specimen against the facts
 its documentation states (1,553 vertices, 3,106 triangles, 100.0 x 76.5 x 85.0 mm)."""
+import os
 from pathlib import Path
 
 import numpy as np
@@ -75,7 +76,8 @@ def test_obj_decode_matches_source_mesh():
     assert st == 0 and oi.tolist() == [0, 1, 2, 0, 2, 3, 0, 8, 1]
 
 
-REF_MUG = Path("/root/reference/native/assets/mug.obj")
+# the reference tree, where present (the same variable and default as oracle/build_ref.sh)
+REF_MUG = Path(os.environ.get("RHIZOME_REFERENCE", "/root/reference")) / "native/assets/mug.obj"
 
 
 @pytest.mark.skipif(not REF_MUG.exists(), reason="the reference tree is not present")
