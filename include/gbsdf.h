@@ -218,8 +218,9 @@ int gbsdf_build_from_mesh(const float* verts, int64_t n_verts, const uint32_t* i
 
 /* Brick features of the learned sign-risk model for one lattice (8^3 bricks, x fastest):
  * GBSDF_MLP_FEATURES floats per brick written to `features_dev` (device memory,
- * capacity_bricks bricks). n_bricks[3] receives the brick grid. No counterpart in the
- * reference. */
+ * capacity_bricks bricks). n_bricks[3] receives the brick grid. The work runs on the device
+ * that holds features_dev; device triangles (tris_on_device = 1) must be on that device too
+ * (GBSDF_EINVAL otherwise). No counterpart in the reference. */
 int gbsdf_brick_features(const gbsdf_tri* tris, int64_t n_tris, float voxel_size, const int32_t min_coord[3],
                          const int32_t max_coord[3], int32_t tris_on_device, float* features_dev,
                          int64_t capacity_bricks, int32_t n_bricks[3], char* err, size_t errlen);
@@ -356,7 +357,10 @@ void gbsdf_release_workspace(int32_t device);
  * make that first call before any stream capture. Every call shares the array, so two
  * calls whose GPU work overlapped would race; the entry point takes a process-wide lock
  * and synchronises `stream` (a cudaStream_t, NULL = legacy default stream) before it
- * returns. */
+ * returns. Unlike the other entry points it builds in place: squared distances are
+ * written to `out_dev` before the sign kernels run, so a GBSDF_ECUDA returned after the
+ * first launch can leave `out_dev` partly written (argument and limit errors leave it
+ * untouched). */
 int gbsdf_legacy_sdf_noalloc(const gbsdf_tri* tris_dev, int64_t n_tris, float voxel_size,
                              const int32_t min_coord[3], const int32_t max_coord[3], float* out_dev,
                              int32_t device, void* stream, gbsdf_stats* stats, char* err, size_t errlen);

@@ -116,6 +116,9 @@ T* P(Buf& b) {
     return static_cast<T*>(b.p);
 }
 
+// Creates the workspace's stream, events and device-state buffers on `device`. On a
+// failure part-way the handles created so far are released again, so a retry starts
+// clean and nothing leaks.
 int init_ws(Workspace& w, int device, Err& e) {
     if (w.device == device) return GBSDF_OK;
     int n = 0;
@@ -124,12 +127,31 @@ int init_ws(Workspace& w, int device, Err& e) {
         return e.set(GBSDF_ENODEV, "no CUDA device available");
     }
     if (device < 0 || device >= n) return e.set(GBSDF_ENODEV, "device %d out of range (%d devices)", device, n);
-    GB_CK(cudaSetDevice(device));
-    GB_CK(cudaDeviceGetAttribute(&w.num_sms, cudaDevAttrMultiProcessorCount, device));
-    GB_CK(cudaStreamCreateWithFlags(&w.st, cudaStreamNonBlocking));
-    for (auto& ev : w.ev) GB_CK(cudaEventCreate(&ev));
-    GB_CK(cudaMalloc(&w.ds, sizeof(DevState)));
-    GB_CK(cudaMallocHost(&w.hs, sizeof(DevState)));
+    auto undo = [&w]() {
+        for (auto& ev : w.ev) {
+            if (ev) cudaEventDestroy(ev);
+            ev = nullptr;
+        }
+        if (w.st) cudaStreamDestroy(w.st);
+        if (w.ds) cudaFree(w.ds);
+        if (w.hs) cudaFreeHost(w.hs);
+        w.st = nullptr;
+        w.ds = nullptr;
+        w.hs = nullptr;
+    };
+    cudaError_t err = cudaSetDevice(device);
+    if (err == cudaSuccess) err = cudaDeviceGetAttribute(&w.num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&w.st, cudaStreamNonBlocking);
+    for (auto& ev : w.ev)
+        if (err == cudaSuccess) err = cudaEventCreate(&ev);
+    if (err == cudaSuccess) err = cudaMalloc(&w.ds, sizeof(DevState));
+    if (err == cudaSuccess) err = cudaMallocHost(&w.hs, sizeof(DevState));
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        undo();
+        return e.set(err == cudaErrorMemoryAllocation ? GBSDF_ENOMEM : GBSDF_ECUDA, "workspace set-up on device %d: %s",
+                     device, cudaGetErrorString(err));
+    }
     w.device = device;
     return GBSDF_OK;
 }
@@ -802,8 +824,12 @@ int gbsdf_build_from_mesh(const float* verts, int64_t n_verts, const uint32_t* i
         GB_CK(cudaMalloc(&tris_dev, (size_t)kept * 48));
         launch_tri_scatter(P<float>(w.verts), n_verts, P<uint32_t>(w.idx), nt, P<unsigned long long>(w.fpos),
                            tris_dev, st);
-        GB_CK(cudaGetLastError());
-        GB_CK(cudaStreamSynchronize(st));
+        cudaError_t se = cudaGetLastError();
+        if (se == cudaSuccess) se = cudaStreamSynchronize(st);
+        if (se != cudaSuccess) {
+            cudaFree(tris_dev);
+            return e.set(GBSDF_ECUDA, "triangle build: %s", cudaGetErrorString(se));
+        }
     }
     o.tris_on_device = 1;
     int rc = compute(tris_dev, kept, true, voxel_size, min_coord, max_coord, out, out_on_device != 0, o, stats, e);
@@ -826,15 +852,41 @@ int gbsdf_brick_features(const gbsdf_tri* tris, int64_t n_tris, float voxel_size
         for (int k = 0; k < 3; ++k) n_bricks[k] = L.nb[k];
     if (L.nbricks > capacity_bricks) return e.set(GBSDF_EINVAL, "feature buffer holds %lld bricks, need %lld",
                                                   (long long)capacity_bricks, L.nbricks);
+    // The features are computed on the device that holds features_dev; device triangles
+    // must live on that device too.
+    int device = 0;
+    {
+        cudaPointerAttributes fa{};
+        if (cudaPointerGetAttributes(&fa, features_dev) != cudaSuccess || fa.type != cudaMemoryTypeDevice) {
+            cudaGetLastError();
+            return e.set(GBSDF_EINVAL, "features_dev is not device memory");
+        }
+        device = fa.device;
+        if (tris_on_device) {
+            cudaPointerAttributes ta{};
+            if (cudaPointerGetAttributes(&ta, tris) != cudaSuccess || ta.type != cudaMemoryTypeDevice ||
+                ta.device != device) {
+                cudaGetLastError();
+                return e.set(GBSDF_EINVAL, "device triangles must be on the device of features_dev (%d)", device);
+            }
+        }
+    }
+    if (device < 0 || device >= 64) return e.set(GBSDF_ENODEV, "device %d out of range", device);
     gbsdf_options o;
     gbsdf_default_options(&o);
     o.mode = GBSDF_MODE_REFERENCE;
     o.tris_on_device = tris_on_device;
-    Workspace& w = g_ws[0];
+    o.device = device;
+    Workspace* wp;
+    {
+        std::lock_guard<std::mutex> g(g_ws_mu);
+        wp = &g_ws[device];
+    }
+    Workspace& w = *wp;
     std::lock_guard<std::mutex> lk(w.mu);
-    int rc = init_ws(w, 0, e);
+    int rc = init_ws(w, device, e);
     if (rc != GBSDF_OK) return rc;
-    GB_CK(cudaSetDevice(0));
+    GB_CK(cudaSetDevice(device));
     GB_CK(ensure(w.t12, (size_t)n_tris * 48));
     GB_CK(cudaMemcpyAsync(w.t12.p, tris, (size_t)n_tris * 48,
                           tris_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, w.st));
@@ -843,15 +895,16 @@ int gbsdf_brick_features(const gbsdf_tri* tris, int64_t n_tris, float voxel_size
     return run_fast(w, n_tris, L, o, nullptr, true, nullptr, e, features_dev);
 }
 
+// The workspace of `device` for the MLP entry points; the caller takes its lock and then
+// calls init_ws under it, as compute() does.
 static Workspace* mlp_ws(int32_t device, Err& e, int& rc) {
     rc = GBSDF_OK;
     if (device < 0 || device >= 64) {
         rc = e.set(GBSDF_ENODEV, "device %d out of range", device);
         return nullptr;
     }
-    Workspace& w = g_ws[device];
-    rc = init_ws(w, device, e);
-    return rc == GBSDF_OK ? &w : nullptr;
+    std::lock_guard<std::mutex> g(g_ws_mu);
+    return &g_ws[device];
 }
 
 int gbsdf_mlp_forward(const float* params_dev, const float* features_dev, int64_t n, float* logits_dev,
@@ -862,6 +915,8 @@ int gbsdf_mlp_forward(const float* params_dev, const float* features_dev, int64_
     Workspace* w = mlp_ws(device, e, rc);
     if (!w) return rc;
     std::lock_guard<std::mutex> lk(w->mu);
+    rc = init_ws(*w, device, e);
+    if (rc != GBSDF_OK) return rc;
     GB_CK(cudaSetDevice(device));
     launch_mlp_forward(params_dev, features_dev, n, logits_dev, w->st);
     GB_CK(cudaGetLastError());
@@ -879,6 +934,8 @@ int gbsdf_mlp_backward(const float* params_dev, const float* features_dev, const
     Workspace* w = mlp_ws(device, e, rc);
     if (!w) return rc;
     std::lock_guard<std::mutex> lk(w->mu);
+    rc = init_ws(*w, device, e);
+    if (rc != GBSDF_OK) return rc;
     GB_CK(cudaSetDevice(device));
     const int parts = mlp_backward_parts(n);
     GB_CK(ensure(w->mparts, (size_t)parts * kMlpParams * 4));
@@ -898,6 +955,8 @@ int gbsdf_mlp_adam(float* params_dev, const float* grad_dev, float* m_dev, float
     Workspace* w = mlp_ws(device, e, rc);
     if (!w) return rc;
     std::lock_guard<std::mutex> lk(w->mu);
+    rc = init_ws(*w, device, e);
+    if (rc != GBSDF_OK) return rc;
     GB_CK(cudaSetDevice(device));
     launch_adam(params_dev, grad_dev, m_dev, v_dev, kMlpParams, lr, beta1, beta2, eps, grad_scale, step, w->st);
     GB_CK(cudaGetLastError());
