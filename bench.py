@@ -257,10 +257,35 @@ def cpu_baseline(tris, mn, mx, h, z_slab=64, threads=None):
     t0 = time.perf_counter()
     status, _, _, st = O.fast_sdf(tris, h, smn, smx, fsm_mode=0, gwn_mode=0, threads=threads)
     dt = time.perf_counter() - t0
-    desc = (f"reference fast path restated on CPU (oracle, {threads} threads), {n} voxels: "
-            f"z-slab {z_slab} of {int(mx[2] - mn[2] + 1)} planes of the 860x860x880 lattice, all "
-            f"{len(tris)} triangles, 8 FSM rounds, 3x4096 probes; status {status}")
+    desc = (f"reference fast path restated on CPU (oracle, {threads} threads), extrapolated from a {z_slab}-plane "
+            f"z-slab ({n} voxels, {z_slab} of {int(mx[2] - mn[2] + 1)} planes of the 860x860x880 lattice, all "
+            f"{len(tris)} triangles, 8 FSM rounds, 3x4096 probes; status {status}) to voxels per second")
     return n / dt / 1e9, dt, desc, threads
+
+
+def run_reference_gpu(tris, mn, mx, h, runs=2):
+    """The reference's own fast path (cuda_rasterizer.cu:796-1159, compiled for sm_103a with
+    its own nvcc flags into oracle/_ref by oracle/build_ref.sh) on this GPU, forced at the
+    bench lattice: its own timer (host clock around its allocations, triangle upload, build
+    and grid download), after one untimed run. A reported figure, not the target; None when
+    the library was not built."""
+    from oracle import ref_gpu as R
+
+    if not R.available():
+        return None
+    ms, wall, ok, st = [], [], False, {}
+    for i in range(runs):
+        t0 = time.perf_counter()
+        ok, _, m, st, _ = R.fast_sdf(tris, h, mn, mx)
+        if i > 0:
+            ms.append(m)
+            wall.append((time.perf_counter() - t0) * 1e3)
+    n = int(np.prod(mx.astype(np.int64) - mn + 1))
+    m = float(np.mean(ms))
+    return {"value": n / (m * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": m, "wall_ms": float(np.mean(wall)),
+            "accepted": bool(ok), "stats": st,
+            "what": "the reference's own CUDA fast path built for sm_103a with its own flags, host-buffer "
+                    "in/out (its own timer: allocations, triangle upload, build, grid download)"}
 
 
 def run_reference_arm(args, rank, world):
@@ -464,8 +489,8 @@ def main():
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "alg_bytes_per_launch": alg_bytes, "launch_ms": per_launch_ms,
-                         "note": "issue-bound below the HBM roof: 66-81 instructions per voxel at 70-77% "
-                                 "issue-active (profiles/sweeps_vec_mug_600x608x608.md)"},
+                         "note": "8 algorithmic bytes per voxel per directional sweep; achieved = those bytes "
+                                 "over the mean CUDA-event time per sweep of the timed builds"},
             "stages_ms": {k: round(float(np.mean([s[k] for s in stats])), 3)
                           for k in ("ms_prep", "ms_splat", "ms_parity", "ms_fixup", "ms_eikonal", "ms_verify",
                                     "ms_apply")},
@@ -482,6 +507,8 @@ def main():
         line["iso_surface"] = run_iso(gbsdf, out_dev, dims, h, mn, args.steps)
     if not args.no_batch and mode in (gbsdf.MODE_REFERENCE, gbsdf.MODE_EXACT_SIGNS):
         line["batched"] = run_batched(gbsdf, torch, dev, mode, args.steps, args.warmup, local)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == WORKLOAD:
+        line["reference_gpu"] = run_reference_gpu(tris, mn, mx, h)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, dt, desc, threads = cpu_baseline(tris, mn, mx, h)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc,

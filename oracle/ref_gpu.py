@@ -45,6 +45,8 @@ def lib():
         for name in ("refgpu_ptd_batch", "refgpu_solid_angle_batch"):
             getattr(L, name).argtypes = [P, P, LL, P]
             getattr(L, name).restype = I
+        L.refgpu_sweep.argtypes = [P, P, F, I, I]
+        L.refgpu_sweep.restype = I
         L.refgpu_godunov_batch.argtypes = [P, F, LL, P]
         L.refgpu_godunov_batch.restype = I
         _lib = L
@@ -140,6 +142,16 @@ def fixup(tris, h, mn, dims, sign):
     k = lib().refgpu_fixup(_p(t), T, C.c_float(h), _p(_ivec(mn)), _p(dims), _p(s))
     assert k >= 0, "CUDA error in the reference fixup driver"
     return int(k), s
+
+
+def sweep(grid, dims, h, axis, direction):
+    """One directional sweep of gpu_eikonal_fsm_sweep_kernel (RAST:433-513) on a copy of
+    `grid`; returns (changed flag, grid). Schedule-independent only when cross-line
+    neighbours cannot change during the sweep."""
+    g = np.ascontiguousarray(grid, np.float32).copy()
+    ch = lib().refgpu_sweep(_p(g), _p(_ivec(dims)), C.c_float(h), int(axis), int(direction))
+    assert ch >= 0, "CUDA error in the reference sweep driver"
+    return int(ch), g
 
 
 def ptd_batch(pts, tris9):

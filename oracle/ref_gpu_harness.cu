@@ -291,6 +291,36 @@ long long refgpu_fixup(const void* tris, int n_tris, float h, const int* mn, con
     return ok ? fixed : -1;
 }
 
+// [D]: one directional sweep of the reference's gpu_eikonal_fsm_sweep_kernel on `grid`
+// (in place, host memory), launched as cuda_rasterizer.cu:993-1001. Its lines read each
+// other's cells while they change, so only grids whose cross-line neighbours cannot
+// change during the sweep give a schedule-independent result. Returns the changed flag,
+// -1 on a CUDA error.
+int refgpu_sweep(float* grid, const int* dims, float h, int axis, int dir) {
+    size_t total = (size_t)dims[0] * dims[1] * dims[2];
+    float* d = nullptr;
+    int* d_flag = nullptr;
+    int ok = cuda_ok(cudaMalloc(&d, total * sizeof(float))) && cuda_ok(cudaMalloc(&d_flag, sizeof(int)));
+    if (ok)
+        ok = cuda_ok(cudaMemcpy(d, grid, total * sizeof(float), cudaMemcpyHostToDevice)) &&
+             cuda_ok(cudaMemset(d_flag, 0, sizeof(int)));
+    int changed = 0;
+    if (ok) {
+        const int THREADS = 256;
+        int n_lines = axis == 0 ? dims[1] * dims[2] : (axis == 1 ? dims[0] * dims[2] : dims[0] * dims[1]);
+        unsigned blocks = (unsigned)((n_lines + THREADS - 1) / THREADS);
+        rhizome::gpu_eikonal_fsm_sweep_kernel<<<blocks, THREADS>>>(d, dims[0], dims[1], dims[2], h, axis, dir,
+                                                                   d_flag);
+        ok = cuda_ok(cudaGetLastError()) && cuda_ok(cudaDeviceSynchronize());
+    }
+    if (ok)
+        ok = cuda_ok(cudaMemcpy(grid, d, total * sizeof(float), cudaMemcpyDeviceToHost)) &&
+             cuda_ok(cudaMemcpy(&changed, d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    cudaFree(d);
+    cudaFree(d_flag);
+    return ok ? changed : -1;
+}
+
 // The reference's device primitives as compiled with its flags, element-wise.
 int refgpu_ptd_batch(const float* pts, const float* tris9, long long n, float* out) {
     return run_elementwise(0, pts, (size_t)n * 3, tris9, (size_t)n * 9, 0.0f, n, out);

@@ -224,19 +224,30 @@ static double gwn_value_d(const OTri* tris, int T, V3 p) {
     return sd / (4.0 * 3.14159265358979323846);
 }
 
-// Godunov update, RAST:405-425 (identical arithmetic, no contraction)
+// Godunov update, RAST:405-425, with the roundings the reference's own build gives it.
+// nvcc compiles the reference with its default FMA contraction (native/CMakeLists.txt
+// sets no -fmad flag), which fuses two of the products into their sums inside the sweep
+// kernel: disc = fma(2h, h, -(d*d)) with d = s1 - s0, and the 3D pairwise sum
+// S = fma(e2, e2, fma(e1, e1, d*d)) with e1 = s2 - s1, e2 = s2 - s0; 3h^2 - S/2 keeps
+// separate roundings (3h*h is formed once per thread). Pinned bit for bit against the
+// reference's gpu_eikonal_fsm_sweep_kernel compiled with its own flags, on sweeps whose
+// cross-line neighbours cannot change (tests/test_gpu_reference_gpu.py). std::fma rounds
+// once on every host, so the restatement is exact on x86 and Arm alike.
 static inline float godunov(float ax, float ay, float az, float h) {
     float s0 = std::fmin(ax, std::fmin(ay, az));
     float s2 = std::fmax(ax, std::fmax(ay, az));
     float s1 = ax + ay + az - s0 - s2;
     float updated = s0 + h;
     if (updated > s1) {
-        float disc = 2.0f * h * h - (s1 - s0) * (s1 - s0);
+        const float d = s1 - s0;
+        const float dd = d * d;
+        float disc = std::fma(2.0f * h, h, -dd);
         if (disc >= 0.0f) {
             updated = (s0 + s1 + std::sqrt(disc)) * 0.5f;
             if (updated > s2) {
-                float disc3 = 3.0f * h * h -
-                              ((s1 - s0) * (s1 - s0) + (s2 - s1) * (s2 - s1) + (s2 - s0) * (s2 - s0)) * 0.5f;
+                const float e1 = s2 - s1, e2 = s2 - s0;
+                const float S = std::fma(e2, e2, std::fma(e1, e1, dd));
+                float disc3 = 3.0f * h * h - S * 0.5f;
                 if (disc3 >= 0.0f) updated = (s0 + s1 + s2 + std::sqrt(disc3)) / 3.0f;
             }
         }
@@ -497,15 +508,17 @@ long long orc_parity_signs_mode(const void* tris_, int T, float h, const int* mn
                 const float* ab = &xyab[4 * (size_t)ti];
                 if (rx < ab[0] || rx > ab[2] || ry < ab[1] || ry > ab[3]) continue;
                 const OTri& tr = tris[ti];
-                float d0 = (tr.v1.x - tr.v0.x) * (ry - tr.v0.y) - (tr.v1.y - tr.v0.y) * (rx - tr.v0.x);
-                float d1 = (tr.v2.x - tr.v1.x) * (ry - tr.v1.y) - (tr.v2.y - tr.v1.y) * (rx - tr.v1.x);
-                float d2 = (tr.v0.x - tr.v2.x) * (ry - tr.v2.y) - (tr.v0.y - tr.v2.y) * (rx - tr.v2.x);
+                // the reference's build contracts a*b - c*d to fma(a, b, -(c*d)) and the hit
+                // height's sum to fma(d0, z2, fma(d1, z0, d2*z1))
+                float d0 = std::fma(tr.v1.x - tr.v0.x, ry - tr.v0.y, -((tr.v1.y - tr.v0.y) * (rx - tr.v0.x)));
+                float d1 = std::fma(tr.v2.x - tr.v1.x, ry - tr.v1.y, -((tr.v2.y - tr.v1.y) * (rx - tr.v1.x)));
+                float d2 = std::fma(tr.v0.x - tr.v2.x, ry - tr.v2.y, -((tr.v0.y - tr.v2.y) * (rx - tr.v2.x)));
                 bool pos = (d0 > 0.0f && d1 > 0.0f && d2 > 0.0f);
                 bool neg = (d0 < 0.0f && d1 < 0.0f && d2 < 0.0f);
                 if (!pos && !neg) continue;
                 float area2 = d0 + d1 + d2;
                 if (std::fabs(area2) < 1e-12f) continue;
-                float zh = (d1 * tr.v0.z + d2 * tr.v1.z + d0 * tr.v2.z) / area2;
+                float zh = std::fma(d0, tr.v2.z, std::fma(d1, tr.v0.z, d2 * tr.v1.z)) / area2;
                 if (nh < kParityMaxHits) {
                     hsg[nh] = neg ? 1 : -1;
                     hit[nh++] = zh;

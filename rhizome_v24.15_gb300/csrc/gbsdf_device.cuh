@@ -142,22 +142,71 @@ __device__ __forceinline__ float div3_rn(float x) {
     return (r == 0.0f || !(fabsf(q) < __int_as_float(0x7f800000))) ? q : __fmaf_rn(r, r3, q);
 }
 
+// div3_rn for x >= +0 or NaN, without its special cases: for finite x >= +0 the
+// remainder is +0 exactly when q is exact (and then q + 0 * RN(1/3) = q), and q is finite,
+// so the two agree; the self-test (gbsdf_selftest(0)) checks every non-negative float.
+// The eikonal's 3D candidate s0 + s1 + s2 + root is such an x.
+__device__ __forceinline__ float div3_pos(float x) {
+    const float r3 = 0.333333343267440796f;  // RN(1/3)
+    const float q = x * r3;
+    return __fmaf_rn(__fmaf_rn(-3.0f, q, x), r3, q);
+}
+
+// Packed FP32 pairs (Blackwell's f32x2 arithmetic, PTX ISA 8.6, sm_100 and later): one
+// instruction rounds each lane exactly as the scalar instruction does (round to nearest
+// even, subnormals kept), so a pair of independent updates costs half the issue slots
+// for every add, subtract, multiply and fused multiply-add.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void up2(f32x2 r, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r)); }
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 // The reference's Godunov update, rhi_eikonal_godunov (cuda_rasterizer.cu:405-425),
-// operation for operation (including its halved 3D pairwise sum). The final division by
-// 3 uses div3_rn, which rounds identically to the IEEE quotient. The branches are kept:
-// whole warps skip the 2D / 3D work where the 1D update applies.
+// operation for operation as the reference's own build computes it: nvcc's default FMA
+// contraction fuses disc = fma(2h, h, -(d*d)) (d = s1 - s0) and the halved 3D pairwise
+// sum S = fma(e2, e2, fma(e1, e1, d*d)) (e1 = s2 - s1, e2 = s2 - s0); 3h^2 - S/2 keeps
+// its roundings. This engine is compiled without contraction, so the fused operations are
+// written out. The final division by 3 uses div3_rn, which rounds identically to the IEEE
+// quotient. The branches are kept: whole warps skip the 2D / 3D work where the 1D update
+// applies.
 __device__ __forceinline__ float godunov_ref(float ax, float ay, float az, float h) {
     const float s0 = fminf(ax, fminf(ay, az));
     const float s2 = fmaxf(ax, fmaxf(ay, az));
     const float s1 = ax + ay + az - s0 - s2;
     float updated = s0 + h;
     if (updated > s1) {
-        const float disc = 2.0f * h * h - (s1 - s0) * (s1 - s0);
+        const float d = s1 - s0;
+        const float dd = d * d;
+        const float disc = __fmaf_rn(2.0f * h, h, -dd);
         if (disc >= 0.0f) {
             updated = (s0 + s1 + sqrtf(disc)) * 0.5f;
             if (updated > s2) {
-                const float disc3 = 3.0f * h * h -
-                                    ((s1 - s0) * (s1 - s0) + (s2 - s1) * (s2 - s1) + (s2 - s0) * (s2 - s0)) * 0.5f;
+                const float e1 = s2 - s1, e2 = s2 - s0;
+                const float S = __fmaf_rn(e2, e2, __fmaf_rn(e1, e1, dd));
+                const float disc3 = 3.0f * h * h - S * 0.5f;
                 if (disc3 >= 0.0f) updated = div3_rn(s0 + s1 + s2 + sqrtf(disc3));
             }
         }
@@ -176,15 +225,65 @@ __device__ __forceinline__ float godunov_ref_sel(float ax, float ay, float az, f
     const float s2 = fmaxf(ax, fmaxf(ay, az));
     const float s1 = ax + ay + az - s0 - s2;
     const float u1 = s0 + h;
-    const float d10 = (s1 - s0) * (s1 - s0);
-    const float disc = 2.0f * h * h - d10;
-    const float disc3 = 3.0f * h * h - (d10 + (s2 - s1) * (s2 - s1) + (s2 - s0) * (s2 - s0)) * 0.5f;
+    const float d = s1 - s0;
+    const float dd = d * d;
+    const float disc = __fmaf_rn(2.0f * h, h, -dd);
+    const float e1 = s2 - s1, e2 = s2 - s0;
+    const float disc3 = 3.0f * h * h - __fmaf_rn(e2, e2, __fmaf_rn(e1, e1, dd)) * 0.5f;
     const bool ok2 = disc >= 0.0f, ok3 = disc3 >= 0.0f;
     const float u2 = (s0 + s1 + sqrtf(ok2 ? disc : 1.0f)) * 0.5f;
     const float u3 = div3_rn(s0 + s1 + s2 + sqrtf(ok3 ? disc3 : 1.0f));
     const bool take2 = (u1 > s1) && ok2;
     const bool take3 = take2 && (u2 > s2) && ok3;
     return take3 ? u3 : (take2 ? u2 : u1);
+}
+
+// Constants of godunov_ref_pair for one voxel size, each in both lanes.
+struct GodunovPairConsts {
+    f32x2 h, m2h, a3, half, r3, m3;
+};
+__device__ __forceinline__ GodunovPairConsts godunov_pair_consts(float h) {
+    const float a3 = 3.0f * h * h;
+    return GodunovPairConsts{pk2(h, h),       pk2(-2.0f * h, -2.0f * h), pk2(a3, a3),
+                             pk2(0.5f, 0.5f), pk2(0.333333343267440796f, 0.333333343267440796f),
+                             pk2(-3.0f, -3.0f)};
+}
+
+// godunov_ref_sel for two independent voxels at once: the arithmetic on packed pairs,
+// the ordering, square roots and selections per lane. Every value rounds exactly as in
+// godunov_ref_sel: disc = fma(2h, h, -dd) is formed negated as fma(-2h, h, dd) (rounding
+// to nearest is symmetric) and only its sign and negation are used; 3h^2 - S/2 keeps the
+// two roundings; the division by 3 is div3_pos.
+__device__ __forceinline__ void godunov_ref_pair(float ax0, float ay0, float az0, float ax1, float ay1, float az1,
+                                                 const GodunovPairConsts& c, float& out0, float& out1) {
+    const float s00 = fminf(ax0, fminf(ay0, az0)), s20 = fmaxf(ax0, fmaxf(ay0, az0));
+    const float s01 = fminf(ax1, fminf(ay1, az1)), s21 = fmaxf(ax1, fmaxf(ay1, az1));
+    const f32x2 S0 = pk2(s00, s01), S2 = pk2(s20, s21);
+    const f32x2 S1 = sub2(sub2(add2(add2(pk2(ax0, ax1), pk2(ay0, ay1)), pk2(az0, az1)), S0), S2);
+    const f32x2 U1 = add2(S0, c.h);
+    const f32x2 D = sub2(S1, S0);
+    const f32x2 DD = mul2(D, D);
+    const f32x2 ND = fma2(c.m2h, c.h, DD);  // -disc
+    const f32x2 SS = fma2(sub2(S2, S0), sub2(S2, S0), fma2(sub2(S2, S1), sub2(S2, S1), DD));
+    const f32x2 D3 = sub2(c.a3, mul2(SS, c.half));
+    float nd0, nd1, d30, d31;
+    up2(ND, nd0, nd1);
+    up2(D3, d30, d31);
+    const bool ok20 = nd0 <= 0.0f, ok21 = nd1 <= 0.0f, ok30 = d30 >= 0.0f, ok31 = d31 >= 0.0f;
+    const f32x2 T01 = add2(S0, S1);
+    const f32x2 U2 = mul2(add2(T01, pk2(sqrtf(ok20 ? -nd0 : 1.0f), sqrtf(ok21 ? -nd1 : 1.0f))), c.half);
+    const f32x2 X3 = add2(add2(T01, S2), pk2(sqrtf(ok30 ? d30 : 1.0f), sqrtf(ok31 ? d31 : 1.0f)));
+    const f32x2 Q = mul2(X3, c.r3);
+    const f32x2 U3 = fma2(fma2(c.m3, Q, X3), c.r3, Q);
+    float u10, u11, s10, s11, u20, u21, u30, u31;
+    up2(U1, u10, u11);
+    up2(S1, s10, s11);
+    up2(U2, u20, u21);
+    up2(U3, u30, u31);
+    const bool t20 = (u10 > s10) && ok20, t21 = (u11 > s11) && ok21;
+    const bool t30 = t20 && (u20 > s20) && ok30, t31 = t21 && (u21 > s21) && ok31;
+    out0 = t30 ? u30 : (t20 ? u20 : u10);
+    out1 = t31 ? u31 : (t21 ? u21 : u11);
 }
 
 // Corrected, monotone Godunov update (the engine's exact mode): sorted minima,

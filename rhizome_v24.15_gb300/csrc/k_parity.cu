@@ -80,15 +80,18 @@ __global__ void __launch_bounds__(kParWarps * 32) parity_kernel(const ParTri* __
             const float4 ab = *reinterpret_cast<const float4*>(p.xyab);
             if (rx < ab.x || rx > ab.z) continue;
             const float* v = p.v;
-            float d0 = (v[3] - v[0]) * (ry - v[1]) - (v[4] - v[1]) * (rx - v[0]);
-            float d1 = (v[6] - v[3]) * (ry - v[4]) - (v[7] - v[4]) * (rx - v[3]);
-            float d2 = (v[0] - v[6]) * (ry - v[7]) - (v[1] - v[7]) * (rx - v[6]);
+            // the roundings of the reference's build (nvcc's default FMA contraction):
+            // a*b - c*d as fma(a, b, -(c*d)), the hit height's sum as
+            // fma(d0, z2, fma(d1, z0, d2*z1))
+            float d0 = __fmaf_rn(v[3] - v[0], ry - v[1], -((v[4] - v[1]) * (rx - v[0])));
+            float d1 = __fmaf_rn(v[6] - v[3], ry - v[4], -((v[7] - v[4]) * (rx - v[3])));
+            float d2 = __fmaf_rn(v[0] - v[6], ry - v[7], -((v[1] - v[7]) * (rx - v[6])));
             bool pos = (d0 > 0.0f && d1 > 0.0f && d2 > 0.0f);
             bool neg = (d0 < 0.0f && d1 < 0.0f && d2 < 0.0f);
             if (!pos && !neg) continue;
             float area2 = d0 + d1 + d2;
             if (fabsf(area2) < 1e-12f) continue;
-            float zh = (d1 * v[2] + d2 * v[5] + d0 * v[8]) / area2;
+            float zh = __fmaf_rn(d0, v[8], __fmaf_rn(d1, v[2], d2 * v[5])) / area2;
             if (nh < kParityMaxHits) {
                 hits[nh * 32 + lane] = zh;
                 if (SIGNED) hsg[nh * 32 + lane] = neg ? 1 : -1;

@@ -35,6 +35,7 @@ __all__ = [
     "vessel_tree",
     "sh_blob",
     "perturbed_sphere",
+    "overlapping_spheres",
     "fit_to_lattice",
     "signed_volume",
     "to_triangles",
@@ -377,6 +378,21 @@ def perturbed_sphere(seed: int = 4, n_lat: int = 64, n_lon: int = 128, base_radi
     r = base_radius + _real_sh_sum(theta, phi, coeffs)
     v = dirs * r[:, None]
     return v, _orient_outward(v, faces)
+
+
+def overlapping_spheres(radius: float = 30.0, distance: float = 56.0, n_lat: int = 48, n_lon: int = 96):
+    """Two closed spheres whose shells overlap in a lens (centres `distance` apart on x),
+    not merged: every ray through the lens crosses four shells, so scanline parity calls
+    the lens outside while its winding number is 2 -- the self-overlap divergence the
+    reference's stratified probes and patch boxes exist for (cuda_rasterizer.cu:1067-1132).
+    A small lens gives a few probe sites and one patch round; a large one more sites than
+    the reference's give-up cap."""
+    dirs, _, _, faces = _uv_sphere(n_lat, n_lon)
+    v = dirs * radius
+    off = np.array([distance / 2.0, 0.0, 0.0])
+    verts = np.vstack([v - off, v + off])
+    f = _orient_outward(v, faces)
+    return verts, np.vstack([f, f + len(v)])
 
 
 # ----------------------------------------------------------------------------------
