@@ -104,9 +104,13 @@ typedef struct gbsdf_options {
                                   logits, one per 8^3 brick (x fastest), in device memory */
     int32_t sweep_schedule; /* eikonal sweep schedules (identical results), x + 10 w: x = 1 x sweep
                                staged by cp.async, 2 by TMA tiles on a CTA-barrier ring, 3 by TMA
-                               tiles on a warp-specialised mbarrier pipeline; w = 1 y / z walks
+                               tiles on a warp-specialised mbarrier pipeline, 4 the same with two
+                               lines per thread updated in packed FP32 pairs (the reference's
+                               update; other modes run 3); w = 1 y / z walks
                                staged by cp.async, 2 by TMA batches on a pipeline, 3 the same
-                               with four adjacent lines per thread; a 0 digit (and
+                               with four adjacent lines per thread, 4 the same with the lines'
+                               updates in packed FP32 pairs (the reference's update; other
+                               modes run 3); a 0 digit (and
                                0 overall) = autotuned (the first build of a lattice class times
                                the candidates). TMA needs rows of a multiple of 4 voxels. */
     int32_t host_output;    /* host outputs: 0 = a page-locked output is written by the sign-apply
@@ -146,8 +150,9 @@ typedef struct gbsdf_stats {
     int64_t csr_entries;   /* entries of the reference's supercell CSR */
     int64_t kernel_launches; /* CUDA kernels this call launched */
     int64_t proposed;      /* learned mode: bricks the network proposed for the exact winding number */
-    int64_t sweep_schedule; /* schedules that ran: x schedule (1-3) + 10 x walk schedule
-                               (1 cp.async, 2 TMA pipeline, 3 TMA pipeline, 4 lines/thread) */
+    int64_t sweep_schedule; /* schedules that ran: x schedule (1-4) + 10 x walk schedule
+                               (1 cp.async, 2 TMA pipeline, 3 TMA pipeline, 4 lines/thread,
+                               4 the same in packed pairs) */
     int64_t winding_certified; /* exact winding decisions settled by the cluster bound */
     int64_t winding_summed;    /* ... and by the triangle-by-triangle sum */
     int64_t reserved[3];
@@ -366,8 +371,9 @@ int gbsdf_legacy_sdf_noalloc(const gbsdf_tri* tris_dev, int64_t n_tris, float vo
                              int32_t device, void* stream, gbsdf_stats* stats, char* err, size_t errlen);
 
 /* Engine self-tests (no counterpart in the reference). which = 0: the correctly rounded
- * division by 3 used by the eikonal update is compared with the IEEE quotient for every
- * non-NaN float input; which = 1: the x sweep's TMA tile layout (32-byte swizzle,
+ * divisions by 3 used by the eikonal update are compared with the IEEE quotient -- the
+ * general one for every non-NaN float input, the one for non-negative arguments for every
+ * finite non-negative float; which = 1: the x sweep's TMA tile layout (32-byte swizzle,
  * out-of-lattice fill) is checked element by element on five boxes of a test grid.
  * *result = number of mismatches (0 expected). */
 int gbsdf_selftest(int32_t which, int32_t device, uint64_t* result, char* err, size_t errlen);

@@ -144,12 +144,27 @@ __device__ __forceinline__ float div3_rn(float x) {
 
 // div3_rn for x >= +0 or NaN, without its special cases: for finite x >= +0 the
 // remainder is +0 exactly when q is exact (and then q + 0 * RN(1/3) = q), and q is finite,
-// so the two agree; the self-test (gbsdf_selftest(0)) checks every non-negative float.
+// so the two agree; the self-test (gbsdf_selftest(0)) checks every finite non-negative
+// float.
 // The eikonal's 3D candidate s0 + s1 + s2 + root is such an x.
 __device__ __forceinline__ float div3_pos(float x) {
     const float r3 = 0.333333343267440796f;  // RN(1/3)
     const float q = x * r3;
     return __fmaf_rn(__fmaf_rn(-3.0f, q, x), r3, q);
+}
+
+// Three-input minimum and maximum (PTX ISA 8.8, sm_100 and later): for operands that are
+// not NaN these equal fminf(a, fminf(b, c)) and fmaxf(a, fmaxf(b, c)) exactly (a minimum
+// or maximum rounds nothing); the Godunov updates never see a NaN operand.
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
 }
 
 // Packed FP32 pairs (Blackwell's f32x2 arithmetic, PTX ISA 8.6, sm_100 and later): one
@@ -193,8 +208,8 @@ __device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
 // quotient. The branches are kept: whole warps skip the 2D / 3D work where the 1D update
 // applies.
 __device__ __forceinline__ float godunov_ref(float ax, float ay, float az, float h) {
-    const float s0 = fminf(ax, fminf(ay, az));
-    const float s2 = fmaxf(ax, fmaxf(ay, az));
+    const float s0 = min3f(ax, ay, az);
+    const float s2 = max3f(ax, ay, az);
     const float s1 = ax + ay + az - s0 - s2;
     float updated = s0 + h;
     if (updated > s1) {
@@ -221,8 +236,8 @@ __device__ __forceinline__ float godunov_ref(float ax, float ay, float az, float
 // thread's independent lines interleave. A square root whose candidate is not selected
 // takes 1 in place of a negative discriminant.
 __device__ __forceinline__ float godunov_ref_sel(float ax, float ay, float az, float h) {
-    const float s0 = fminf(ax, fminf(ay, az));
-    const float s2 = fmaxf(ax, fmaxf(ay, az));
+    const float s0 = min3f(ax, ay, az);
+    const float s2 = max3f(ax, ay, az);
     const float s1 = ax + ay + az - s0 - s2;
     const float u1 = s0 + h;
     const float d = s1 - s0;
@@ -256,8 +271,8 @@ __device__ __forceinline__ GodunovPairConsts godunov_pair_consts(float h) {
 // two roundings; the division by 3 is div3_pos.
 __device__ __forceinline__ void godunov_ref_pair(float ax0, float ay0, float az0, float ax1, float ay1, float az1,
                                                  const GodunovPairConsts& c, float& out0, float& out1) {
-    const float s00 = fminf(ax0, fminf(ay0, az0)), s20 = fmaxf(ax0, fmaxf(ay0, az0));
-    const float s01 = fminf(ax1, fminf(ay1, az1)), s21 = fmaxf(ax1, fmaxf(ay1, az1));
+    const float s00 = min3f(ax0, ay0, az0), s20 = max3f(ax0, ay0, az0);
+    const float s01 = min3f(ax1, ay1, az1), s21 = max3f(ax1, ay1, az1);
     const f32x2 S0 = pk2(s00, s01), S2 = pk2(s20, s21);
     const f32x2 S1 = sub2(sub2(add2(add2(pk2(ax0, ax1), pk2(ay0, ay1)), pk2(az0, az1)), S0), S2);
     const f32x2 U1 = add2(S0, c.h);

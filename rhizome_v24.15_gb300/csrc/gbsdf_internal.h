@@ -233,13 +233,16 @@ struct GridMap {
 bool encode_grid_map(GridMap& m, const float* base, const Lattice& L);
 // Schedules of the x sweep (all give identical results): staged by per-thread cp.async
 // copies, by TMA tiles on a CTA-barrier ring, by TMA tiles on a warp-specialised mbarrier
-// pipeline. 0 picks the pipeline when a TMA
-// descriptor is valid.
-enum XSchedule : int { kXAuto = 0, kXCpAsync = 1, kXTmaRing = 2, kXTmaPipe = 3 };
+// pipeline, the same pipeline with two lines per thread updated in packed FP32 pairs (the
+// reference's update on lattices with at least two voxels along y and z; elsewhere it runs
+// as the pipeline). 0 picks the pipeline when a TMA descriptor is valid.
+enum XSchedule : int { kXAuto = 0, kXCpAsync = 1, kXTmaRing = 2, kXTmaPipe = 3, kXTmaPipe2 = 4 };
 // Schedules of the y and z walks: cp.async slice ring, TMA batches on a warp-specialised
-// mbarrier pipeline (one line per thread in two rows, or four adjacent lines per thread).
-// 0 picks the pipeline when its descriptors are valid.
-enum WSchedule : int { kWAuto = 0, kWCpAsync = 1, kWTmaPipe = 2, kWTmaVec = 3 };
+// mbarrier pipeline (one line per thread in two rows, or four adjacent lines per thread,
+// or four adjacent lines per thread updated in packed FP32 pairs -- the reference's
+// update on lattices with at least two rows across the walk; elsewhere it runs as the
+// four-lines schedule). 0 picks the pipeline when its descriptors are valid.
+enum WSchedule : int { kWAuto = 0, kWCpAsync = 1, kWTmaPipe = 2, kWTmaVec = 3, kWTmaVec2 = 4 };
 // `src_map`: the descriptor of `src` (or null); `x_schedule`: an XSchedule.
 void launch_sweep(int rule, int axis, int dir, int round, const float* src, float* dst, const Lattice& L,
                   DevState* ds, cudaStream_t st, const GridMap* src_map = nullptr, int x_schedule = kXAuto,

@@ -648,6 +648,177 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
     mark_changed(ch, &ds->changed[round]);
 }
 
+// ---- x sweeps, TMA pipeline, two lines per thread updated in packed pairs ------------
+// sweep_x_pipe_kernel's tiles, ring and barriers with 4 consumer warps: the thread of
+// lane ty in warp w walks the lines (y0 + ty, z0 + w) and (y0 + ty, z0 + w + 4), and the
+// two serial chains advance together, their reference updates computed by
+// godunov_ref_pair on packed FP32 pairs (same roundings, half the arithmetic issue
+// slots). The neighbour minima skip the far-sentinel clamp, which a lattice with at least
+// two voxels along y and z never needs (an out-of-lattice NaN always meets an in-lattice
+// partner); the launcher falls back to sweep_x_pipe_kernel elsewhere.
+constexpr int kP2Consumers = kXThreads / 2;              // 4 consumer warps
+constexpr int kP2Threads = kP2Consumers + 32;
+
+template <int DIR>
+__global__ void __launch_bounds__(kP2Threads, 4) sweep_x_pipe2_kernel(const __grid_constant__ CUtensorMap tm,
+                                                                   float* __restrict__ dst, Lattice L, int round,
+                                                                   DevState* ds) {
+    if (ds->stop) return;
+    extern __shared__ unsigned char tsm_raw[];
+    unsigned char* tsm = align1k(tsm_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kPS * kTSlotBytes);
+    uint64_t* empty = full + kPS;
+    const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
+    const size_t plane = (size_t)dx * dy;
+    const int tid = threadIdx.x;
+    const int y0 = blockIdx.x * kXY, z0 = blockIdx.y * kXZ;
+    const int nchunks = (dx + kXC - 1) / kXC;
+    if (tid == 0) {
+        for (int s = 0; s < kPS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kP2Consumers / 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();  // the only CTA-wide barrier: the ring's barriers are initialised
+    if (tid >= kP2Consumers) {
+        if (tid != kP2Consumers) return;
+        int ci = 0;
+        for (; ci < nchunks; ++ci) {
+            const int s = ci % kPS;
+            if (ci >= kPS && !mbar_wait(&empty[s], ((ci / kPS) - 1) & 1)) break;
+            const int c = (DIR > 0) ? ci : (nchunks - 1 - ci);
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            mbar_expect_tx(&full[s], kTBox * 4);
+            tma_load_3d(tsm + s * kTSlotBytes, &tm, c * kXC, y0 - 1, z0 - 1, &full[s]);
+        }
+        if (ci < nchunks) {  // consumers stopped releasing slots: drain what is in flight
+            for (int k = max(0, ci - kPS); k < ci; ++k) mbar_wait(&full[k % kPS], (k / kPS) & 1);
+            atomicAdd(&ds->wait_timeouts, 1ull);
+        }
+        return;
+    }
+    const int ty = tid & 31, tz = tid >> 5;
+    const int y = y0 + ty;
+    const int za = z0 + tz, zb = z0 + tz + 4;
+    const bool act_a = (y < dy) && (za < dz), act_b = (y < dy) && (zb < dz);
+    const int rma = (tz + 1) * kXHY + (ty + 1), rmb = rma + 4 * kXHY;
+    const GodunovPairConsts gc = godunov_pair_consts(L.h);
+    const float h = L.h;
+    float preva = kFarSentinel, prevb = kFarSentinel;
+    bool ch = false;
+#pragma unroll 1
+    for (int ci = 0; ci < nchunks; ++ci) {
+        bool ok = mbar_wait(&full[ci % kPS], (ci / kPS) & 1);
+        if (ok && ci + 1 < nchunks) ok = mbar_wait(&full[(ci + 1) % kPS], ((ci + 1) / kPS) & 1);
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (ty == 0) atomicAdd(&ds->wait_timeouts, 1ull);
+            return;
+        }
+        const int c = (DIR > 0) ? ci : (nchunks - 1 - ci);
+        const int xc = c * kXC;
+        const float* tile = reinterpret_cast<const float*>(tsm + (ci % kPS) * kTSlotBytes);
+        const float* ntile = reinterpret_cast<const float*>(tsm + ((ci + 1) % kPS) * kTSlotBytes);
+        if (act_a && xc + kXC <= dx && ci + 1 < nchunks) {
+            // both lines' chunks are whole (line b may be outside the lattice: it then
+            // reads the NaN fill and its results are not stored). The chunk is walked in
+            // two 4-voxel halves, so only one half's operands are live at a time.
+            float* da = dst + (size_t)za * plane + (size_t)y * dx + xc;
+            float* db = dst + (size_t)zb * plane + (size_t)y * dx + xc;
+            const float nxta = (DIR > 0) ? ntile[tsw(rma, 0)] : ntile[tsw(rma, kXC - 1)];
+            const float nxtb = (DIR > 0) ? ntile[tsw(rmb, 0)] : ntile[tsw(rmb, kXC - 1)];
+            float4 ma = tvec(tile, rma, (DIR > 0) ? 0 : 1), mb = tvec(tile, rmb, (DIR > 0) ? 0 : 1);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int hv = (DIR > 0) ? k : 1 - k;
+                const float cura[4] = {ma.x, ma.y, ma.z, ma.w}, curb[4] = {mb.x, mb.y, mb.z, mb.w};
+                float enda, endb;  // the other half's first cell in walk order, or the next chunk's
+                if (k == 0) {
+                    const float4 na = tvec(tile, rma, 1 - hv), nb = tvec(tile, rmb, 1 - hv);
+                    enda = (DIR > 0) ? na.x : na.w;
+                    endb = (DIR > 0) ? nb.x : nb.w;
+                    ma = na;
+                    mb = nb;
+                } else {
+                    enda = nxta;
+                    endb = nxtb;
+                }
+                const float4 a = tvec(tile, rma - 1, hv), b = tvec(tile, rma + 1, hv);
+                const float4 p = tvec(tile, rma - kXHY, hv), q = tvec(tile, rma + kXHY, hv);
+                const float4 a2 = tvec(tile, rmb - 1, hv), b2 = tvec(tile, rmb + 1, hv);
+                const float4 p2 = tvec(tile, rmb - kXHY, hv), q2 = tvec(tile, rmb + kXHY, hv);
+                const float aya[4] = {fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), fminf(a.w, b.w)};
+                const float aza[4] = {fminf(p.x, q.x), fminf(p.y, q.y), fminf(p.z, q.z), fminf(p.w, q.w)};
+                const float ayb[4] = {fminf(a2.x, b2.x), fminf(a2.y, b2.y), fminf(a2.z, b2.z), fminf(a2.w, b2.w)};
+                const float azb[4] = {fminf(p2.x, q2.x), fminf(p2.y, q2.y), fminf(p2.z, q2.z), fminf(p2.w, q2.w)};
+                float resa[4], resb[4];
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj) {
+                    const int j = (DIR > 0) ? jj : (3 - jj);
+                    const float downa = (DIR > 0) ? ((j + 1 < 4) ? cura[j + 1] : enda) : ((j > 0) ? cura[j - 1] : enda);
+                    const float downb = (DIR > 0) ? ((j + 1 < 4) ? curb[j + 1] : endb) : ((j > 0) ? curb[j - 1] : endb);
+                    float ua, ub;
+                    godunov_ref_pair(fminf(preva, downa), aya[j], aza[j], fminf(prevb, downb), ayb[j], azb[j], gc, ua,
+                                     ub);
+                    const bool la = ua < cura[j], lb = act_b && (ub < curb[j]);
+                    resa[j] = la ? ua : cura[j];
+                    resb[j] = lb ? ub : curb[j];
+                    ch |= la | lb;
+                    preva = resa[j];
+                    prevb = resb[j];
+                }
+                reinterpret_cast<float4*>(da)[hv] = make_float4(resa[0], resa[1], resa[2], resa[3]);
+                if (act_b) reinterpret_cast<float4*>(db)[hv] = make_float4(resb[0], resb[1], resb[2], resb[3]);
+            }
+        } else {
+            // a partial or the last chunk: each line on its own with the scalar update
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                const bool act = side ? act_b : act_a;
+                if (!act) continue;
+                const int rme = side ? rmb : rma;
+                const int z = side ? zb : za;
+                float prev = side ? prevb : preva;
+                float res[kXC];
+#pragma unroll
+                for (int jj = 0; jj < kXC; ++jj) {
+                    const int j = (DIR > 0) ? jj : (kXC - 1 - jj);
+                    res[j] = 0.0f;
+                    if (xc + j >= dx) continue;
+                    const float cur = tile[tsw(rme, j)];
+                    float down;
+                    if (DIR > 0) down = (j + 1 < kXC) ? tile[tsw(rme, j + 1)]
+                                                      : ((ci + 1 < nchunks) ? ntile[tsw(rme, 0)] : kFarSentinel);
+                    else down = (j > 0) ? tile[tsw(rme, j - 1)]
+                                        : ((ci + 1 < nchunks) ? ntile[tsw(rme, kXC - 1)] : kFarSentinel);
+                    const float ayj = fminf(tile[tsw(rme - 1, j)], tile[tsw(rme + 1, j)]);
+                    const float azj = fminf(tile[tsw(rme - kXHY, j)], tile[tsw(rme + kXHY, j)]);
+                    const float u = godunov_ref(fminf(prev, down), ayj, azj, h);
+                    const float out = (u < cur) ? u : cur;
+                    ch |= (u < cur);
+                    res[j] = out;
+                    prev = out;
+                }
+                float* drow = dst + (size_t)z * plane + (size_t)y * dx + xc;
+                if (xc + kXC <= dx) {
+                    reinterpret_cast<float4*>(drow)[0] = make_float4(res[0], res[1], res[2], res[3]);
+                    reinterpret_cast<float4*>(drow)[1] = make_float4(res[4], res[5], res[6], res[7]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < kXC; ++j)
+                        if (xc + j < dx) drow[j] = res[j];
+                }
+                if (side) prevb = prev;
+                else preva = prev;
+            }
+        }
+        // this warp's last read of chunk ci's slot is done (it was also chunk ci-1's "next")
+        __syncwarp();
+        if (ty == 0) mbar_arrive(&empty[ci % kPS]);
+    }
+    mark_changed(ch, &ds->changed[round]);
+}
+
 // ---- y and z walks, TMA batches on a warp-specialised pipeline ------------------------
 // The lines, tile (32 x 16 lines, two per thread) and per-line arithmetic of
 // sweep_walk_kernel; the slices come in batches of 4, one cp.async.bulk.tensor copy per
@@ -917,6 +1088,136 @@ __global__ void __launch_bounds__(kWVThreads) sweep_walk_vec_kernel(const __grid
     mark_changed(ch, &ds->changed[round]);
 }
 
+// ---- y and z walks, four adjacent lines per thread, updates in packed pairs ----------
+// sweep_walk_vec_kernel (tile, boxes, pipeline, loads and stores) for the reference's
+// update with lines 0-1 and 2-3 of a thread's quad updated together by
+// godunov_ref_pair on packed FP32 pairs (same roundings, half the arithmetic issue
+// slots), and without the far-sentinel clamps of the neighbour minima, which a lattice
+// with dim x a multiple of 4 and at least two rows across the walk never needs.
+template <int AXIS, int DIR>
+__global__ void __launch_bounds__(kWVThreads) sweep_walk_vec2_kernel(const __grid_constant__ CUtensorMap tm,
+                                                                     float* __restrict__ dst, Lattice L,
+                                                                     int round, DevState* ds) {
+    if (ds->stop) return;
+    extern __shared__ unsigned char tsm_raw[];
+    unsigned char* tsm = align1k(tsm_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kWVS * kWPSlotBytes);
+    uint64_t* empty = full + kWVS;
+    const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
+    const size_t plane = (size_t)dx * dy;
+    const int n_walk = (AXIS == 2) ? dz : dy;
+    const int n_rows = (AXIS == 2) ? dy : dz;
+    const size_t step_stride = (AXIS == 2) ? plane : (size_t)dx;
+    const size_t row_stride = (AXIS == 2) ? (size_t)dx : plane;
+    constexpr int kSliceS = (AXIS == 2) ? kWHR * kWPX : kWPX;
+    constexpr int kRowS = (AXIS == 2) ? kWPX : kWPB * kWPX;
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * kWX, r0 = blockIdx.y * kWR;
+    const int nbatches = (n_walk + kWPB - 1) / kWPB;
+    if (tid == 0) {
+        for (int s = 0; s < kWVS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kWVConsumers / 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    if (tid >= kWVConsumers) {
+        if (tid != kWVConsumers) return;
+        int b = 0;
+        for (; b < nbatches; ++b) {
+            const int s = b % kWVS;
+            if (b >= kWVS && !mbar_wait(&empty[s], ((b / kWVS) - 1) & 1)) break;
+            const int sl0 = (DIR > 0) ? b * kWPB : n_walk - kWPB - b * kWPB;
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            mbar_expect_tx(&full[s], kWPBox * 4);
+            if (AXIS == 2) tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, r0 - 1, sl0, &full[s]);
+            else tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, sl0, r0 - 1, &full[s]);
+        }
+        if (b < nbatches) {
+            for (int k = max(0, b - kWVS); k < b; ++k) mbar_wait(&full[k % kWVS], (k / kWVS) & 1);
+            atomicAdd(&ds->wait_timeouts, 1ull);
+        }
+        return;
+    }
+    const int cx = tid & 7, tr = tid >> 3;       // quad of x, row
+    const int x = x0 + 4 * cx, r = r0 + tr;
+    const bool act = (x < dx) && (r < n_rows);  // dim x is a multiple of 4: the quad is all in
+    const GodunovPairConsts gc = godunov_pair_consts(L.h);
+    const int m = (tr + 1) * kRowS + 4 * cx + 4;  // 16-byte aligned: kRowS, kSliceS are multiples of 4
+    auto slice_ptr = [&](int s) -> const float* {
+        const int b = s / kWPB, q = s - b * kWPB;
+        const int qb = (DIR > 0) ? q : (kWPB - 1 - q);
+        return reinterpret_cast<const float*>(tsm + (b % kWVS) * kWPSlotBytes) + qb * kSliceS;
+    };
+    float prev[4] = {kFarSentinel, kFarSentinel, kFarSentinel, kFarSentinel};
+    float cur[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    bool ch = false;
+    const long long sstep = (DIR > 0) ? (long long)step_stride : -(long long)step_stride;
+    float* p = dst + (size_t)((DIR > 0) ? 0 : n_walk - 1) * step_stride + (size_t)r * row_stride + x;
+#pragma unroll 1
+    for (int b = 0; b < nbatches; ++b) {
+        bool ok = mbar_wait(&full[b % kWVS], (b / kWVS) & 1);
+        if (ok && b + 1 < nbatches) ok = mbar_wait(&full[(b + 1) % kWVS], ((b + 1) / kWVS) & 1);
+        if (!__all_sync(0xffffffffu, ok)) {
+            if ((tid & 31) == 0) atomicAdd(&ds->wait_timeouts, 1ull);
+            return;
+        }
+        if (b == 0) {
+            const float4 c = *reinterpret_cast<const float4*>(slice_ptr(0) + m);
+            cur[0] = c.x; cur[1] = c.y; cur[2] = c.z; cur[3] = c.w;
+        }
+#pragma unroll
+        for (int q = 0; q < kWPB; ++q) {
+            const int s = b * kWPB + q;
+            if (s >= n_walk) break;
+            const float* cs = slice_ptr(s);
+            float nxt[4] = {kFarSentinel, kFarSentinel, kFarSentinel, kFarSentinel};
+            if (s + 1 < n_walk) {
+                const float4 n4 = *reinterpret_cast<const float4*>(slice_ptr(s + 1) + m);
+                nxt[0] = n4.x; nxt[1] = n4.y; nxt[2] = n4.z; nxt[3] = n4.w;
+            }
+            if (act) {
+                const float4 rm = *reinterpret_cast<const float4*>(cs + m - kRowS);
+                const float4 rp = *reinterpret_cast<const float4*>(cs + m + kRowS);
+                const float xl = cs[m - 1], xr = cs[m + 4];
+                const float rmv[4] = {rm.x, rm.y, rm.z, rm.w}, rpv[4] = {rp.x, rp.y, rp.z, rp.w};
+                float ax[4], ar[4], al[4], u[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    // no far-sentinel clamps: an out-of-lattice NaN always meets an
+                    // in-lattice partner here (dim x a multiple of 4, at least 2 rows)
+                    ax[j] = fminf((j == 0) ? xl : cur[j - 1], (j == 3) ? xr : cur[j + 1]);
+                    ar[j] = fminf(rmv[j], rpv[j]);
+                    al[j] = fminf(prev[j], nxt[j]);
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j += 2) {
+                    if (AXIS == 2) godunov_ref_pair(ax[j], ar[j], al[j], ax[j + 1], ar[j + 1], al[j + 1], gc, u[j], u[j + 1]);
+                    else godunov_ref_pair(ax[j], al[j], ar[j], ax[j + 1], al[j + 1], ar[j + 1], gc, u[j], u[j + 1]);
+                }
+                float out[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    out[j] = cur[j];
+                    if (u[j] < cur[j]) {
+                        out[j] = u[j];
+                        ch = true;
+                    }
+                    prev[j] = out[j];
+                }
+                *reinterpret_cast<float4*>(p) = make_float4(out[0], out[1], out[2], out[3]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) cur[j] = nxt[j];
+            p += sstep;
+        }
+        __syncwarp();
+        if ((tid & 31) == 0) mbar_arrive(&empty[b % kWVS]);
+    }
+    mark_changed(ch, &ds->changed[round]);
+}
+
 // Layout check of the staged tile: one CTA loads the box at (x, y, z) of a grid whose
 // cells hold their own linear index, and every thread compares elements (scalar reads
 // through tsw, vector reads through tvec) with the expected value or NaN outside.
@@ -1040,8 +1341,22 @@ void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lat
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
     GBSDF_COUNT_LAUNCH();
     // four lines per thread: 16-byte stores need an aligned destination (rows already are)
-    if (wsched == kWTmaVec && (reinterpret_cast<uintptr_t>(dst) & 15)) wsched = kWTmaPipe;
-    if (axis != 0 && wsched == kWTmaVec) {
+    if ((wsched == kWTmaVec || wsched == kWTmaVec2) && (reinterpret_cast<uintptr_t>(dst) & 15)) wsched = kWTmaPipe;
+    // packed pairs: the reference's update, at least two rows across the walk
+    if (wsched == kWTmaVec2 && (RULE != 0 || (axis == 2 ? dy : dz) < 2)) wsched = kWTmaVec;
+    if (axis != 0 && wsched == kWTmaVec2) {
+        const int n_rows = (axis == 2) ? dy : dz;
+        dim3 grid((dx + kWX - 1) / kWX, (n_rows + kWR - 1) / kWR);
+        if (axis == 2) {
+            cudaFuncSetAttribute(sweep_walk_vec2_kernel<2, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kWVSmem);
+            sweep_walk_vec2_kernel<2, DIR><<<grid, kWVThreads, kWVSmem, st>>>(src_map->zmap, dst, L, round, ds);
+        } else {
+            cudaFuncSetAttribute(sweep_walk_vec2_kernel<1, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kWVSmem);
+            sweep_walk_vec2_kernel<1, DIR><<<grid, kWVThreads, kWVSmem, st>>>(src_map->ymap, dst, L, round, ds);
+        }
+    } else if (axis != 0 && wsched == kWTmaVec) {
         const int n_rows = (axis == 2) ? dy : dz;
         dim3 grid((dx + kWX - 1) / kWX, (n_rows + kWR - 1) / kWR);
         if (axis == 2) {
@@ -1079,7 +1394,11 @@ void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lat
         cudaFuncSetAttribute(sweep_walk_kernel<1, RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kWSmem);
         sweep_walk_kernel<1, RULE, DIR><<<grid, kWThreads, kWSmem, st>>>(src, dst, L, round, ds);
-    } else if (xsched == kXTmaPipe) {
+    } else if (xsched == kXTmaPipe2 && RULE == 0 && dy >= 2 && dz >= 2) {
+        dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
+        cudaFuncSetAttribute(sweep_x_pipe2_kernel<DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPSmem);
+        sweep_x_pipe2_kernel<DIR><<<grid, kP2Threads, kPSmem, st>>>(src_map->map, dst, L, round, ds);
+    } else if (xsched == kXTmaPipe || xsched == kXTmaPipe2) {
         dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
         cudaFuncSetAttribute(sweep_x_pipe_kernel<RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kPSmem);

@@ -136,7 +136,8 @@ __global__ void legacy_combine_kernel(const float* __restrict__ d2, const uint32
     }
 }
 
-// Self-test: div3_rn against the IEEE quotient x / 3.0f for every non-NaN float.
+// Self-test: div3_rn against the IEEE quotient x / 3.0f for every non-NaN float, and
+// div3_pos for every finite non-negative one.
 __global__ void selftest_div3_kernel(unsigned long long* __restrict__ mism) {
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     unsigned long long bad = 0;
@@ -146,6 +147,7 @@ __global__ void selftest_div3_kernel(unsigned long long* __restrict__ mism) {
         if (isnan(x)) continue;
         const float a = div3_rn(x), b = x / 3.0f;
         bad += (__float_as_uint(a) != __float_as_uint(b)) ? 1ull : 0ull;
+        if (i < 0x7f800000ull) bad += (__float_as_uint(div3_pos(x)) != __float_as_uint(b)) ? 1ull : 0ull;
     }
     if (bad) atomicAdd(mism, bad);
 }

@@ -1,6 +1,6 @@
 // tune.cu — the sweep-schedule autotuner.
 //
-// The x sweep has three schedules and the y / z walks three, all with identical results
+// The x sweep has four schedules and the y / z walks four, all with identical results
 // (internal header, XSchedule / WSchedule). Which is fastest depends on the lattice (row
 // length, CTAs per wave), the device and the field: the first round sweeps a band in a far
 // field, where most updates are one-dimensional, later rounds a field where most warps
@@ -72,7 +72,7 @@ SweepPlan tuned_sweep_plan(int device, const Lattice& L, const float* src, float
     };
     if (tma) {
         float best = 1e30f;
-        for (int cand : {kXCpAsync, kXTmaRing, kXTmaPipe}) {
+        for (int cand : {kXCpAsync, kXTmaRing, kXTmaPipe, kXTmaPipe2}) {
             const float ms = time_it(0, cand, plan.w);
             if (ms >= 0.0f && ms < best) {
                 best = ms;
@@ -82,7 +82,7 @@ SweepPlan tuned_sweep_plan(int device, const Lattice& L, const float* src, float
     }
     if (wtma) {
         float best = 1e30f;
-        for (int cand : {kWCpAsync, kWTmaPipe, kWTmaVec}) {
+        for (int cand : {kWCpAsync, kWTmaPipe, kWTmaVec, kWTmaVec2}) {
             const float ms = time_it(2, plan.x, cand);
             if (ms >= 0.0f && ms < best) {
                 best = ms;
