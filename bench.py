@@ -122,10 +122,15 @@ def make_workload(dims=None, h=None, name=WORKLOAD):
     return tris, mn, mx, h
 
 
-def run_batched(gbsdf, torch, dev, mode, steps, warmup, local):
+def run_batched(gbsdf, torch, dev, mode, steps, warmup, local, mlp):
     """The 64-mesh batched workload: one planned batch (one CUDA graph per run) against
     64 sequential single-mesh calls, device-resident triangles and outputs, timed on the
-    host around whole runs (each run returns after its last kernel)."""
+    host around whole runs (each run returns after its last kernel). Modes: the headline
+    mode, plain (the reference-compatible fast path) and learned (plain signs, the
+    sign-risk network's proposals re-decided exactly, and re-decided signs instead of a
+    decline where plain's verify diverges). A plain mesh that declines has no output: the
+    reference would rebuild it with its O(voxels x triangles) legacy kernel, which is not
+    timed here."""
     from gbsdf import meshgen
 
     meshes = meshgen.batch_workload()
@@ -152,8 +157,10 @@ def run_batched(gbsdf, torch, dev, mode, steps, warmup, local):
                        f"64^3-384^3, {vox} voxels, fast path, device buffers",
            "voxels": vox}
     launches = 0
-    for name, m in (("batched", mode), ("batched_plain", gbsdf.MODE_REFERENCE)):
-        with gbsdf.Batch(dmeshes, outs=outs, mode=m, device=local) as b:
+    for name, m in (("batched", mode), ("batched_plain", gbsdf.MODE_REFERENCE),
+                    ("batched_learned", gbsdf.MODE_LEARNED)):
+        kw = {"mlp_params": mlp} if m == gbsdf.MODE_LEARNED else {}
+        with gbsdf.Batch(dmeshes, outs=outs, mode=m, device=local, **kw) as b:
             st, stats = b.run()
             ms = timed(b.run, slow=(m == gbsdf.MODE_REFERENCE))
             if name == "batched":
@@ -162,6 +169,9 @@ def run_batched(gbsdf, torch, dev, mode, steps, warmup, local):
         # it still costs its full build and is counted in the throughput
         res[name] = {"value": vox / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms,
                      "declined": sum(1 for x in st if x != 0)}
+        if m == gbsdf.MODE_LEARNED:
+            res[name]["escalated"] = int(sum(x["escalated"] for x in stats))
+            res[name]["proposed_bricks"] = int(sum(x["proposed"] for x in stats))
 
     declined = []
 
@@ -169,14 +179,16 @@ def run_batched(gbsdf, torch, dev, mode, steps, warmup, local):
         declined.clear()
         for (t, h, mn, mx), o in zip(dmeshes, outs):
             _, r = gbsdf.compute_mesh_sdf(t, h, mn, mx, out=o, mode=m, path=gbsdf.PATH_FAST, device=local,
-                                          raise_on_error=False)
+                                          raise_on_error=False, mlp_params=mlp if m == gbsdf.MODE_LEARNED else None)
             declined.append(not r.ok)
 
-    for name, m in (("sequential", mode), ("sequential_plain", gbsdf.MODE_REFERENCE)):
+    for name, m in (("sequential", mode), ("sequential_plain", gbsdf.MODE_REFERENCE),
+                    ("sequential_learned", gbsdf.MODE_LEARNED)):
         ms = timed(lambda: sequential(m), slow=(m == gbsdf.MODE_REFERENCE))
         res[name] = {"value": vox / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms,
                      "declined": int(sum(declined))}
     res["graph_kernel_launches"] = launches
+    res["learned_batched_vs_plain"] = res["batched_learned"]["value"] / res["sequential_plain"]["value"]
     return res
 
 
@@ -383,11 +395,9 @@ def main():
         return
     dims_override = tuple(int(x) for x in args.dims.split(",")) if args.dims else None
     tris, mn, mx, h = make_workload(dims_override, args.h, args.workload)
-    mlp = None
-    if mode == gbsdf.MODE_LEARNED:
-        from gbsdf import learn
+    from gbsdf import learn
 
-        mlp = torch.from_numpy(np.load(learn.MODEL_PATH)["params"]).to(dev)
+    mlp = torch.from_numpy(np.load(learn.MODEL_PATH)["params"]).to(dev)
     dims = mx.astype(np.int64) - mn + 1
     N = int(np.prod(dims))
     T = len(tris)
@@ -434,6 +444,24 @@ def main():
         barrier()
         pms = max_over_ranks(dist, p0.elapsed_time(p1) / args.steps)
         plain = {"mode": "reference", "value": whole_job_gvox(world, N, pms), "ms_per_step": pms}
+
+    # learned mode on the same lattice, same protocol (the shipped network)
+    learned = None
+    if args.mode != "learned" and not args.no_plain:
+        lst = []
+        for _ in range(args.warmup):
+            step_device(gbsdf.MODE_LEARNED)
+        barrier()
+        l0 = torch.cuda.Event(enable_timing=True)
+        l1 = torch.cuda.Event(enable_timing=True)
+        l0.record()
+        for _ in range(args.steps):
+            lst.append(step_device(gbsdf.MODE_LEARNED).stats)
+        l1.record()
+        barrier()
+        lms = max_over_ranks(dist, l0.elapsed_time(l1) / args.steps)
+        learned = {"mode": "learned", "value": whole_job_gvox(world, N, lms), "ms_per_step": lms,
+                   "proposed_bricks": int(lst[-1]["proposed"]), "escalated": int(lst[-1]["escalated"])}
 
     # ---- end to end through the public API with pinned host buffers
     e2e = e2e_ms = None
@@ -498,6 +526,9 @@ def main():
                                              "unknown_columns", "band_voxels", "splat_evals", "gwn_pairs",
                                              "fp64_rechecks")},
             "plain": plain,
+            "learned": learned,
+            "precision": {"band_err_fp64_vox": s0["band_err_fp64"], "band_err_samples": s0["band_err_samples"],
+                          "what": "largest |FP32 - FP64| band-splat distance over sampled band voxels, in voxels"},
             "clocks": clk.summary(),
             "gpu_launches": int(sum(s["kernel_launches"] for s in stats))}
     if mode == gbsdf.MODE_LEARNED:
@@ -506,7 +537,7 @@ def main():
         line["decode"] = run_decode(gbsdf, args.steps)
         line["iso_surface"] = run_iso(gbsdf, out_dev, dims, h, mn, args.steps)
     if not args.no_batch and mode in (gbsdf.MODE_REFERENCE, gbsdf.MODE_EXACT_SIGNS):
-        line["batched"] = run_batched(gbsdf, torch, dev, mode, args.steps, args.warmup, local)
+        line["batched"] = run_batched(gbsdf, torch, dev, mode, args.steps, args.warmup, local, mlp)
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == WORKLOAD:
         line["reference_gpu"] = run_reference_gpu(tris, mn, mx, h)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

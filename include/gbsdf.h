@@ -79,7 +79,10 @@ typedef enum gbsdf_mode {
      * 64 -> 1, BF16 weights, FP32 accumulation) scores every 8^3 brick's sign-error risk
      * and the riskiest bricks are re-decided by the exact winding kernel after the
      * stratified probes and patch boxes (which therefore see the plain path's signs); the
-     * network never supplies a sign. Needs opt->mlp_params. */
+     * network never supplies a sign. Where the plain path's verify diverges (it would
+     * decline), the signs are re-decided instead: signed crossings along near-lattice rays,
+     * the exact winding number for rays through holes (stats->escalated). No int-range
+     * guard. Needs opt->mlp_params (or opt->brick_scores). */
     GBSDF_MODE_LEARNED = 3
 } gbsdf_mode;
 
@@ -155,7 +158,12 @@ typedef struct gbsdf_stats {
                                4 the same in packed pairs) */
     int64_t winding_certified; /* exact winding decisions settled by the cluster bound */
     int64_t winding_summed;    /* ... and by the triangle-by-triangle sum */
-    int64_t reserved[3];
+    int64_t escalated;         /* learned mode: 1 when the stratified verify diverged and the signs
+                                  were re-decided (signed crossings, exact winding number for rays
+                                  through holes) instead of declining */
+    double band_err_fp64;      /* largest |FP32 band distance - FP64 distance| over the sampled band
+                                  voxels, in voxels (fast path; 0 when no band voxel was sampled) */
+    int64_t band_err_samples;  /* band voxels sampled for band_err_fp64 */
 } gbsdf_stats;
 
 /* Fill `opt` with defaults: reference mode, AUTO path, device 0, host triangles. */
@@ -181,10 +189,11 @@ typedef struct gbsdf_mesh_desc {
 } gbsdf_mesh_desc;
 
 /* Batched form of gbsdf_compute_mesh_sdf (the descriptor list of the reference-side
- * C ABI plan). With the fast path (opt->path == GBSDF_PATH_FAST) in reference or
- * exact-signs mode the meshes run as one planned batch (gbsdf_batch_create / _run /
- * _destroy below, one CUDA graph, every mesh its own branch); otherwise they run back to
- * back through gbsdf_compute_mesh_sdf. Returns GBSDF_OK when every mesh succeeded, else
+ * C ABI plan). With the fast path (opt->path == GBSDF_PATH_FAST) in reference, exact-signs
+ * or learned mode (the network's parameters, not caller-supplied brick scores) the meshes
+ * run as one planned batch (gbsdf_batch_create / _run / _destroy below, one CUDA graph,
+ * every mesh its own branch); otherwise they run back to back through
+ * gbsdf_compute_mesh_sdf. Returns GBSDF_OK when every mesh succeeded, else
  * the first failing mesh's status; per-mesh statuses are written to meshes[i].status and
  * per-mesh statistics to stats[i] (stats may be NULL). A failing mesh's output is left
  * untouched. No reference counterpart. */
@@ -198,7 +207,9 @@ int gbsdf_compute_mesh_sdf_batch(gbsdf_mesh_desc* meshes, int32_t n_meshes, int3
  * the graph: the descriptors' pointers and lattices are fixed at creation, their
  * triangle contents may change between runs (a run whose counts outgrow the planned
  * lists re-plans itself and runs again). Fast path only; opt->mode must be
- * GBSDF_MODE_REFERENCE or GBSDF_MODE_EXACT_SIGNS. No reference counterpart. */
+ * GBSDF_MODE_REFERENCE, GBSDF_MODE_EXACT_SIGNS or GBSDF_MODE_LEARNED (with opt->mlp_params
+ * in device memory, kept alive by the caller while the batch exists; the budget and
+ * threshold apply to each mesh). No reference counterpart. */
 typedef struct gbsdf_batch gbsdf_batch;
 int gbsdf_batch_create(const gbsdf_mesh_desc* meshes, int32_t n_meshes, int32_t out_on_device,
                        const gbsdf_options* opt, gbsdf_batch** batch, char* err, size_t errlen);

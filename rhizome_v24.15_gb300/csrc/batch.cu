@@ -94,6 +94,13 @@ struct Job {
     int wsched = kWAuto;       // else the defaults) ...
     int xsched1 = kXAuto;      // ... and of the later rounds
     int wsched1 = kWAuto;
+    // learned mode: the signed-crossing pass, the exact-decided mask, the brick features,
+    // the open-edge table, the network's logits and the proposal histogram
+    uint32_t *S2 = nullptr, *U2 = nullptr, *E = nullptr;
+    float *fbase = nullptr, *fX = nullptr, *logits = nullptr;
+    unsigned *opencnt = nullptr, *ecnt = nullptr, *phist = nullptr;
+    unsigned long long* ekeys = nullptr;
+    long long ecap = 0;
 };
 
 // Carves aligned sub-buffers out of one allocation: a sizing pass, then a placing pass.
@@ -127,12 +134,33 @@ struct gbsdf_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned long long launches_per_run = 0;
+    // learned mode: the network's parameters (device memory, the caller's), the proposal
+    // threshold as a logit and the budget (0: 1/16 of each lattice's bricks)
+    const float* mlp_params = nullptr;
+    float logit_thr = 0.0f;
+    unsigned budget = 0;
 };
 
 namespace gbsdf {
 namespace {
 
 bool exact_signs_mode(const gbsdf_batch& b) { return b.mode == GBSDF_MODE_EXACT_SIGNS; }
+bool learned_mode(const gbsdf_batch& b) { return b.mode == GBSDF_MODE_LEARNED; }
+
+void place_learned(Job& j, Carver& c) {
+    const Lattice& L = j.L;
+    j.S2 = c.take<uint32_t>((size_t)L.nwords * 4);
+    j.U2 = c.take<uint32_t>((size_t)L.nwords * 4);
+    j.E = c.take<uint32_t>((size_t)L.nwords * 4);
+    j.fbase = c.take<float>((size_t)L.nbricks * kBrickBase * 4);
+    j.fX = c.take<float>((size_t)L.nbricks * kMlpIn * 4);
+    j.logits = c.take<float>((size_t)L.nbricks * 4);
+    j.opencnt = c.take<unsigned>((size_t)L.nbricks * 4);
+    j.phist = c.take<unsigned>((size_t)kPropBins * 4);
+    j.ecap = edge_table_cap(j.T);
+    j.ekeys = c.take<unsigned long long>((size_t)j.ecap * 8);
+    j.ecnt = c.take<unsigned>((size_t)j.ecap * 4);
+}
 
 void place_phase1(Job& j, Carver& c) {
     const Lattice& L = j.L;
@@ -211,19 +239,26 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
     // [init] + [A]: one CTA per brick of the lattice, the surplus over the active count exits
     launch_fill(j.A, N, kFarSentinel, st);
     launch_splat(j.stt, j.boff, j.bcount, j.blist, j.active, -1, L, j.A, j.ds, st);
+    launch_band_error(j.stt, j.boff, j.bcount, j.blist, L, j.A, j.ds, st);
     // [B]
     launch_parity(j.ptt, j.soff, j.scount, j.slist, L, j.S, j.U, j.ds, xs ? 1 : 0, st);
-    // [C]: enough list passes to drain every voxel of the lattice
+    // [C]: enough list passes to drain every voxel of the lattice (learned mode records the
+    // voxels decided exactly in E, a feature of the sign-risk model)
+    const bool learned = learned_mode(b);
+    if (learned) cudaMemsetAsync(j.E, 0, (size_t)L.nwords * 4, st);
     const long long passes = std::min<long long>(64, (N + j.list_cap - 1) / j.list_cap + 1);
-    for (long long p = 0; p < passes; ++p) {
-        cudaMemsetAsync(&j.ds->listed, 0, sizeof(unsigned long long), st);
-        cudaMemsetAsync(&j.ds->list_overflow, 0, sizeof(unsigned long long), st);
-        cudaMemsetAsync(&j.ds->recheck_n, 0, sizeof(unsigned long long), st);
-        launch_list_unknown(j.U, j.S, L, j.list, j.list_cap, j.ds, 0, st);
-        launch_winding(&j.fwn, j.t9, T, L, j.list, j.list_cap, kGwnFixup, 0, j.S, j.recheck, j.list_cap, j.A, 0, stol,
-                       j.ds, b.num_sms, st);
-        launch_gwn_recheck(j.t9, T, L, j.recheck, j.list_cap, kGwnFixup, j.S, j.ds, b.num_sms, st);
-    }
+    auto fixup_passes = [&](uint32_t* ebits) {
+        for (long long p = 0; p < passes; ++p) {
+            cudaMemsetAsync(&j.ds->listed, 0, sizeof(unsigned long long), st);
+            cudaMemsetAsync(&j.ds->list_overflow, 0, sizeof(unsigned long long), st);
+            cudaMemsetAsync(&j.ds->recheck_n, 0, sizeof(unsigned long long), st);
+            launch_list_unknown(j.U, j.S, L, j.list, j.list_cap, j.ds, 0, st, ebits);
+            launch_winding(&j.fwn, j.t9, T, L, j.list, j.list_cap, kGwnFixup, 0, j.S, j.recheck, j.list_cap, j.A, 0,
+                           stol, j.ds, b.num_sms, st);
+            launch_gwn_recheck(j.t9, T, L, j.recheck, j.list_cap, kGwnFixup, j.S, j.ds, b.num_sms, st);
+        }
+    };
+    fixup_passes(learned ? j.E : nullptr);
     // [D]: the reference's round loop, stopped on the device when a round changes nothing
     float* src = j.A;
     float* dst = j.B;
@@ -247,13 +282,32 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
         launch_verify_plan(gen, j.ds, st);
         if (gen == kProbeGens - 1) break;
         launch_patch_mark(L, j.U, j.ds, st);
-        launch_list_unknown(j.U, j.S, L, j.list, j.list_cap, j.ds, 1, st);
+        launch_list_unknown(j.U, j.S, L, j.list, j.list_cap, j.ds, 1, st, learned ? j.E : nullptr);
         launch_winding(&j.fwn, j.t9, T, L, j.list, j.list_cap, kGwnFixup, 1, j.S, j.recheck, j.list_cap, j.A, 0,
                        stol, j.ds, b.num_sms, st);
         launch_gwn_recheck(j.t9, T, L, j.recheck, j.list_cap, kGwnFixup, j.S, j.ds, b.num_sms, st);
     }
+    // learned mode, as in the single-mesh path: the signed-crossing pass (its unknown
+    // columns are not counted), escalation of a diverged verify, the brick features, the
+    // network's scores and the budgeted proposals, re-decided by the exact winding number
+    if (learned) {
+        cudaMemcpyAsync(&j.ds->unknown_columns_kept, &j.ds->unknown_columns, 8, cudaMemcpyDeviceToDevice, st);
+        launch_parity(j.ptt, j.soff, j.scount, j.slist, L, j.S2, j.U2, j.ds, 1, st);
+        cudaMemcpyAsync(&j.ds->unknown_columns, &j.ds->unknown_columns_kept, 8, cudaMemcpyDeviceToDevice, st);
+        launch_escalate(j.ds, j.S, j.U, j.S2, j.U2, L, b.num_sms, st);
+        fixup_passes(j.E);
+        cudaMemsetAsync(j.ekeys, 0, (size_t)j.ecap * 8, st);
+        cudaMemsetAsync(j.ecnt, 0, (size_t)j.ecap * 4, st);
+        cudaMemsetAsync(j.opencnt, 0, (size_t)L.nbricks * 4, st);
+        launch_open_edges(j.t12, T, L, j.ekeys, j.ecnt, j.ecap, j.opencnt, st);
+        launch_brick_features(j.A, j.S, j.E, j.S2, j.U2, j.bcount, j.opencnt, L, j.fbase, j.fX, st);
+        launch_mlp_forward(b.mlp_params, j.fX, L.nbricks, j.logits, st);
+        const unsigned budget = b.budget > 0 ? b.budget : (unsigned)std::max<long long>(1, L.nbricks / 16);
+        launch_propose_dev(j.logits, L, b.logit_thr, budget, j.phist, j.ds, j.U, st);
+        fixup_passes(nullptr);
+    }
     // [F], written only when the build passed its checks
-    launch_batch_finalize(j.ds, 1, st);
+    launch_batch_finalize(j.ds, learned ? 0 : 1, st);
     launch_apply(j.A, j.S, L, b.out_dev ? j.out : j.B, j.ds, xs ? stol * L.h : 0.0f, st);
     if (!b.out_dev) cudaMemcpyAsync(j.hout, j.B, (size_t)N * 4, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(j.hs, j.ds, sizeof(DevState), cudaMemcpyDeviceToHost, st);
@@ -275,12 +329,16 @@ int plan(gbsdf_batch& b, BErr& e) {
     // phase 1 buffers
     Carver c1;
     for (Job& j : b.jobs)
-        if (j.pre_status == GBSDF_OK) place_phase1(j, c1);
+        if (j.pre_status == GBSDF_OK) {
+            place_phase1(j, c1);
+            if (learned_mode(b)) place_learned(j, c1);
+        }
     GBB_CK(cudaMalloc(&b.arena1, std::max<size_t>(c1.off, 256)));
     Carver p1{static_cast<char*>(b.arena1), 0};
     for (Job& j : b.jobs)
         if (j.pre_status == GBSDF_OK) {
             place_phase1(j, p1);
+            if (learned_mode(b)) place_learned(j, p1);
             encode_grid_map(j.map_a, j.A, j.L);
             encode_grid_map(j.map_b, j.B, j.L);
             const SweepPlan plan = tuned_sweep_plan(b.device, j.L, j.A, j.B, &j.map_a, j.ds, b.origin, false, 0);
@@ -372,9 +430,8 @@ int status_of(const gbsdf_batch& b, const Job& j, bool& overflow) {
     }
     if (h.wait_timeouts) return GBSDF_ECUDA;
     if (h.invalid_tris > 0) return GBSDF_EINVAL;
-    if (h.csr_entries == 0 || h.csr_entries > 100000000ull) return GBSDF_ECSR;
+    if (!learned_mode(b) && (h.csr_entries == 0 || h.csr_entries > 100000000ull)) return GBSDF_ECSR;
     if (h.verify_state != 1) return GBSDF_EVERIFY;
-    (void)b;
     return GBSDF_OK;
 }
 
@@ -402,6 +459,10 @@ void fill_stats(const Job& j, int status, float ms, unsigned long long launches,
     s->csr_entries = (long long)h.csr_entries;
     s->winding_certified = (long long)h.fwn_certified;
     s->winding_summed = (long long)h.fwn_fallback_total;
+    s->proposed = (long long)h.proposed;
+    s->escalated = h.escalated;
+    std::memcpy(&s->band_err_fp64, &h.band_err_bits, sizeof(double));
+    s->band_err_samples = (long long)h.band_err_n;
     s->sweep_schedule = (j.map_a.valid ? (j.xsched1 == kXAuto ? kXTmaPipe : j.xsched1) : kXCpAsync) +
                         10 * (j.map_a.walk_valid ? (j.wsched1 == kWAuto ? kWTmaPipe : j.wsched1) : kWCpAsync);
 }
@@ -479,8 +540,10 @@ int gbsdf_batch_create(const gbsdf_mesh_desc* meshes, int32_t n_meshes, int32_t 
     gbsdf_options o;
     gbsdf_default_options(&o);
     if (opt) o = *opt;
-    if (o.mode != GBSDF_MODE_REFERENCE && o.mode != GBSDF_MODE_EXACT_SIGNS)
-        return e.set(GBSDF_EINVAL, "planned batches run the reference or exact-signs mode");
+    if (o.mode != GBSDF_MODE_REFERENCE && o.mode != GBSDF_MODE_EXACT_SIGNS && o.mode != GBSDF_MODE_LEARNED)
+        return e.set(GBSDF_EINVAL, "planned batches run the reference, exact-signs or learned mode");
+    if (o.mode == GBSDF_MODE_LEARNED && !o.mlp_params)
+        return e.set(GBSDF_EINVAL, "a learned batch needs mlp_params (device memory)");
     if (o.path == GBSDF_PATH_LEGACY) return e.set(GBSDF_EINVAL, "planned batches run the fast path");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
@@ -493,6 +556,12 @@ int gbsdf_batch_create(const gbsdf_mesh_desc* meshes, int32_t n_meshes, int32_t 
     b->device = o.device;
     b->mode = o.mode;
     b->sweep_schedule = o.sweep_schedule;
+    if (o.mode == GBSDF_MODE_LEARNED) {
+        const float pthr = (o.mlp_threshold > 0.0f && o.mlp_threshold < 1.0f) ? o.mlp_threshold : 0.5f;
+        b->mlp_params = o.mlp_params;
+        b->logit_thr = logf(pthr / (1.0f - pthr));
+        b->budget = o.mlp_budget > 0 ? (unsigned)o.mlp_budget : 0u;
+    }
     b->out_dev = out_on_device != 0;
     b->tris_dev = o.tris_on_device != 0;
     auto fail = [&](int rc) {

@@ -248,13 +248,28 @@ int fixup_unknown(Workspace& w, const Lattice& L, long long T, float stol, Err& 
     return e.set(GBSDF_ECUDA, "unknown-voxel fixup did not drain");
 }
 
-// Learned-model brick features into w.fX, from the unsigned distance field (w.A), the
-// plain path's signs (w.S), the exact-decided mask (w.E) and a second, signed-crossing
-// parity pass (w.S2 / w.U2); runs after the verify / patch stage.
-int brick_features(Workspace& w, long long T, const Lattice& L, Err& e) {
+// The signed-crossing parity pass into w.S2 / w.U2 (learned mode: the escalation's signs
+// and a feature input). It adds its unknown columns to the state's count; the reference
+// pass's count is kept.
+int signed_pass(Workspace& w, const Lattice& L, Err& e) {
     cudaStream_t st = w.st;
     GB_CK(ensure(w.S2, (size_t)L.nwords * 4));
     GB_CK(ensure(w.U2, (size_t)L.nwords * 4));
+    GB_CK(cudaMemcpyAsync(&w.hs->unknown_columns, &w.ds->unknown_columns, 8, cudaMemcpyDeviceToHost, st));
+    GB_CK(cudaStreamSynchronize(st));
+    const unsigned long long unk_ref = w.hs->unknown_columns;
+    launch_parity(P<ParTri>(w.ptt), P<unsigned long long>(w.soff), P<unsigned>(w.scount), P<unsigned>(w.slist), L,
+                  P<uint32_t>(w.S2), P<uint32_t>(w.U2), w.ds, 1, st);
+    GB_CK(cudaMemcpyAsync(&w.ds->unknown_columns, &unk_ref, 8, cudaMemcpyHostToDevice, st));
+    GB_CK(cudaGetLastError());
+    return GBSDF_OK;
+}
+
+// Learned-model brick features into w.fX, from the unsigned distance field (w.A), the
+// current signs (w.S), the exact-decided mask (w.E) and the signed-crossing pass
+// (w.S2 / w.U2, signed_pass).
+int brick_features(Workspace& w, long long T, const Lattice& L, Err& e) {
+    cudaStream_t st = w.st;
     GB_CK(ensure(w.fbase, (size_t)L.nbricks * kBrickBase * 4));
     GB_CK(ensure(w.fX, (size_t)L.nbricks * kMlpIn * 4));
     GB_CK(ensure(w.opencnt, (size_t)L.nbricks * 4));
@@ -264,8 +279,6 @@ int brick_features(Workspace& w, long long T, const Lattice& L, Err& e) {
     GB_CK(cudaMemsetAsync(w.ekeys.p, 0, (size_t)cap * 8, st));
     GB_CK(cudaMemsetAsync(w.ecnt.p, 0, (size_t)cap * 4, st));
     GB_CK(cudaMemsetAsync(w.opencnt.p, 0, (size_t)L.nbricks * 4, st));
-    launch_parity(P<ParTri>(w.ptt), P<unsigned long long>(w.soff), P<unsigned>(w.scount), P<unsigned>(w.slist), L,
-                  P<uint32_t>(w.S2), P<uint32_t>(w.U2), w.ds, 1, st);
     launch_open_edges(P<float>(w.t12), T, L, P<unsigned long long>(w.ekeys), P<unsigned>(w.ecnt), cap,
                       P<unsigned>(w.opencnt), st);
     launch_brick_features(P<float>(w.A), P<uint32_t>(w.S), P<uint32_t>(w.E), P<uint32_t>(w.S2), P<uint32_t>(w.U2),
@@ -345,6 +358,8 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     launch_fill(P<float>(w.A), N, kFarSentinel, st);
     launch_splat(P<SplatTri>(w.stt), P<unsigned long long>(w.boff), P<unsigned>(w.bcount), P<unsigned>(w.blist),
                  P<unsigned>(w.active), n_active, L, P<float>(w.A), w.ds, st);
+    launch_band_error(P<SplatTri>(w.stt), P<unsigned long long>(w.boff), P<unsigned>(w.bcount), P<unsigned>(w.blist), L,
+                      P<float>(w.A), w.ds, st);
     GB_CK(cudaGetLastError());
     GB_CK(cudaEventRecord(w.ev[3], st));
     // ---- [B]
@@ -441,16 +456,23 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
                            w.ds, w.num_sms, st);
     }
     GB_CK(cudaGetLastError());
-    // ---- learned proposals: the riskiest bricks re-decided by the exact winding number
-    // (after [E], so the probes and patch boxes ran exactly as in the plain path)
+    // ---- learned mode, after [E] (the probes and patch boxes ran exactly as in the plain
+    // path): the signed-crossing pass; a diverged verify escalates to its signs, its columns
+    // through holes decided by the exact winding number, instead of declining; then the
+    // brick features, the network's scores and the riskiest bricks re-decided by the exact
+    // winding number. The network never supplies a sign.
     if (learned || features_out) {
-        // the signed pass counts unknown columns too; keep the reference pass's count
-        GB_CK(cudaMemcpyAsync(&w.hs->unknown_columns, &w.ds->unknown_columns, 8, cudaMemcpyDeviceToHost, st));
-        GB_CK(cudaStreamSynchronize(st));
-        const unsigned long long unk_ref = w.hs->unknown_columns;
+        int rcs = signed_pass(w, L, e);
+        if (rcs != GBSDF_OK) return rcs;
+        if (learned) {
+            launch_escalate(w.ds, P<uint32_t>(w.S), P<uint32_t>(w.U), P<uint32_t>(w.S2), P<uint32_t>(w.U2), L,
+                            w.num_sms, st);
+            GB_CK(cudaGetLastError());
+            int rce = fixup_unknown(w, L, T, stol, e, ebits, fwn);
+            if (rce != GBSDF_OK) return rce;
+        }
         int rcf = brick_features(w, T, L, e);
         if (rcf != GBSDF_OK) return rcf;
-        GB_CK(cudaMemcpyAsync(&w.ds->unknown_columns, &unk_ref, 8, cudaMemcpyHostToDevice, st));
         if (features_out) {
             GB_CK(cudaMemcpyAsync(features_out, w.fX.p, (size_t)L.nbricks * kMlpIn * 4, cudaMemcpyDeviceToDevice, st));
             GB_CK(cudaStreamSynchronize(st));
@@ -468,13 +490,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         const unsigned budget =
             o.mlp_budget > 0 ? (unsigned)o.mlp_budget : (unsigned)std::max<long long>(1, L.nbricks / 16);
         GB_CK(ensure(w.phist, (size_t)kPropBins * 4));
-        GB_CK(cudaMemsetAsync(w.phist.p, 0, (size_t)kPropBins * 4, st));
-        launch_propose_hist(logits, L.nbricks, lthr, P<unsigned>(w.phist), st);
-        std::vector<unsigned> hist(kPropBins);
-        GB_CK(cudaMemcpyAsync(hist.data(), w.phist.p, (size_t)kPropBins * 4, cudaMemcpyDeviceToHost, st));
-        GB_CK(cudaStreamSynchronize(st));
-        const int cut = propose_cut_bin(hist.data(), budget);
-        launch_propose(logits, L, lthr, cut, &w.ds->proposed, P<uint32_t>(w.U), st);
+        launch_propose_dev(logits, L, lthr, budget, P<unsigned>(w.phist), w.ds, P<uint32_t>(w.U), st);
         GB_CK(cudaGetLastError());
         int rcp = fixup_unknown(w, L, T, stol, e, nullptr, fwn);
         if (rcp != GBSDF_OK) return rcp;
@@ -543,6 +559,9 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         stats->csr_entries = (long long)h.csr_entries;
         stats->path_taken = GBSDF_PATH_FAST;
         stats->proposed = (long long)h.proposed;
+        stats->escalated = h.escalated;
+        std::memcpy(&stats->band_err_fp64, &h.band_err_bits, sizeof(double));
+        stats->band_err_samples = (long long)h.band_err_n;
         stats->winding_certified = (long long)h.fwn_certified;
         stats->winding_summed = (long long)h.fwn_fallback_total;
         // x schedule + 10 x walk schedule of the last round's sweeps
@@ -636,9 +655,9 @@ int compute(const float* tris12, long long T, bool tris_dev, float h, const int3
     const long long N = dims[0] * dims[1] * dims[2];
     int path = o.path;
     if (path == GBSDF_PATH_AUTO) path = ((unsigned long long)N >= kFastMinVoxels) ? GBSDF_PATH_FAST : GBSDF_PATH_LEGACY;
-    // the reference's int-range guards (cuda_rasterizer.cu:816-820): reference and learned
-    // modes (the engine indexes in 64 bits; exact-signs and exact modes serve such lattices)
-    if (path == GBSDF_PATH_FAST && (o.mode == GBSDF_MODE_REFERENCE || o.mode == GBSDF_MODE_LEARNED)) {
+    // the reference's int-range guards (cuda_rasterizer.cu:816-820): reference mode only (the
+    // engine indexes in 64 bits; the other modes serve such lattices)
+    if (path == GBSDF_PATH_FAST && o.mode == GBSDF_MODE_REFERENCE) {
         const long long G = 2000000000LL;
         if (N > G || T * dims[2] > G || dims[0] * dims[1] > G || dims[0] * dims[2] > G || dims[1] * dims[2] > G) {
             if (o.path != GBSDF_PATH_AUTO)
@@ -726,7 +745,8 @@ int gbsdf_compute_mesh_sdf_batch(gbsdf_mesh_desc* meshes, int32_t n_meshes, int3
     gbsdf_options o;
     gbsdf_default_options(&o);
     if (opt) o = *opt;
-    if (o.path == GBSDF_PATH_FAST && (o.mode == GBSDF_MODE_REFERENCE || o.mode == GBSDF_MODE_EXACT_SIGNS)) {
+    if (o.path == GBSDF_PATH_FAST && (o.mode == GBSDF_MODE_REFERENCE || o.mode == GBSDF_MODE_EXACT_SIGNS ||
+                                      (o.mode == GBSDF_MODE_LEARNED && o.mlp_params && !o.brick_scores))) {
         gbsdf_batch* b = nullptr;
         int rc = gbsdf_batch_create(meshes, n_meshes, out_on_device, &o, &b, err, errlen);
         if (rc != GBSDF_OK) return rc;

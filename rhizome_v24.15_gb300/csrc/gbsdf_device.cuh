@@ -4,11 +4,14 @@
 // Every translation unit of the engine is compiled with -fmad=false: products
 // and sums round separately, in the operation order of the reference's
 // expressions (native/src/core/math_utils.cuh, native/src/engine/sdf/
-// cuda_rasterizer.cu), so band distances, parity hits and eikonal updates are
-// bit-identical to a contraction-free CPU evaluation of the same formulas.
-// Where speed matters more than bit-identity (the FP32 winding sum, whose
-// sign decisions are re-checked in FP64 near the threshold), fused
-// multiply-adds are written explicitly with __fmaf_rn.
+// cuda_rasterizer.cu), and every fused multiply-add is written out with
+// __fmaf_rn. The parity edge functions and hit heights and the Godunov update
+// fuse exactly the products that the reference's own build (nvcc's default
+// contraction) fuses, so they are bit-identical to the reference's kernels; the
+// band distances round as a contraction-free evaluation (within 1e-5 voxel of
+// the reference's). Where speed matters more than bit-identity (the FP32 winding
+// sum, whose sign decisions are re-checked in FP64 near the threshold), fused
+// multiply-adds are chosen freely.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -151,6 +154,42 @@ __device__ __forceinline__ float div3_pos(float x) {
     const float r3 = 0.333333343267440796f;  // RN(1/3)
     const float q = x * r3;
     return __fmaf_rn(__fmaf_rn(-3.0f, q, x), r3, q);
+}
+
+// The same squared distance in FP64 (Ericson's regions, Real-Time Collision Detection
+// 5.1.5), for the band error statement: the point and vertices are the FP32 inputs, every
+// operation FP64.
+__device__ __forceinline__ double ptd_sq_f64(double px, double py, double pz, const float* v) {
+    const double ax = v[0], ay = v[1], az = v[2], bx = v[3], by = v[4], bz = v[5], cx = v[6], cy = v[7], cz = v[8];
+    const double abx = bx - ax, aby = by - ay, abz = bz - az, acx = cx - ax, acy = cy - ay, acz = cz - az;
+    const double apx = px - ax, apy = py - ay, apz = pz - az;
+    auto d2 = [](double x, double y, double z) { return x * x + y * y + z * z; };
+    const double d1 = abx * apx + aby * apy + abz * apz, d2v = acx * apx + acy * apy + acz * apz;
+    if (d1 <= 0.0 && d2v <= 0.0) return d2(apx, apy, apz);
+    const double bpx = px - bx, bpy = py - by, bpz = pz - bz;
+    const double d3 = abx * bpx + aby * bpy + abz * bpz, d4 = acx * bpx + acy * bpy + acz * bpz;
+    if (d3 >= 0.0 && d4 <= d3) return d2(bpx, bpy, bpz);
+    const double vc = d1 * d4 - d3 * d2v;
+    if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
+        const double t = d1 / (d1 - d3);
+        return d2(px - (ax + t * abx), py - (ay + t * aby), pz - (az + t * abz));
+    }
+    const double cpx = px - cx, cpy = py - cy, cpz = pz - cz;
+    const double d5 = abx * cpx + aby * cpy + abz * cpz, d6 = acx * cpx + acy * cpy + acz * cpz;
+    if (d6 >= 0.0 && d5 <= d6) return d2(cpx, cpy, cpz);
+    const double vb = d5 * d2v - d1 * d6;
+    if (vb <= 0.0 && d2v >= 0.0 && d6 <= 0.0) {
+        const double t = d2v / (d2v - d6);
+        return d2(px - (ax + t * acx), py - (ay + t * acy), pz - (az + t * acz));
+    }
+    const double va = d3 * d6 - d5 * d4;
+    if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0) {
+        const double t = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        return d2(px - (bx + t * (cx - bx)), py - (by + t * (cy - by)), pz - (bz + t * (cz - bz)));
+    }
+    const double den = 1.0 / (va + vb + vc);
+    const double sv = vb * den, sw = vc * den;
+    return d2(px - (ax + abx * sv + acx * sw), py - (ay + aby * sv + acy * sw), pz - (az + abz * sv + acz * sw));
 }
 
 // Three-input minimum and maximum (PTX ISA 8.8, sm_100 and later): for operands that are

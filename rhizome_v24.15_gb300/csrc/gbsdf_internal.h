@@ -54,6 +54,9 @@ struct DevState {
     unsigned long long band_voxels;
     unsigned long long splat_evals;    // exact point-triangle evaluations
     unsigned long long unknown_columns;
+    unsigned long long unknown_columns_kept;  // learned batches: the reference pass's count
+    unsigned long long band_err_bits;  // largest |FP32 - FP64| band distance of the samples (double bits)
+    unsigned long long band_err_n;     // band voxels sampled for it
     unsigned long long listed;         // voxels listed for an exact winding evaluation
     unsigned long long list_overflow;
     unsigned long long fixup_voxels;
@@ -81,6 +84,8 @@ struct DevState {
     int total_sites;
     int patch_rounds;
     unsigned proposed;                 // learned mode: bricks the network proposed
+    int prop_cut;                      // learned mode: lowest logit bin proposed (device-side budget)
+    int escalated;                     // learned mode: the verify diverged, signs re-decided exactly
     int abort_;                        // batches: the build failed a check, write no output
     long long sites[4096];
 };
@@ -122,6 +127,13 @@ void launch_active_bricks(const unsigned* brick_count, long long nbricks, unsign
 void launch_fill(float* g, long long n, float value, cudaStream_t st);
 // n_active < 0: the active-brick count is read on the device (one CTA per brick of the
 // lattice is launched and the surplus exits), so the launch needs no host round trip.
+// The band splat's error against FP64: kBandErrSamples voxels at fixed, evenly spread
+// lattice positions; those in the band (splat value <= 8h) get the FP64 distance to their
+// brick's binned triangles (the splat's own candidates) and the largest difference, in
+// voxels, goes to DevState::band_err_bits / band_err_n.
+constexpr long long kBandErrSamples = 16384;
+void launch_band_error(const SplatTri* stt, const unsigned long long* brick_off, const unsigned* brick_count,
+                       const unsigned* brick_list, const Lattice& L, const float* dist, DevState* ds, cudaStream_t st);
 void launch_splat(const SplatTri* stt, const unsigned long long* brick_off, const unsigned* brick_count,
                   const unsigned* brick_list, const unsigned* active, long long n_active, const Lattice& L,
                   float* dist, DevState* ds, cudaStream_t st);
@@ -290,13 +302,20 @@ void launch_mlp_backward(const float* P, const float* X, const float* y, const f
 void launch_adam(float* P, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps,
                  float scale, int step, cudaStream_t st);
 // learned proposals: logit histogram (kPropBins bins above the threshold), the cut bin
-// that keeps the proposal count within the budget (host), then the marking pass
+// that keeps the proposal count within the budget, then the marking pass
 constexpr int kPropBins = 4096;
 constexpr float kPropScale = 128.0f;
 void launch_propose_hist(const float* logits, long long nb, float logit_thr, unsigned* hist, cudaStream_t st);
-int propose_cut_bin(const unsigned* hist, unsigned budget);
-void launch_propose(const float* logits, const Lattice& L, float logit_thr, int cut_bin, unsigned* n_prop, uint32_t* U,
-                    cudaStream_t st);
+// Proposals with the budget's cut taken on the device (no host round trip): the bricks above
+// the logit threshold, the highest-scoring ones first, at most `budget` of them, marked
+// unknown in U (hist: kPropBins scratch counters).
+void launch_propose_dev(const float* logits, const Lattice& L, float logit_thr, unsigned budget, unsigned* hist,
+                        DevState* ds, uint32_t* U, cudaStream_t st);
+// Learned mode: when the verify diverged, take the signed-crossing pass's signs (S2) and
+// unknown columns (U2) in place of S / U and mark the state clean and escalated.
+void launch_escalate(DevState* ds, uint32_t* S, uint32_t* U, const uint32_t* S2, const uint32_t* U2,
+                     const Lattice& L, int num_sms, cudaStream_t st);
+
 void launch_selftest_div3(unsigned long long* mism, cudaStream_t st);
 
 }  // namespace gbsdf

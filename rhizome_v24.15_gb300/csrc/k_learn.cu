@@ -349,8 +349,8 @@ __global__ void adam_kernel(float* __restrict__ P, const float* __restrict__ g, 
 
 // ---- proposals: mark every voxel of a risky brick unknown (exact winding next) ---------
 // Deterministic budget: bricks above the threshold are binned by logit (kPropBins bins of
-// 1/kPropScale); the host picks the lowest bin whose bricks, together with all higher
-// bins, still fit the budget, and every brick at or above it is proposed.
+// 1/kPropScale); the lowest bin whose bricks, together with all higher bins, still fit the
+// budget is picked on the device, and every brick at or above it is proposed.
 __device__ __forceinline__ int prop_bin(float logit, float thr) {
     return (int)fminf((float)(kPropBins - 1), (logit - thr) * kPropScale);
 }
@@ -364,12 +364,29 @@ __global__ void propose_hist_kernel(const float* __restrict__ logits, long long 
     atomicAdd(&hist[prop_bin(z, logit_thr)], 1u);
 }
 
-__global__ void propose_kernel(const float* __restrict__ logits, Lattice L, float logit_thr, int cut_bin,
-                               unsigned* __restrict__ n_prop, uint32_t* __restrict__ U) {
+// The budget's cut on the device, so a build needs no host round trip between scoring and
+// proposing.
+__global__ void propose_cut_kernel(const unsigned* __restrict__ hist, unsigned budget, int* __restrict__ cut) {
+    unsigned long long total = 0;
+    int c = 0;
+    for (int b = kPropBins - 1; b >= 0; --b) {
+        if (total + hist[b] > budget) {
+            c = b + 1;
+            break;
+        }
+        total += hist[b];
+    }
+    *cut = c;
+}
+
+__global__ void propose_dev_kernel(const float* __restrict__ logits, Lattice L, float logit_thr,
+                                   const int* __restrict__ cut, unsigned* __restrict__ n_prop,
+                                   uint32_t* __restrict__ U) {
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= L.nbricks) return;
     const float z = logits[b];
-    if (!(z > logit_thr) || prop_bin(z, logit_thr) < cut_bin) return;
+    const int cut_bin = *cut;
+    if (cut_bin >= kPropBins || !(z > logit_thr) || prop_bin(z, logit_thr) < cut_bin) return;
     atomicAdd(n_prop, 1u);
     const int nbx = L.nb[0], nby = L.nb[1];
     const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((long long)nbx * nby));
@@ -381,7 +398,49 @@ __global__ void propose_kernel(const float* __restrict__ logits, Lattice L, floa
             atomicOr(&U[((size_t)z3 * L.dims[1] + y) * L.wx + (x0 >> 5)], mask);
 }
 
+// Escalation of a diverged verify (learned mode): the signs become the signed-crossing
+// pass's (the winding number along near-lattice rays) and its unknown columns -- rays
+// through holes -- are listed for the exact winding number. The decision is read by
+// every block before the state is marked, in a kernel of its own.
+__global__ void escalate_copy_kernel(const DevState* __restrict__ ds, uint32_t* __restrict__ S,
+                                     uint32_t* __restrict__ U, const uint32_t* __restrict__ S2,
+                                     const uint32_t* __restrict__ U2, long long nwords) {
+    if (ds->verify_state == 1) return;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += stride) {
+        S[i] = S2[i];
+        U[i] = U2[i];
+    }
+}
+
+__global__ void escalate_mark_kernel(DevState* ds) {
+    if (ds->verify_state == 1) return;
+    ds->escalated = 1;
+    ds->verify_state = 1;
+}
+
 }  // namespace
+
+void launch_propose_dev(const float* logits, const Lattice& L, float logit_thr, unsigned budget, unsigned* hist,
+                        DevState* ds, uint32_t* U, cudaStream_t st) {
+    if (L.nbricks <= 0) return;
+    cudaMemsetAsync(hist, 0, (size_t)kPropBins * 4, st);
+    launch_propose_hist(logits, L.nbricks, logit_thr, hist, st);
+    GBSDF_COUNT_LAUNCH();
+    propose_cut_kernel<<<1, 1, 0, st>>>(hist, budget, &ds->prop_cut);
+    GBSDF_COUNT_LAUNCH();
+    propose_dev_kernel<<<(unsigned)((L.nbricks + 255) / 256), 256, 0, st>>>(logits, L, logit_thr, &ds->prop_cut,
+                                                                             &ds->proposed, U);
+}
+
+void launch_escalate(DevState* ds, uint32_t* S, uint32_t* U, const uint32_t* S2, const uint32_t* U2,
+                     const Lattice& L, int num_sms, cudaStream_t st) {
+    GBSDF_COUNT_LAUNCH();
+    const long long blocks = std::min<long long>((L.nwords + 255) / 256, (long long)num_sms * 8);
+    escalate_copy_kernel<<<(unsigned)std::max<long long>(blocks, 1), 256, 0, st>>>(ds, S, U, S2, U2, L.nwords);
+    GBSDF_COUNT_LAUNCH();
+    escalate_mark_kernel<<<1, 1, 0, st>>>(ds);
+}
 
 long long edge_table_cap(long long T) {
     long long need = 6 * T + 1024, cap = 1024;
@@ -437,22 +496,6 @@ void launch_propose_hist(const float* logits, long long nb, float logit_thr, uns
     if (nb <= 0) return;
     GBSDF_COUNT_LAUNCH();
     propose_hist_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(logits, nb, logit_thr, hist);
-}
-
-int propose_cut_bin(const unsigned* hist, unsigned budget) {
-    unsigned long long total = 0;
-    for (int b = kPropBins - 1; b >= 0; --b) {
-        if (total + hist[b] > budget) return b + 1;
-        total += hist[b];
-    }
-    return 0;
-}
-
-void launch_propose(const float* logits, const Lattice& L, float logit_thr, int cut_bin, unsigned* n_prop, uint32_t* U,
-                    cudaStream_t st) {
-    if (cut_bin >= kPropBins || L.nbricks <= 0) return;
-    GBSDF_COUNT_LAUNCH();
-    propose_kernel<<<(unsigned)((L.nbricks + 255) / 256), 256, 0, st>>>(logits, L, logit_thr, cut_bin, n_prop, U);
 }
 
 }  // namespace gbsdf

@@ -456,6 +456,58 @@ void launch_fill(float* g, long long n, float value, cudaStream_t st) {
     if (n4 * 4 < n) { GBSDF_COUNT_LAUNCH(); fill_tail_kernel<<<1, 4, 0, st>>>(g, n4 * 4, n, value); }
 }
 
+namespace {
+// One warp per sample: the lanes split the brick's triangle list, find the FP32 minimum
+// (the splat's arithmetic), then evaluate in FP64 only the triangles whose FP32 squared
+// distance lies within 0.1% (plus 1e-6 h^2) of it -- the FP64 minimum is among them.
+constexpr int kBandErrWarps = 4;
+__global__ void __launch_bounds__(kBandErrWarps * 32)
+    band_error_kernel(const SplatTri* __restrict__ stt, const unsigned long long* __restrict__ boff,
+                      const unsigned* __restrict__ bcount, const unsigned* __restrict__ blist, Lattice L,
+                      const float* __restrict__ dist, DevState* ds) {
+    const long long k = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (k >= kBandErrSamples) return;
+    const long long v = (long long)(((double)k + 0.5) * (double)L.N / (double)kBandErrSamples);
+    if (v >= L.N) return;
+    const float d = dist[v];
+    if (!(d <= (float)kBandVoxels * L.h)) return;
+    const int x = (int)(v % L.dims[0]);
+    const long long r = v / L.dims[0];
+    const int y = (int)(r % L.dims[1]), z = (int)(r / L.dims[1]);
+    const long long b = ((long long)(z / kBrick) * L.nb[1] + y / kBrick) * L.nb[0] + x / kBrick;
+    const f3 p = lattice_point(L.mn[0], L.mn[1], L.mn[2], x, y, z, L.h);
+    const unsigned long long e0 = boff[b], n = bcount[b];
+    float m32 = 3.0e38f;
+    for (unsigned long long e = lane; e < n; e += 32) {
+        const float* t = stt[blist[e0 + e]].v;
+        m32 = fminf(m32, ptd_sq(p, mk(t[0], t[1], t[2]), mk(t[3], t[4], t[5]), mk(t[6], t[7], t[8])));
+    }
+    for (int o = 16; o > 0; o >>= 1) m32 = fminf(m32, __shfl_xor_sync(0xffffffffu, m32, o));
+    const float lim = m32 + m32 * 1e-3f + 1e-6f * L.h * L.h;
+    double best = 1e300;
+    for (unsigned long long e = lane; e < n; e += 32) {
+        const float* t = stt[blist[e0 + e]].v;
+        if (ptd_sq(p, mk(t[0], t[1], t[2]), mk(t[3], t[4], t[5]), mk(t[6], t[7], t[8])) <= lim)
+            best = fmin(best, ptd_sq_f64(p.x, p.y, p.z, t));
+    }
+    for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if (lane == 0) {
+        const double err = fabs(sqrt(best) - (double)d) / (double)L.h;
+        atomicMax(&ds->band_err_bits, (unsigned long long)__double_as_longlong(err));
+        atomicAdd(&ds->band_err_n, 1ull);
+    }
+}
+}  // namespace
+
+void launch_band_error(const SplatTri* stt, const unsigned long long* brick_off, const unsigned* brick_count,
+                       const unsigned* brick_list, const Lattice& L, const float* dist, DevState* ds, cudaStream_t st) {
+    if (L.N <= 0) return;
+    GBSDF_COUNT_LAUNCH();
+    band_error_kernel<<<(unsigned)((kBandErrSamples + kBandErrWarps - 1) / kBandErrWarps), kBandErrWarps * 32, 0,
+                        st>>>(stt, brick_off, brick_count, brick_list, L, dist, ds);
+}
+
 void launch_splat(const SplatTri* stt, const unsigned long long* brick_off, const unsigned* brick_count,
                   const unsigned* brick_list, const unsigned* active, long long n_active, const Lattice& L,
                   float* dist, DevState* ds, cudaStream_t st) {

@@ -42,10 +42,11 @@ class Stats(C.Structure):
                 ("band_voxels", C.c_int64), ("splat_evals", C.c_int64), ("gwn_pairs", C.c_int64),
                 ("brick_pairs", C.c_int64), ("csr_entries", C.c_int64), ("kernel_launches", C.c_int64),
                 ("proposed", C.c_int64), ("sweep_schedule", C.c_int64), ("winding_certified", C.c_int64),
-                ("winding_summed", C.c_int64), ("reserved", C.c_int64 * 3)]
+                ("winding_summed", C.c_int64), ("escalated", C.c_int64), ("band_err_fp64", C.c_double),
+                ("band_err_samples", C.c_int64)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "pad0")}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad0"}
 
 
 class MeshDesc(C.Structure):

@@ -199,7 +199,8 @@ class Batch:
     The arrays are referenced, not copied: their contents may change between runs, their
     sizes may not."""
 
-    def __init__(self, meshes, outs=None, mode=MODE_REFERENCE, device=0, sweep_schedule=0):
+    def __init__(self, meshes, outs=None, mode=MODE_REFERENCE, device=0, sweep_schedule=0, mlp_params=None,
+                 mlp_budget=None, mlp_threshold=None):
         n = len(meshes)
         self.n = n
         self._descs = (_lib.MeshDesc * n)()
@@ -227,6 +228,8 @@ class Batch:
         L.gbsdf_default_options(C.byref(o))
         o.mode, o.path, o.device, o.tris_on_device = int(mode), int(PATH_FAST), int(device), int(bool(tdev))
         o.sweep_schedule = int(sweep_schedule)
+        # learned mode: the network's parameters stay referenced for the batch's lifetime
+        self._mlp = _set_learned(o, mode, device, mlp_params, mlp_budget, mlp_threshold)
         self._h = C.c_void_p()
         err = C.create_string_buffer(512)
         rc = L.gbsdf_batch_create(self._descs, n, int(bool(odev)), C.byref(o), C.byref(self._h), err, len(err))

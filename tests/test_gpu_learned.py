@@ -206,3 +206,83 @@ def test_ablation_learned_vs_plain_vs_random(engine):
     assert tot["learned"] <= tot["random"] <= tot["plain"]
     assert tot["learned"] < 0.5 * tot["plain"], tot
     assert tot["plain"] - tot["learned"] > 3 * (tot["plain"] - tot["random"]), tot
+
+
+def test_learned_mode_matches_oracle_with_given_proposals(engine, oracle):
+    """Learned mode with caller-supplied brick scores (the proposals known exactly) against
+    the oracle composed stage by stage: the reference fast path, then every voxel of the
+    proposed bricks re-decided by the exact winding number (on-surface voxels inside), then
+    the signs applied to the same unsigned field. Bit for bit."""
+    from gbsdf import MODE_LEARNED, PATH_FAST, compute_mesh_sdf, learn
+
+    tris, h, mn, mx = _mesh(81, grid=56)
+    dims = mx.astype(np.int64) - mn + 1
+    nb = learn.brick_grid(mn, mx)
+    n_b = int(np.prod(nb))
+    rng = np.random.default_rng(9)
+    pick = rng.choice(n_b, size=max(1, n_b // 10), replace=False)
+    scores = np.full(n_b, -10.0, np.float32)
+    scores[pick] = 10.0
+    out, res = compute_mesh_sdf(tris, h, mn, mx, mode=MODE_LEARNED, path=PATH_FAST, brick_scores=scores,
+                                mlp_budget=len(pick), mlp_threshold=0.5)
+    assert res.ok and res.stats["proposed"] == len(pick) and res.stats["escalated"] == 0
+    st, ref, sign, _ = oracle.fast_sdf(tris, h, mn, mx, fsm_mode=0, gwn_mode=1)
+    assert st == oracle.OK
+    unsigned = np.abs(ref)
+    s2 = sign.copy()
+    vox = s2.reshape(dims[2], dims[1], dims[0])
+    for b in pick:
+        bx, by, bz = b % nb[0], (b // nb[0]) % nb[1], b // (nb[0] * nb[1])
+        vox[bz * 8:bz * 8 + 8, by * 8:by * 8 + 8, bx * 8:bx * 8 + 8] = 2
+    oracle.fixup_unknown(tris, h, mn, dims, s2, dist=unsigned, gwn_mode=1)
+    want = np.where(s2 == 1, -unsigned, unsigned).astype(np.float32)
+    assert np.array_equal(out.view(np.uint32), want.view(np.uint32)), (
+        f"{np.count_nonzero(out.view(np.uint32) != want.view(np.uint32))} voxels differ")
+
+
+def test_learned_mode_escalates_where_plain_declines(engine, oracle):
+    """A self-overlapping shell whose lens fills more of the lattice than the stratified
+    probes tolerate: the plain fast path declines (the reference's fall-back case); learned
+    mode re-decides the signs instead -- signed crossings, the exact winding number for rays
+    through holes -- and every voxel off the surface gets the full winding number's side."""
+    from gbsdf import MODE_LEARNED, MODE_REFERENCE, PATH_FAST, compute_mesh_sdf, meshgen
+
+    v, f = meshgen.overlapping_spheres(30.0, 36.0)
+    vf, mn, mx = meshgen.fit_to_lattice(v, (96, 64, 64), 1.0)
+    tris = meshgen.to_triangles(vf, f)
+    _, rp = compute_mesh_sdf(tris, 1.0, mn, mx, mode=MODE_REFERENCE, path=PATH_FAST, raise_on_error=False)
+    assert rp.status == 4  # EVERIFY
+    out, rl = compute_mesh_sdf(tris, 1.0, mn, mx, mode=MODE_LEARNED, path=PATH_FAST)
+    assert rl.ok and rl.stats["escalated"] == 1
+    dims = mx.astype(np.int64) - mn + 1
+    vid = np.arange(0, out.size, 5, dtype=np.int64)
+    w_in = oracle.gwn_sign_voxels(tris, 1.0, mn, dims, vid, mode=1)
+    off = np.abs(out[vid]) > 1e-3
+    assert np.count_nonzero(((out[vid] < 0) != (w_in == 1)) & off) == 0
+
+
+def test_learned_batch_matches_single_calls(engine):
+    """Learned mode in a planned batch (one CUDA graph, device-side proposal budget) gives
+    each mesh's single-call grid bit for bit, with the same statuses, proposals and
+    escalations -- a declining mesh included."""
+    import torch
+
+    from gbsdf import MODE_LEARNED, PATH_FAST, Batch, compute_mesh_sdf, learn, meshgen
+
+    meshes = [(t, h, mn, mx) for t, h, mn, mx in learn.training_meshes(5, seed=777, grid=48)]
+    v, f = meshgen.overlapping_spheres(30.0, 36.0)
+    vf, mn, mx = meshgen.fit_to_lattice(v, (96, 64, 64), 1.0)
+    meshes.append((meshgen.to_triangles(vf, f), 1.0, mn, mx))
+    P = torch.from_numpy(np.load(learn.MODEL_PATH)["params"]).cuda()
+    dm = [(torch.from_numpy(t).cuda(), h, a, b) for t, h, a, b in meshes]
+    outs = [torch.empty(int(np.prod(b.astype(np.int64) - a + 1)), dtype=torch.float32, device="cuda")
+            for _, _, a, b in meshes]
+    with Batch(dm, outs=outs, mode=MODE_LEARNED, mlp_params=P) as bt:
+        sts, stats = bt.run()
+    assert all(s == 0 for s in sts), sts
+    assert any(s["escalated"] for s in stats)
+    for (t, h, a, b), o, s in zip(meshes, outs, stats):
+        ref, r = compute_mesh_sdf(t, h, a, b, mode=MODE_LEARNED, path=PATH_FAST, mlp_params=P)
+        assert r.ok
+        assert r.stats["proposed"] == s["proposed"] and r.stats["escalated"] == s["escalated"]
+        assert np.array_equal(o.cpu().numpy().view(np.uint32), ref.view(np.uint32))
