@@ -75,14 +75,15 @@ typedef enum gbsdf_mode {
      * number; voxels within 1e-3 voxel of the surface are on it (inside). Reference
      * eikonal and decline conditions. */
     GBSDF_MODE_EXACT_SIGNS = 2,
-    /* Reference mode plus learned proposals: a small network (32 brick features -> 64 ->
-     * 64 -> 1, BF16 weights, FP32 accumulation) scores every 8^3 brick's sign-error risk
-     * and the riskiest bricks are re-decided by the exact winding kernel after the
-     * stratified probes and patch boxes (which therefore see the plain path's signs); the
-     * network never supplies a sign. Where the plain path's verify diverges (it would
-     * decline), the signs are re-decided instead: signed crossings along near-lattice rays,
-     * the exact winding number for rays through holes (stats->escalated). No int-range
-     * guard. Needs opt->mlp_params (or opt->brick_scores). */
+    /* Reference mode's signs plus learned proposals: a small network (32 brick features ->
+     * 64 -> 64 -> 1, BF16 weights, FP32 accumulation) scores every 8^3 brick's sign-error
+     * risk and the riskiest bricks are re-decided by the exact winding kernel after the
+     * stratified probes; the network never supplies a sign. Where a probe finds a mismatch
+     * (the plain path would patch boxes or decline), no box is patched: the signs are
+     * re-decided instead -- signed crossings along near-lattice rays, the exact winding
+     * number for rays through holes (stats->escalated) -- and no brick is proposed (the
+     * signs are no longer the plain path's). No int-range guard. Needs opt->mlp_params (or
+     * opt->brick_scores). */
     GBSDF_MODE_LEARNED = 3
 } gbsdf_mode;
 
@@ -101,7 +102,10 @@ typedef struct gbsdf_options {
     int32_t max_rounds;    /* exact mode: safety cap on sweep rounds (0 = default 4096) */
     int32_t mlp_budget;    /* learned mode: most bricks proposed (0 = 1/16 of the bricks) */
     float mlp_threshold;   /* learned mode: risk probability above which a brick is proposed */
-    int32_t reserved0;
+    int32_t wait_poll_limit; /* the eikonal's bounded waits on staged tiles: 0 = the default limit
+                                (2^22 polls), > 0 = that many polls, < 0 = no polling (every wait
+                                gives up at once: exercises the failure path, which returns
+                                GBSDF_ECUDA with the output untouched) */
     const float* mlp_params; /* learned mode: GBSDF_MLP_PARAMS FP32 parameters in device memory */
     const float* brick_scores; /* learned mode, instead of the network: caller-supplied risk
                                   logits, one per 8^3 brick (x fastest), in device memory */

@@ -279,7 +279,7 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
         launch_winding(&j.fwn, j.t9, T, L, j.list, j.list_cap, kGwnVerify, 0, j.S, j.recheck, j.list_cap, j.A, 0,
                        stol, j.ds, b.num_sms, st);
         launch_gwn_recheck(j.t9, T, L, j.recheck, j.list_cap, kGwnVerify, j.S, j.ds, b.num_sms, st);
-        launch_verify_plan(gen, j.ds, st);
+        launch_verify_plan(gen, j.ds, st, learned ? 1 : 0);
         if (gen == kProbeGens - 1) break;
         launch_patch_mark(L, j.U, j.ds, st);
         launch_list_unknown(j.U, j.S, L, j.list, j.list_cap, j.ds, 1, st, learned ? j.E : nullptr);

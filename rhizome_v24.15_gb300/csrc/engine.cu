@@ -316,6 +316,11 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
 
     // ---- [prep] + counts
     GB_CK(cudaMemsetAsync(w.ds, 0, sizeof(DevState), st));
+    if (o.wait_poll_limit != 0) {
+        w.hs->wait_polls = o.wait_poll_limit;
+        GB_CK(cudaMemcpyAsync(&w.ds->wait_polls, &w.hs->wait_polls, sizeof(int), cudaMemcpyHostToDevice, st));
+        GB_CK(cudaStreamSynchronize(st));
+    }
     GB_CK(cudaMemsetAsync(w.bcount.p, 0, (size_t)L.nbricks * 4, st));
     GB_CK(cudaMemsetAsync(w.scount.p, 0, (size_t)L.nstrips * 4, st));
     launch_prep(P<float>(w.t12), T, L, P<SplatTri>(w.stt), P<ParTri>(w.ptt), P<unsigned>(w.bcount),
@@ -445,7 +450,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
                        P<long long>(w.recheck), kListCap, P<float>(w.A), 0, stol, w.ds, w.num_sms, st);
         launch_gwn_recheck(P<float>(w.t9), T, L, P<long long>(w.recheck), kListCap, kGwnVerify, P<uint32_t>(w.S),
                            w.ds, w.num_sms, st);
-        launch_verify_plan(gen, w.ds, st);
+        launch_verify_plan(gen, w.ds, st, learned ? 1 : 0);
         if (gen == kProbeGens - 1) break;  // the last generation never patches
         launch_patch_mark(L, P<uint32_t>(w.U), w.ds, st);
         launch_list_unknown(P<uint32_t>(w.U), P<uint32_t>(w.S), L, P<long long>(w.list), kListCap, w.ds, 1, st,

@@ -85,6 +85,7 @@ struct DevState {
     int patch_rounds;
     unsigned proposed;                 // learned mode: bricks the network proposed
     int prop_cut;                      // learned mode: lowest logit bin proposed (device-side budget)
+    int wait_polls;                    // tile-wait limit: 0 default, > 0 that many polls, < 0 none
     int escalated;                     // learned mode: the verify diverged, signs re-decided exactly
     int abort_;                        // batches: the build failed a check, write no output
     long long sites[4096];
@@ -230,7 +231,9 @@ void launch_gwn_recheck(const float* tri9, long long T, const Lattice& L, long l
                         cudaStream_t st);
 void launch_verify_prepare(const Lattice& L, int gen, const uint32_t* ubits, long long* list, DevState* ds,
                            cudaStream_t st);
-void launch_verify_plan(int gen, DevState* ds, cudaStream_t st);
+// escalate (learned mode): any mismatch of a probe ends the verify as diverged, with no
+// patch boxes, so the signs are re-decided (launch_escalate) instead.
+void launch_verify_plan(int gen, DevState* ds, cudaStream_t st, int escalate = 0);
 void launch_patch_mark(const Lattice& L, uint32_t* ubits, DevState* ds, cudaStream_t st);
 // TMA descriptor of one grid copy (x fastest) for the staged x sweep. `valid` is false
 // when the lattice does not admit one (row pitch not a multiple of 16 bytes) or the
@@ -308,7 +311,7 @@ constexpr float kPropScale = 128.0f;
 void launch_propose_hist(const float* logits, long long nb, float logit_thr, unsigned* hist, cudaStream_t st);
 // Proposals with the budget's cut taken on the device (no host round trip): the bricks above
 // the logit threshold, the highest-scoring ones first, at most `budget` of them, marked
-// unknown in U (hist: kPropBins scratch counters).
+// unknown in U (hist: kPropBins scratch counters); none after an escalation.
 void launch_propose_dev(const float* logits, const Lattice& L, float logit_thr, unsigned budget, unsigned* hist,
                         DevState* ds, uint32_t* U, cudaStream_t st);
 // Learned mode: when the verify diverged, take the signed-crossing pass's signs (S2) and

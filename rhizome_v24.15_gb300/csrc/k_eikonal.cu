@@ -356,10 +356,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
         : "memory");
     return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-    for (int i = 0; i < kWaitPolls; ++i)
+// `polls` bounds the wait (a build's DevState::wait_polls, wait_poll_limit below); the
+// drains that let a leaving CTA's copies land always use the full kWaitPolls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int polls = kWaitPolls) {
+    for (int i = 0; i < polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
+}
+// The poll limit of a build's tile waits: kWaitPolls by default (DevState::wait_polls 0), a
+// caller's limit when positive, none at all when negative (every wait gives up at once --
+// the failure path's test).
+__device__ __forceinline__ int wait_poll_limit(const DevState* ds) {
+    const int w = ds->wait_polls;
+    return w == 0 ? kWaitPolls : (w > 0 ? w : 0);
 }
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
     asm volatile(
@@ -383,6 +392,7 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_tma_kernel(const __grid_con
                                                                  float* __restrict__ dst, Lattice L, int round,
                                                                  DevState* ds) {
     if (ds->stop) return;
+    const int polls = wait_poll_limit(ds);
     extern __shared__ unsigned char tsm_raw[];
     unsigned char* tsm = align1k(tsm_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(tsm + kTS * kTSlotBytes);
@@ -417,8 +427,8 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_tma_kernel(const __grid_con
         __syncthreads();  // every thread is done with chunk ci - 1, so slot (ci + kTD) % kTS is free
         if (tid == 0) {
             if (ci + kTD < nchunks) issue(ci + kTD);
-            bool ok = mbar_wait(&bars[ci % kTS], (ci / kTS) & 1);
-            if (ok && ci + 1 < nchunks) ok = mbar_wait(&bars[(ci + 1) % kTS], ((ci + 1) / kTS) & 1);
+            bool ok = mbar_wait(&bars[ci % kTS], (ci / kTS) & 1, polls);
+            if (ok && ci + 1 < nchunks) ok = mbar_wait(&bars[(ci + 1) % kTS], ((ci + 1) / kTS) & 1, polls);
             if (!ok) {
                 // let the copies still in flight land before the CTA's shared memory goes
                 for (int k = ci; k < min(nchunks, ci + kTD + 1); ++k) mbar_wait(&bars[k % kTS], (k / kTS) & 1);
@@ -522,6 +532,7 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
                                                                   float* __restrict__ dst, Lattice L, int round,
                                                                   DevState* ds) {
     if (ds->stop) return;
+    const int polls = wait_poll_limit(ds);
     extern __shared__ unsigned char tsm_raw[];
     unsigned char* tsm = align1k(tsm_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kPS * kTSlotBytes);
@@ -546,16 +557,16 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
         int ci = 0;
         for (; ci < nchunks; ++ci) {
             const int s = ci % kPS;
-            if (ci >= kPS && !mbar_wait(&empty[s], ((ci / kPS) - 1) & 1)) break;
+            if (ci >= kPS && !mbar_wait(&empty[s], ((ci / kPS) - 1) & 1, polls)) break;
             const int c = (DIR > 0) ? ci : (nchunks - 1 - ci);
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_expect_tx(&full[s], kTBox * 4);
             tma_load_3d(tsm + s * kTSlotBytes, &tm, c * kXC, y0 - 1, z0 - 1, &full[s]);
         }
-        if (ci < nchunks) {  // consumers stopped releasing slots: drain what is in flight
-            for (int k = max(0, ci - kPS); k < ci; ++k) mbar_wait(&full[k % kPS], (k / kPS) & 1);
-            atomicAdd(&ds->wait_timeouts, 1ull);
-        }
+        // let every copy still in flight land before the producer leaves (consumers that gave
+        // up have left already); a break means the consumers stopped releasing slots
+        for (int k = max(0, ci - kPS); k < ci; ++k) mbar_wait(&full[k % kPS], (k / kPS) & 1);
+        if (ci < nchunks) atomicAdd(&ds->wait_timeouts, 1ull);
         return;
     }
     const int ty = tid & 31, tz = tid >> 5;
@@ -567,8 +578,8 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
     bool ch = false;
 #pragma unroll 1
     for (int ci = 0; ci < nchunks; ++ci) {
-        bool ok = mbar_wait(&full[ci % kPS], (ci / kPS) & 1);
-        if (ok && ci + 1 < nchunks) ok = mbar_wait(&full[(ci + 1) % kPS], ((ci + 1) / kPS) & 1);
+        bool ok = mbar_wait(&full[ci % kPS], (ci / kPS) & 1, polls);
+        if (ok && ci + 1 < nchunks) ok = mbar_wait(&full[(ci + 1) % kPS], ((ci + 1) / kPS) & 1, polls);
         if (!__all_sync(0xffffffffu, ok)) {
             if (ty == 0) atomicAdd(&ds->wait_timeouts, 1ull);
             return;
@@ -664,6 +675,7 @@ __global__ void __launch_bounds__(kP2Threads, 4) sweep_x_pipe2_kernel(const __gr
                                                                    float* __restrict__ dst, Lattice L, int round,
                                                                    DevState* ds) {
     if (ds->stop) return;
+    const int polls = wait_poll_limit(ds);
     extern __shared__ unsigned char tsm_raw[];
     unsigned char* tsm = align1k(tsm_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kPS * kTSlotBytes);
@@ -686,16 +698,16 @@ __global__ void __launch_bounds__(kP2Threads, 4) sweep_x_pipe2_kernel(const __gr
         int ci = 0;
         for (; ci < nchunks; ++ci) {
             const int s = ci % kPS;
-            if (ci >= kPS && !mbar_wait(&empty[s], ((ci / kPS) - 1) & 1)) break;
+            if (ci >= kPS && !mbar_wait(&empty[s], ((ci / kPS) - 1) & 1, polls)) break;
             const int c = (DIR > 0) ? ci : (nchunks - 1 - ci);
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_expect_tx(&full[s], kTBox * 4);
             tma_load_3d(tsm + s * kTSlotBytes, &tm, c * kXC, y0 - 1, z0 - 1, &full[s]);
         }
-        if (ci < nchunks) {  // consumers stopped releasing slots: drain what is in flight
-            for (int k = max(0, ci - kPS); k < ci; ++k) mbar_wait(&full[k % kPS], (k / kPS) & 1);
-            atomicAdd(&ds->wait_timeouts, 1ull);
-        }
+        // let every copy still in flight land before the producer leaves (consumers that gave
+        // up have left already); a break means the consumers stopped releasing slots
+        for (int k = max(0, ci - kPS); k < ci; ++k) mbar_wait(&full[k % kPS], (k / kPS) & 1);
+        if (ci < nchunks) atomicAdd(&ds->wait_timeouts, 1ull);
         return;
     }
     const int ty = tid & 31, tz = tid >> 5;
@@ -709,8 +721,8 @@ __global__ void __launch_bounds__(kP2Threads, 4) sweep_x_pipe2_kernel(const __gr
     bool ch = false;
 #pragma unroll 1
     for (int ci = 0; ci < nchunks; ++ci) {
-        bool ok = mbar_wait(&full[ci % kPS], (ci / kPS) & 1);
-        if (ok && ci + 1 < nchunks) ok = mbar_wait(&full[(ci + 1) % kPS], ((ci + 1) / kPS) & 1);
+        bool ok = mbar_wait(&full[ci % kPS], (ci / kPS) & 1, polls);
+        if (ok && ci + 1 < nchunks) ok = mbar_wait(&full[(ci + 1) % kPS], ((ci + 1) / kPS) & 1, polls);
         if (!__all_sync(0xffffffffu, ok)) {
             if (ty == 0) atomicAdd(&ds->wait_timeouts, 1ull);
             return;
@@ -839,6 +851,7 @@ __global__ void __launch_bounds__(kWPThreads) sweep_walk_pipe_kernel(const __gri
                                                                       float* __restrict__ dst, Lattice L,
                                                                       int round, DevState* ds) {
     if (ds->stop) return;
+    const int polls = wait_poll_limit(ds);
     extern __shared__ unsigned char tsm_raw[];
     unsigned char* tsm = align1k(tsm_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kWPS * kWPSlotBytes);
@@ -868,7 +881,7 @@ __global__ void __launch_bounds__(kWPThreads) sweep_walk_pipe_kernel(const __gri
         int b = 0;
         for (; b < nbatches; ++b) {
             const int s = b % kWPS;
-            if (b >= kWPS && !mbar_wait(&empty[s], ((b / kWPS) - 1) & 1)) break;
+            if (b >= kWPS && !mbar_wait(&empty[s], ((b / kWPS) - 1) & 1, polls)) break;
             // lattice slices of this batch (walk order 4b .. 4b + 3)
             const int sl0 = (DIR > 0) ? b * kWPB : n_walk - kWPB - b * kWPB;
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -876,10 +889,10 @@ __global__ void __launch_bounds__(kWPThreads) sweep_walk_pipe_kernel(const __gri
             if (AXIS == 2) tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, r0 - 1, sl0, &full[s]);
             else tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, sl0, r0 - 1, &full[s]);
         }
-        if (b < nbatches) {
-            for (int k = max(0, b - kWPS); k < b; ++k) mbar_wait(&full[k % kWPS], (k / kWPS) & 1);
-            atomicAdd(&ds->wait_timeouts, 1ull);
-        }
+        // let every copy still in flight land before the producer leaves (consumers that gave
+        // up have left already); a break means the consumers stopped releasing slots
+        for (int k = max(0, b - kWPS); k < b; ++k) mbar_wait(&full[k % kWPS], (k / kWPS) & 1);
+        if (b < nbatches) atomicAdd(&ds->wait_timeouts, 1ull);
         return;
     }
     const int tx = tid & 31, tr = tid >> 5;
@@ -902,8 +915,8 @@ __global__ void __launch_bounds__(kWPThreads) sweep_walk_pipe_kernel(const __gri
     float* pb = dst + (size_t)((DIR > 0) ? 0 : n_walk - 1) * step_stride + (size_t)rb * row_stride + x;
 #pragma unroll 1
     for (int b = 0; b < nbatches; ++b) {
-        bool ok = mbar_wait(&full[b % kWPS], (b / kWPS) & 1);
-        if (ok && b + 1 < nbatches) ok = mbar_wait(&full[(b + 1) % kWPS], ((b + 1) / kWPS) & 1);
+        bool ok = mbar_wait(&full[b % kWPS], (b / kWPS) & 1, polls);
+        if (ok && b + 1 < nbatches) ok = mbar_wait(&full[(b + 1) % kWPS], ((b + 1) / kWPS) & 1, polls);
         if (!__all_sync(0xffffffffu, ok)) {
             if (tx == 0) atomicAdd(&ds->wait_timeouts, 1ull);
             return;
@@ -976,6 +989,7 @@ __global__ void __launch_bounds__(kWVThreads) sweep_walk_vec_kernel(const __grid
                                                                      float* __restrict__ dst, Lattice L,
                                                                      int round, DevState* ds) {
     if (ds->stop) return;
+    const int polls = wait_poll_limit(ds);
     extern __shared__ unsigned char tsm_raw[];
     unsigned char* tsm = align1k(tsm_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kWVS * kWPSlotBytes);
@@ -1004,17 +1018,17 @@ __global__ void __launch_bounds__(kWVThreads) sweep_walk_vec_kernel(const __grid
         int b = 0;
         for (; b < nbatches; ++b) {
             const int s = b % kWVS;
-            if (b >= kWVS && !mbar_wait(&empty[s], ((b / kWVS) - 1) & 1)) break;
+            if (b >= kWVS && !mbar_wait(&empty[s], ((b / kWVS) - 1) & 1, polls)) break;
             const int sl0 = (DIR > 0) ? b * kWPB : n_walk - kWPB - b * kWPB;
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_expect_tx(&full[s], kWPBox * 4);
             if (AXIS == 2) tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, r0 - 1, sl0, &full[s]);
             else tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, sl0, r0 - 1, &full[s]);
         }
-        if (b < nbatches) {
-            for (int k = max(0, b - kWVS); k < b; ++k) mbar_wait(&full[k % kWVS], (k / kWVS) & 1);
-            atomicAdd(&ds->wait_timeouts, 1ull);
-        }
+        // let every copy still in flight land before the producer leaves (consumers that gave
+        // up have left already); a break means the consumers stopped releasing slots
+        for (int k = max(0, b - kWVS); k < b; ++k) mbar_wait(&full[k % kWVS], (k / kWVS) & 1);
+        if (b < nbatches) atomicAdd(&ds->wait_timeouts, 1ull);
         return;
     }
     const int cx = tid & 7, tr = tid >> 3;       // quad of x, row
@@ -1034,8 +1048,8 @@ __global__ void __launch_bounds__(kWVThreads) sweep_walk_vec_kernel(const __grid
     float* p = dst + (size_t)((DIR > 0) ? 0 : n_walk - 1) * step_stride + (size_t)r * row_stride + x;
 #pragma unroll 1
     for (int b = 0; b < nbatches; ++b) {
-        bool ok = mbar_wait(&full[b % kWVS], (b / kWVS) & 1);
-        if (ok && b + 1 < nbatches) ok = mbar_wait(&full[(b + 1) % kWVS], ((b + 1) / kWVS) & 1);
+        bool ok = mbar_wait(&full[b % kWVS], (b / kWVS) & 1, polls);
+        if (ok && b + 1 < nbatches) ok = mbar_wait(&full[(b + 1) % kWVS], ((b + 1) / kWVS) & 1, polls);
         if (!__all_sync(0xffffffffu, ok)) {
             if ((tid & 31) == 0) atomicAdd(&ds->wait_timeouts, 1ull);
             return;
@@ -1099,6 +1113,7 @@ __global__ void __launch_bounds__(kWVThreads) sweep_walk_vec2_kernel(const __gri
                                                                      float* __restrict__ dst, Lattice L,
                                                                      int round, DevState* ds) {
     if (ds->stop) return;
+    const int polls = wait_poll_limit(ds);
     extern __shared__ unsigned char tsm_raw[];
     unsigned char* tsm = align1k(tsm_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kWVS * kWPSlotBytes);
@@ -1127,17 +1142,17 @@ __global__ void __launch_bounds__(kWVThreads) sweep_walk_vec2_kernel(const __gri
         int b = 0;
         for (; b < nbatches; ++b) {
             const int s = b % kWVS;
-            if (b >= kWVS && !mbar_wait(&empty[s], ((b / kWVS) - 1) & 1)) break;
+            if (b >= kWVS && !mbar_wait(&empty[s], ((b / kWVS) - 1) & 1, polls)) break;
             const int sl0 = (DIR > 0) ? b * kWPB : n_walk - kWPB - b * kWPB;
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_expect_tx(&full[s], kWPBox * 4);
             if (AXIS == 2) tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, r0 - 1, sl0, &full[s]);
             else tma_load_3d(tsm + s * kWPSlotBytes, &tm, x0 - 4, sl0, r0 - 1, &full[s]);
         }
-        if (b < nbatches) {
-            for (int k = max(0, b - kWVS); k < b; ++k) mbar_wait(&full[k % kWVS], (k / kWVS) & 1);
-            atomicAdd(&ds->wait_timeouts, 1ull);
-        }
+        // let every copy still in flight land before the producer leaves (consumers that gave
+        // up have left already); a break means the consumers stopped releasing slots
+        for (int k = max(0, b - kWVS); k < b; ++k) mbar_wait(&full[k % kWVS], (k / kWVS) & 1);
+        if (b < nbatches) atomicAdd(&ds->wait_timeouts, 1ull);
         return;
     }
     const int cx = tid & 7, tr = tid >> 3;       // quad of x, row
@@ -1157,8 +1172,8 @@ __global__ void __launch_bounds__(kWVThreads) sweep_walk_vec2_kernel(const __gri
     float* p = dst + (size_t)((DIR > 0) ? 0 : n_walk - 1) * step_stride + (size_t)r * row_stride + x;
 #pragma unroll 1
     for (int b = 0; b < nbatches; ++b) {
-        bool ok = mbar_wait(&full[b % kWVS], (b / kWVS) & 1);
-        if (ok && b + 1 < nbatches) ok = mbar_wait(&full[(b + 1) % kWVS], ((b + 1) / kWVS) & 1);
+        bool ok = mbar_wait(&full[b % kWVS], (b / kWVS) & 1, polls);
+        if (ok && b + 1 < nbatches) ok = mbar_wait(&full[(b + 1) % kWVS], ((b + 1) / kWVS) & 1, polls);
         if (!__all_sync(0xffffffffu, ok)) {
             if ((tid & 31) == 0) atomicAdd(&ds->wait_timeouts, 1ull);
             return;

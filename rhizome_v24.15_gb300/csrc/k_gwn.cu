@@ -918,12 +918,17 @@ __global__ void verify_prepare_kernel(Lattice L, int gen, const uint32_t* __rest
     }
 }
 
-__global__ void verify_plan_kernel(int gen, DevState* ds) {
+__global__ void verify_plan_kernel(int gen, DevState* ds, int escalate) {
     if (ds->verify_state != 0) return;
     int m = ds->probe_m;
     ds->probes += 1;
     if (m == 0) {
         ds->verify_state = 1;
+        return;
+    }
+    if (escalate) {  // learned mode: any mismatch re-decides the signs, no patch boxes
+        ds->total_sites += m;
+        ds->verify_state = 2;
         return;
     }
     if (m > kVerifySamples) m = kVerifySamples;
@@ -1160,9 +1165,9 @@ void launch_verify_prepare(const Lattice& L, int gen, const uint32_t* ubits, lon
     verify_prepare_kernel<<<1, 1024, 0, st>>>(L, gen, ubits, list, ds);
 }
 
-void launch_verify_plan(int gen, DevState* ds, cudaStream_t st) {
+void launch_verify_plan(int gen, DevState* ds, cudaStream_t st, int escalate) {
     GBSDF_COUNT_LAUNCH();
-    verify_plan_kernel<<<1, 1, 0, st>>>(gen, ds);
+    verify_plan_kernel<<<1, 1, 0, st>>>(gen, ds, escalate);
 }
 
 void launch_patch_mark(const Lattice& L, uint32_t* ubits, DevState* ds, cudaStream_t st) {

@@ -381,9 +381,10 @@ __global__ void propose_cut_kernel(const unsigned* __restrict__ hist, unsigned b
 
 __global__ void propose_dev_kernel(const float* __restrict__ logits, Lattice L, float logit_thr,
                                    const int* __restrict__ cut, unsigned* __restrict__ n_prop,
-                                   uint32_t* __restrict__ U) {
+                                   uint32_t* __restrict__ U, const DevState* __restrict__ ds) {
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= L.nbricks) return;
+    // after an escalation the signs are no longer the plain path's: nothing to aim at
+    if (b >= L.nbricks || ds->escalated) return;
     const float z = logits[b];
     const int cut_bin = *cut;
     if (cut_bin >= kPropBins || !(z > logit_thr) || prop_bin(z, logit_thr) < cut_bin) return;
@@ -430,7 +431,7 @@ void launch_propose_dev(const float* logits, const Lattice& L, float logit_thr, 
     propose_cut_kernel<<<1, 1, 0, st>>>(hist, budget, &ds->prop_cut);
     GBSDF_COUNT_LAUNCH();
     propose_dev_kernel<<<(unsigned)((L.nbricks + 255) / 256), 256, 0, st>>>(logits, L, logit_thr, &ds->prop_cut,
-                                                                             &ds->proposed, U);
+                                                                             &ds->proposed, U, ds);
 }
 
 void launch_escalate(DevState* ds, uint32_t* S, uint32_t* U, const uint32_t* S2, const uint32_t* U2,

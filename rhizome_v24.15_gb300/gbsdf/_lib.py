@@ -22,7 +22,7 @@ PATH_AUTO, PATH_FAST, PATH_LEGACY = 0, 1, 2
 class Options(C.Structure):
     _fields_ = [("mode", C.c_int32), ("path", C.c_int32), ("device", C.c_int32), ("tris_on_device", C.c_int32),
                 ("max_rounds", C.c_int32), ("mlp_budget", C.c_int32), ("mlp_threshold", C.c_float),
-                ("reserved0", C.c_int32), ("mlp_params", C.c_void_p), ("brick_scores", C.c_void_p),
+                ("wait_poll_limit", C.c_int32), ("mlp_params", C.c_void_p), ("brick_scores", C.c_void_p),
                 ("sweep_schedule", C.c_int32), ("host_output", C.c_int32),
                 ("winding_eval", C.c_int32), ("reserved", C.c_int32)]
 

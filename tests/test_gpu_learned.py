@@ -108,6 +108,18 @@ def _mesh(seed, grid=64):
     return learn.training_meshes(1, seed=seed, grid=grid)[0]
 
 
+def _quiet_mesh(seed, grid=64):
+    """A defective training mesh whose stratified probes find no mismatch, so learned mode
+    proposes bricks rather than escalating."""
+    from gbsdf import MODE_REFERENCE, PATH_FAST, compute_mesh_sdf, learn
+
+    for tris, h, mn, mx in learn.training_meshes(12, seed=seed, grid=grid):
+        _, r = compute_mesh_sdf(tris, h, mn, mx, mode=MODE_REFERENCE, path=PATH_FAST, raise_on_error=False)
+        if r.ok and r.stats["sites"] == 0:
+            return tris, h, mn, mx
+    pytest.fail("no training mesh without probe mismatches")
+
+
 def test_brick_features(engine):
     import torch
 
@@ -130,7 +142,7 @@ def test_learned_mode_is_deterministic_and_within_budget(engine):
     from gbsdf import MODE_LEARNED, PATH_FAST, compute_mesh_sdf
     from gbsdf.learn import brick_grid, init_params
 
-    tris, h, mn, mx = _mesh(78)
+    tris, h, mn, mx = _quiet_mesh(78)
     P = init_params(13)
     P[M.ob3] = 5.0  # untrained network, biased to propose many bricks
     nb = brick_grid(mn, mx)
@@ -166,9 +178,10 @@ def _mismatch(out, exact, h):
 
 
 def test_ablation_learned_vs_plain_vs_random(engine):
-    """Held-out meshes (seeds disjoint from the training set), at most 3% of the bricks
-    re-decided by the exact winding number: the shipped network's picks remove most of
-    the plain fast path's sign errors, far more than the same number of random band
+    """Held-out meshes (seeds disjoint from the training set) whose stratified probes
+    found no mismatch (so learned mode proposes instead of escalating), at most 3% of the
+    bricks re-decided by the exact winding number: the shipped network's picks remove most
+    of the plain fast path's sign errors, far more than the same number of random band
     bricks. The single best hand feature (the count of voxels where the sign and the
     signed crossings disagree) is printed beside them."""
     from gbsdf import MODE_LEARNED, MODE_REFERENCE, PATH_FAST, PATH_LEGACY, compute_mesh_sdf, learn
@@ -187,6 +200,8 @@ def test_ablation_learned_vs_plain_vs_random(engine):
         budget = max(1, nb * 3 // 100)
         lo, rl = compute_mesh_sdf(tris, h, mn, mx, mode=MODE_LEARNED, path=PATH_FAST, mlp_params=trained,
                                   mlp_budget=budget, mlp_threshold=0.01)
+        if rl.stats["escalated"]:
+            continue  # a probe found a mismatch: the signs were re-decided, nothing was proposed
         k = max(1, int(rl.stats["proposed"]))
         rand = np.where(X[:, 4] > 0, rng.uniform(0.0, 10.0, nb), -100.0).astype(np.float32)
         ra, rr = compute_mesh_sdf(tris, h, mn, mx, mode=MODE_LEARNED, path=PATH_FAST, brick_scores=rand,
@@ -215,7 +230,7 @@ def test_learned_mode_matches_oracle_with_given_proposals(engine, oracle):
     the signs applied to the same unsigned field. Bit for bit."""
     from gbsdf import MODE_LEARNED, PATH_FAST, compute_mesh_sdf, learn
 
-    tris, h, mn, mx = _mesh(81, grid=56)
+    tris, h, mn, mx = _quiet_mesh(81, grid=56)
     dims = mx.astype(np.int64) - mn + 1
     nb = learn.brick_grid(mn, mx)
     n_b = int(np.prod(nb))

@@ -39,7 +39,14 @@ def test_clustered_equals_per_triangle(engine, case):
 def test_clustered_learned_proposals(engine):
     from gbsdf import MODE_LEARNED, PATH_FAST, learn
 
-    name, tris, h, mn, mx = _cases()[0]
+    # a defective mesh whose stratified probes find no mismatch: learned mode proposes
+    for tris, h, mn, mx in learn.training_meshes(12, seed=31, grid=80):
+        _, r = engine.compute_mesh_sdf(tris, h, mn, mx, mode=engine.MODE_REFERENCE, path=PATH_FAST,
+                                       raise_on_error=False)
+        if r.ok and r.stats["sites"] == 0:
+            break
+    else:
+        pytest.fail("no training mesh without probe mismatches")
     trained = np.load(learn.MODEL_PATH)["params"]
     a, ra = engine.compute_mesh_sdf(tris, h, mn, mx, mode=MODE_LEARNED, path=PATH_FAST, mlp_params=trained,
                                     mlp_budget=200, winding_eval=0)
