@@ -113,7 +113,7 @@ def _quiet_mesh(seed, grid=64):
     proposes bricks rather than escalating."""
     from gbsdf import MODE_REFERENCE, PATH_FAST, compute_mesh_sdf, learn
 
-    for tris, h, mn, mx in learn.training_meshes(12, seed=seed, grid=grid):
+    for tris, h, mn, mx in learn.training_meshes(32, seed=seed, grid=grid):
         _, r = compute_mesh_sdf(tris, h, mn, mx, mode=MODE_REFERENCE, path=PATH_FAST, raise_on_error=False)
         if r.ok and r.stats["sites"] == 0:
             return tris, h, mn, mx
@@ -230,7 +230,7 @@ def test_learned_mode_matches_oracle_with_given_proposals(engine, oracle):
     the signs applied to the same unsigned field. Bit for bit."""
     from gbsdf import MODE_LEARNED, PATH_FAST, compute_mesh_sdf, learn
 
-    tris, h, mn, mx = _quiet_mesh(81, grid=56)
+    tris, h, mn, mx = _quiet_mesh(81, grid=64)
     dims = mx.astype(np.int64) - mn + 1
     nb = learn.brick_grid(mn, mx)
     n_b = int(np.prod(nb))
