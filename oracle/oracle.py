@@ -44,7 +44,8 @@ def build_ref() -> Path | None:
 
 class FastParams(C.Structure):
     _fields_ = [("fsm_mode", C.c_int), ("gwn_mode", C.c_int), ("threads", C.c_int),
-                ("max_conv_rounds", C.c_int), ("skip_verify", C.c_int), ("signed_parity", C.c_int)]
+                ("max_conv_rounds", C.c_int), ("skip_verify", C.c_int), ("signed_parity", C.c_int),
+                ("skip_eikonal", C.c_int), ("lazy_winding", C.c_int)]
 
 
 class FastStats(C.Structure):
@@ -204,9 +205,15 @@ def eikonal(g, sign, dims, h, fsm_mode=1, max_conv_rounds=100000, threads=None):
 
 
 def fast_sdf(tris, h, mn, mx, fsm_mode=1, gwn_mode=1, threads=None, skip_verify=False, max_conv_rounds=100000,
-             signed_parity=False):
+             signed_parity=False, skip_eikonal=False, lazy_winding=False):
     """The whole fast path (RAST:796-1159). Returns (status, dist or None, sign, stats dict).
-    ``signed_parity``: signed crossings in stage [B] (the engine's exact-signs modes)."""
+    ``signed_parity``: signed crossings in stage [B] (the engine's exact-signs modes).
+    ``skip_eikonal``: signs, statuses and statistics only -- no stage [D], which changes no
+    voxel the surface tolerance reads; ``dist`` is then the signed band field.
+    ``lazy_winding``: the voxels of columns through holes ([C]) and of patch boxes are
+    marked (sign 3: the winding number decides) instead of summed; statuses and statistics
+    (bar fp64_rechecks) are unchanged, since a probe never reads an undecided voxel and
+    makes the fixup's own decision where it would."""
     t, T = _tris(tris)
     mn, mx = _ivec(mn), _ivec(mx)
     dims = mx.astype(np.int64) - mn + 1
@@ -214,7 +221,7 @@ def fast_sdf(tris, h, mn, mx, fsm_mode=1, gwn_mode=1, threads=None, skip_verify=
     dist = np.empty(max(N, 1), np.float32)
     sign = np.empty(max(N, 1), np.uint8)
     prm = FastParams(fsm_mode, gwn_mode, threads or default_threads(), max_conv_rounds, 1 if skip_verify else 0,
-                     1 if signed_parity else 0)
+                     1 if signed_parity else 0, 1 if skip_eikonal else 0, 1 if lazy_winding else 0)
     st = FastStats()
     s = lib().orc_fast_sdf(_p(t), C.c_int(T), C.c_float(h), _p(mn), _p(mx), C.byref(prm), _p(dist), _p(sign),
                            C.byref(st))

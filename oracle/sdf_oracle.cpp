@@ -298,6 +298,10 @@ struct orc_fast_params {
     int max_conv_rounds; // cap for fsm_mode 1 (safety only)
     int skip_verify;     // 1: skip stage [E] (used to time/compare stages separately)
     int signed_parity;   // 1: exact signs -- signed crossings, near-lattice rays, surface tolerance 1e-3 voxel
+    int skip_eikonal;    // 1: signs and statuses only -- no stage [D]; out_dist holds the signed band field
+    int lazy_winding;    // 1: voxels that [C] and the patch boxes would decide by the winding number are
+                         //    marked (sign 3), not summed; the probes skip them, since a probe there makes
+                         //    the same winding decision as the fixup
 };
 // Exact-signs mode: voxels within this many voxels of the surface are on it (inside).
 constexpr float kSurfaceTolExact = 1e-3f;
@@ -777,9 +781,23 @@ int orc_eikonal_exact_f64(const float* band, const int* dims, double h, double* 
 float orc_godunov_exact(float ax, float ay, float az, float h) { return godunov_exact_f(ax, ay, az, h); }
 
 // ---- [E] stratified verify + patch (RAST:566-646, RAST:1078-1132) --------------------
-// Returns 1 when a probe came back clean, 0 on systematic divergence.
-int orc_verify_patch(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
-                     const float* dist, int gwn_mode, int threads, orc_fast_stats* st, float tol) {
+// Undecided voxels (2) become 3, "the winding number decides", without the sum; returns
+// their count, the count the fixup would return.
+static long long mark_lazy(uint8_t* sign, size_t N) {
+    long long n = 0;
+    for (size_t i = 0; i < N; ++i)
+        if (sign[i] == 2) {
+            sign[i] = 3;
+            ++n;
+        }
+    return n;
+}
+
+// Returns 1 when a probe came back clean, 0 on systematic divergence. ``lazy``: patch boxes
+// are marked 3 (decided by the winding number, not summed here) and counted as patched;
+// probes skip them, since the fixup and the probe make the same winding decision there.
+static int verify_patch_impl(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
+                             const float* dist, int gwn_mode, int threads, orc_fast_stats* st, float tol, int lazy) {
     const OTri* tris = static_cast<const OTri*>(tris_);
     const long long dx = dims[0], dy = dims[1], dz = dims[2];
     const size_t N = (size_t)(dx * dy * dz);
@@ -797,7 +815,7 @@ int orc_verify_patch(const void* tris_, int T, float h, const int* mn, const int
             for (long long i = b; i < e; ++i) {
                 long long v = vidx[(size_t)i];
                 uint8_t s = sign[v];
-                if (s == 2) continue;
+                if (s == 2 || s == 3) continue;
                 int x = (int)(v % dx), y = (int)((v / dx) % dy), z = (int)(v / (dx * dy));
                 V3 p{(float)(mn[0] + x) * h, (float)(mn[1] + y) * h, (float)(mn[2] + z) * h};
                 bool inside = gwn_inside(tris, T, p, gwn_mode, &ctr, dist ? dist[v] : 1e30f, h, tol);
@@ -824,13 +842,19 @@ int orc_verify_patch(const void* tris_, int T, float h, const int* mn, const int
                 for (int y = y0; y <= y1; ++y)
                     for (int x = x0; x <= x1; ++x) sign[(size_t)z * dx * dy + (size_t)y * dx + x] = 2;
         }
-        long long fixed =
-            orc_fixup_unknown_tol(tris_, T, h, mn, dims, sign, dist, gwn_mode, threads, &st->fp64_rechecks, tol);
+        long long fixed = lazy ? mark_lazy(sign, N)
+                               : orc_fixup_unknown_tol(tris_, T, h, mn, dims, sign, dist, gwn_mode, threads,
+                                                       &st->fp64_rechecks, tol);
         st->patched_voxels += fixed;
         st->sites += m;
         st->patch_rounds += 1;
     }
     return 0;
+}
+
+int orc_verify_patch(const void* tris_, int T, float h, const int* mn, const int* dims, uint8_t* sign,
+                     const float* dist, int gwn_mode, int threads, orc_fast_stats* st, float tol) {
+    return verify_patch_impl(tris_, T, h, mn, dims, sign, dist, gwn_mode, threads, st, tol, 0);
 }
 
 // ---- [F] sign apply (RAST:650-661) --------------------------------------------------
@@ -843,7 +867,8 @@ void orc_apply_signs(float* g, const uint8_t* sign, long long N) {
 }
 
 // ---- the whole fast path (RAST:796-1159) ---------------------------------------------
-// out_dist: N floats (left untouched on failure); out_sign: N bytes scratch (0/1 final).
+// out_dist: N floats (left untouched on failure); out_sign: N bytes scratch (0/1 final; 3 marks
+// a voxel left to the winding number under lazy_winding, written with a positive distance).
 int orc_fast_sdf(const void* tris_, int T, float h, const int* mn, const int* mx, const orc_fast_params* prm,
                  float* out_dist, uint8_t* out_sign, orc_fast_stats* st) {
     using clk = std::chrono::steady_clock;
@@ -855,8 +880,10 @@ int orc_fast_sdf(const void* tris_, int T, float h, const int* mn, const int* mx
     int dims[3] = {mx[0] - mn[0] + 1, mx[1] - mn[1] + 1, mx[2] - mn[2] + 1};
     if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0 || T <= 0) return st->status = 1;
     long long N = (long long)dims[0] * dims[1] * dims[2];
-    if (N > 2000000000LL || (long long)T * dims[2] > 2000000000LL || (long long)dims[0] * dims[1] > 2000000000LL ||
-        (long long)dims[0] * dims[2] > 2000000000LL || (long long)dims[1] * dims[2] > 2000000000LL)
+    // the reference's 32-bit index guard (RAST:816-820); the exact-signs modes index in 64 bits
+    if (!prm->signed_parity &&
+        (N > 2000000000LL || (long long)T * dims[2] > 2000000000LL || (long long)dims[0] * dims[1] > 2000000000LL ||
+         (long long)dims[0] * dims[2] > 2000000000LL || (long long)dims[1] * dims[2] > 2000000000LL))
         return st->status = 2;
     int threads = std::max(1, prm->threads);
     std::vector<float> g((size_t)N);
@@ -870,17 +897,20 @@ int orc_fast_sdf(const void* tris_, int T, float h, const int* mn, const int* mx
     if (unk < 0) return st->status = 3;
     st->unknown_columns = (int)unk;
     if (unk > 0)
-        st->fixup_voxels =
-            orc_fixup_unknown_tol(tris_, T, h, mn, dims, out_sign, g.data(), prm->gwn_mode, threads,
-                                  &st->fp64_rechecks, tol);
+        st->fixup_voxels = prm->lazy_winding ? mark_lazy(out_sign, (size_t)N)
+                                             : orc_fixup_unknown_tol(tris_, T, h, mn, dims, out_sign, g.data(),
+                                                                     prm->gwn_mode, threads, &st->fp64_rechecks, tol);
     auto td = clk::now();
-    st->eikonal_rounds = orc_eikonal(g.data(), out_sign, dims, h, prm->fsm_mode,
-                                     prm->max_conv_rounds > 0 ? prm->max_conv_rounds : 100000, threads,
-                                     &st->extra_rounds, &st->far_residual, &st->safe_clamped);
+    // [D] changes no voxel at or below the surface tolerance (a Godunov update of non-negative
+    // neighbours is at least h/sqrt(3)), so [E] decides the same without it.
+    if (!prm->skip_eikonal)
+        st->eikonal_rounds = orc_eikonal(g.data(), out_sign, dims, h, prm->fsm_mode,
+                                         prm->max_conv_rounds > 0 ? prm->max_conv_rounds : 100000, threads,
+                                         &st->extra_rounds, &st->far_residual, &st->safe_clamped);
     auto te = clk::now();
     int ok = prm->skip_verify ? 1
-                              : orc_verify_patch(tris_, T, h, mn, dims, out_sign, g.data(), prm->gwn_mode, threads, st,
-                                                 tol);
+                              : verify_patch_impl(tris_, T, h, mn, dims, out_sign, g.data(), prm->gwn_mode, threads, st,
+                                                  tol, prm->lazy_winding);
     auto tf = clk::now();
     st->ms_splat = ms(ta, tb);
     st->ms_parity = ms(tb, tc);
