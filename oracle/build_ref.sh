@@ -4,8 +4,7 @@
 # Builds the checkers made from the reference's own code. Every output goes to
 # oracle/_ref/, which is never committed.
 #
-# 1. Where the reference tree is present (RHIZOME_REFERENCE, default below; a recipe
-#    that reads the reference where it lies names that location):
+# 1. Where the reference tree is named by RHIZOME_REFERENCE and present:
 #    * oracle/_ref/libref_math.so — the reference's host/device geometry primitives
 #      (native/src/core/math_utils.cuh) compiled on the host with g++, through the
 #      project-written glm stand-in in oracle/ref_shim/;
@@ -22,14 +21,14 @@
 # Exits 0 when a step's inputs are absent.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF_ROOT="${RHIZOME_REFERENCE:-/root/reference}"
+REF_ROOT="${RHIZOME_REFERENCE:-}"
 REF_SRC="$REF_ROOT/native/src"
 OUT="$HERE/_ref"
 STAGE="$OUT/src"
 CLOSURE="engine/sdf/cuda_rasterizer.cu engine/sdf/cuda_rasterizer.hpp engine/sdf/cuda_types.hpp
 engine/sdf/cuda_common.cuh engine/io/mesh.hpp core/math_utils.cuh core/unified_logger.hpp"
 
-if [ -f "$REF_SRC/core/math_utils.cuh" ]; then
+if [ -n "$REF_ROOT" ] && [ -f "$REF_SRC/core/math_utils.cuh" ]; then
   mkdir -p "$OUT"
   g++ -O2 -std=c++20 -ffp-contract=off -fPIC -shared \
     -I "$HERE/ref_shim" -I "$REF_SRC" \
@@ -45,7 +44,7 @@ if [ -f "$REF_SRC/core/math_utils.cuh" ]; then
   fi
   echo "staged the reference's fast-SDF sources in $STAGE"
 else
-  echo "reference tree not present; libref_math.so not built, sources not staged"
+  echo "RHIZOME_REFERENCE unset or not a reference tree; libref_math.so not built, sources not staged"
 fi
 
 NVCC="${NVCC:-$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)}"

@@ -35,10 +35,14 @@ def build(force: bool = False) -> Path:
     return LIB_PATH
 
 
-def build_ref() -> Path | None:
-    """Compile the reference's own primitives into oracle/_ref (only where the
-    reference tree exists)."""
-    subprocess.check_call(["bash", str(HERE / "build_ref.sh")])
+def build_ref(reference_root=None) -> Path | None:
+    """Compile the reference's own primitives into oracle/_ref: from the reference tree at
+    ``reference_root`` (or the RHIZOME_REFERENCE environment variable) where given, and the
+    reference GPU checker from the staged sources wherever they are."""
+    env = dict(os.environ)
+    if reference_root is not None:
+        env["RHIZOME_REFERENCE"] = str(reference_root)
+    subprocess.check_call(["bash", str(HERE / "build_ref.sh")], env=env)
     return REF_LIB_PATH if REF_LIB_PATH.exists() else None
 
 

@@ -2,7 +2,6 @@
 against an independent numpy restatement, the OBJ decode against the source mesh, and --
 where the reference tree is present -- the reference's own mug specimen against the facts
 its documentation states (1,553 vertices, 3,106 triangles, 100.0 x 76.5 x 85.0 mm)."""
-import os
 from pathlib import Path
 
 import numpy as np
@@ -76,11 +75,11 @@ def test_obj_decode_matches_source_mesh():
     assert st == 0 and oi.tolist() == [0, 1, 2, 0, 2, 3, 0, 8, 1]
 
 
-# the reference tree, where present (the same variable and default as oracle/build_ref.sh)
-REF_MUG = Path(os.environ.get("RHIZOME_REFERENCE", "/root/reference")) / "native/assets/mug.obj"
+# the reference's own specimen, staged by oracle/build_ref.sh from the reference tree
+REF_MUG = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "assets" / "mug.obj"
 
 
-@pytest.mark.skipif(not REF_MUG.exists(), reason="the reference tree is not present")
+@pytest.mark.skipif(not REF_MUG.exists(), reason="the reference's specimen is not staged")
 def test_reference_mug_specimen():
     st, v, i = O.parse_obj(REF_MUG.read_bytes())
     assert st == 0 and len(v) == 1553 and len(i) == 3 * 3106
