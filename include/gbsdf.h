@@ -113,11 +113,11 @@ typedef struct gbsdf_options {
                                staged by cp.async, 2 by TMA tiles on a CTA-barrier ring, 3 by TMA
                                tiles on a warp-specialised mbarrier pipeline, 4 the same with two
                                lines per thread updated in packed FP32 pairs (the reference's
-                               update; other modes run 3); w = 1 y / z walks
+                               update at voxel sizes 2^-20 to 2^20; otherwise 3 runs); w = 1 y / z walks
                                staged by cp.async, 2 by TMA batches on a pipeline, 3 the same
                                with four adjacent lines per thread, 4 the same with the lines'
-                               updates in packed FP32 pairs (the reference's update; other
-                               modes run 3); a 0 digit (and
+                               updates in packed FP32 pairs (the reference's update at voxel
+                               sizes 2^-20 to 2^20; otherwise 3 runs); a 0 digit (and
                                0 overall) = autotuned (the first build of a lattice class times
                                the candidates). TMA needs rows of a multiple of 4 voxels. */
     int32_t host_output;    /* host outputs: 0 = a page-locked output is written by the sign-apply
@@ -388,7 +388,8 @@ int gbsdf_legacy_sdf_noalloc(const gbsdf_tri* tris_dev, int64_t n_tris, float vo
 /* Engine self-tests (no counterpart in the reference). which = 0: the correctly rounded
  * divisions by 3 used by the eikonal update are compared with the IEEE quotient -- the
  * general one for every non-NaN float input, the one for non-negative arguments for every
- * finite non-negative float; which = 1: the x sweep's TMA tile layout (32-byte swizzle,
+ * finite non-negative float -- and the packed square root of the paired updates with
+ * sqrtf on zero and every float in [2^-100, 2^100]; which = 1: the x sweep's TMA tile layout (32-byte swizzle,
  * out-of-lattice fill) is checked element by element on five boxes of a test grid.
  * *result = number of mismatches (0 expected). */
 int gbsdf_selftest(int32_t which, int32_t device, uint64_t* result, char* err, size_t errlen);

@@ -308,7 +308,7 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
     }
     // [F], written only when the build passed its checks
     launch_batch_finalize(j.ds, learned ? 0 : 1, st);
-    launch_apply(j.A, j.S, L, b.out_dev ? j.out : j.B, j.ds, xs ? stol * L.h : 0.0f, st);
+    launch_apply(j.A, j.S, L, b.out_dev ? j.out : j.B, j.ds, xs ? stol * L.h : -1.0f, st);
     if (!b.out_dev) cudaMemcpyAsync(j.hout, j.B, (size_t)N * 4, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(j.hs, j.ds, sizeof(DevState), cudaMemcpyDeviceToHost, st);
 }

@@ -515,7 +515,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
             cudaGetLastError();
         }
     }
-    launch_apply(P<float>(w.A), P<uint32_t>(w.S), L, final_dst, w.ds, exact_signs ? stol * L.h : 0.0f, st);
+    launch_apply(P<float>(w.A), P<uint32_t>(w.S), L, final_dst, w.ds, exact_signs ? stol * L.h : -1.0f, st);
     GB_CK(cudaGetLastError());
     GB_CK(cudaEventRecord(w.ev[8], st));
     GB_CK(cudaMemcpyAsync(w.hs, w.ds, sizeof(DevState), cudaMemcpyDeviceToHost, st));

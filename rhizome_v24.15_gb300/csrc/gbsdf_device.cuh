@@ -192,9 +192,12 @@ __device__ __forceinline__ double ptd_sq_f64(double px, double py, double pz, co
     return d2(px - (ax + abx * sv + acx * sw), py - (ay + aby * sv + acy * sw), pz - (az + abz * sv + acz * sw));
 }
 
-// Three-input minimum and maximum (PTX ISA 8.8, sm_100 and later): for operands that are
-// not NaN these equal fminf(a, fminf(b, c)) and fmaxf(a, fmaxf(b, c)) exactly (a minimum
-// or maximum rounds nothing); the Godunov updates never see a NaN operand.
+// Three-input minimum and maximum (PTX ISA 8.8, sm_100 and later): these equal
+// fminf(a, fminf(b, c)) and fmaxf(a, fmaxf(b, c)) exactly (a minimum or maximum rounds
+// nothing; without the .NaN modifier a NaN operand is passed over, as by fminf). The x
+// pipeline clamps a pair of tile neighbours, either of which may be the tiles' NaN
+// out-of-lattice fill, with min3f(a, b, far sentinel); the Godunov updates never see a
+// NaN operand.
 __device__ __forceinline__ float min3f(float a, float b, float c) {
     float r;
     asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
@@ -292,22 +295,61 @@ __device__ __forceinline__ float godunov_ref_sel(float ax, float ay, float az, f
     return take3 ? u3 : (take2 ? u2 : u1);
 }
 
+// Reciprocal square root approximation (the MUFU unit; relative error below 2^-22.9 per
+// the PTX ISA's rsqrt.approx.f32).
+__device__ __forceinline__ float rsqrt_approx(float a) {
+    float r;
+    asm("rsqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+
+// -sqrt(a) in both lanes of NA = -a, correctly rounded (bit-identical to -sqrtf(a)) for
+// every a in [2^-100, 2^100], and a zero of either sign for a = 0 (NA = +0 or -0). Markstein's FMA square root (P. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990): y ~ 1/sqrt(a), g = a*y, h = y/2; one Newton step on h,
+// r = 1/2 - g*h, h1 = h + h*r; the residual e = g*g - a, exact in one FMA; sqrt(a) =
+// g - e*h1. It runs on the negated values: rounding to nearest is symmetric, so each step
+// is the exact negation of the positive form. y is capped at 2^100 so that a = 0 gives 0.
+// A lane with a < 0 gives a meaningless value. Below 2^-100 the residual e can underflow
+// (roots of operands under 2^-102 misround); pair_sqrt_ok keeps the updates' operands out
+// of that range. The self-test (gbsdf_selftest(0)) checks zero and every float in
+// [2^-100, 2^100] against sqrtf.
+__device__ __forceinline__ f32x2 nsqrt2_rn(f32x2 NA, f32x2 half) {
+    float na0, na1;
+    up2(NA, na0, na1);
+    const f32x2 Y = pk2(fminf(rsqrt_approx(fabsf(na0)), 0x1p100f), fminf(rsqrt_approx(fabsf(na1)), 0x1p100f));
+    const f32x2 NG = mul2(NA, Y);
+    const f32x2 H = mul2(Y, half);
+    const f32x2 H1 = fma2(H, fma2(NG, H, half), H);
+    return fma2(fma2(NG, NG, NA), H1, NG);
+}
+
+// Voxel sizes for which every square-root operand of the paired updates lies in
+// nsqrt2_rn's checked range, {0} and [2^-100, 2^100]: a non-zero discriminant
+// 2h*h - d*d is at least 2^(2e-45) with e = floor(log2 h) (the granularity of the exact
+// product), i.e. at least 2^-85 for h >= 2^-20, and no operand exceeds 3h^2 < 2^42 for
+// h <= 2^20; a non-zero 3D discriminant 3h^2 - S/2 is either near 3h^2 or, where S/2 is
+// near 3h^2, a multiple of ulp(3h^2)/2 >= 2^-64. Other voxel sizes take the scalar kernels.
+__host__ __device__ __forceinline__ bool pair_sqrt_ok(float h) { return h >= 0x1p-20f && h <= 0x1p20f; }
+
 // Constants of godunov_ref_pair for one voxel size, each in both lanes.
 struct GodunovPairConsts {
-    f32x2 h, m2h, a3, half, r3, m3;
+    f32x2 h, m2h, na3, half, r3, m3;
 };
 __device__ __forceinline__ GodunovPairConsts godunov_pair_consts(float h) {
     const float a3 = 3.0f * h * h;
-    return GodunovPairConsts{pk2(h, h),       pk2(-2.0f * h, -2.0f * h), pk2(a3, a3),
+    return GodunovPairConsts{pk2(h, h),       pk2(-2.0f * h, -2.0f * h), pk2(-a3, -a3),
                              pk2(0.5f, 0.5f), pk2(0.333333343267440796f, 0.333333343267440796f),
                              pk2(-3.0f, -3.0f)};
 }
 
 // godunov_ref_sel for two independent voxels at once: the arithmetic on packed pairs,
-// the ordering, square roots and selections per lane. Every value rounds exactly as in
-// godunov_ref_sel: disc = fma(2h, h, -dd) is formed negated as fma(-2h, h, dd) (rounding
-// to nearest is symmetric) and only its sign and negation are used; 3h^2 - S/2 keeps the
-// two roundings; the division by 3 is div3_pos.
+// the ordering and selections per lane. Every value rounds exactly as in godunov_ref_sel,
+// formed negated where that saves an operation (rounding to nearest is symmetric):
+// -disc = fma(-2h, h, dd); -disc3 = fma(S, 1/2, -3h^2), one rounding of the exact
+// S/2 - 3h^2 where the reference rounds S*0.5 (exact) and then 3h^2 - S*0.5; the square
+// roots are nsqrt2_rn (correctly rounded, as sqrtf); the division by 3 is div3_pos. A
+// candidate whose discriminant is negative holds a meaningless value and is not selected.
 __device__ __forceinline__ void godunov_ref_pair(float ax0, float ay0, float az0, float ax1, float ay1, float az1,
                                                  const GodunovPairConsts& c, float& out0, float& out1) {
     const float s00 = min3f(ax0, ay0, az0), s20 = max3f(ax0, ay0, az0);
@@ -318,15 +360,16 @@ __device__ __forceinline__ void godunov_ref_pair(float ax0, float ay0, float az0
     const f32x2 D = sub2(S1, S0);
     const f32x2 DD = mul2(D, D);
     const f32x2 ND = fma2(c.m2h, c.h, DD);  // -disc
-    const f32x2 SS = fma2(sub2(S2, S0), sub2(S2, S0), fma2(sub2(S2, S1), sub2(S2, S1), DD));
-    const f32x2 D3 = sub2(c.a3, mul2(SS, c.half));
-    float nd0, nd1, d30, d31;
+    const f32x2 E2 = sub2(S2, S0), E1 = sub2(S2, S1);
+    const f32x2 SS = fma2(E2, E2, fma2(E1, E1, DD));
+    const f32x2 ND3 = fma2(SS, c.half, c.na3);  // -disc3
+    float nd0, nd1, nd30, nd31;
     up2(ND, nd0, nd1);
-    up2(D3, d30, d31);
-    const bool ok20 = nd0 <= 0.0f, ok21 = nd1 <= 0.0f, ok30 = d30 >= 0.0f, ok31 = d31 >= 0.0f;
+    up2(ND3, nd30, nd31);
+    const bool ok20 = nd0 <= 0.0f, ok21 = nd1 <= 0.0f, ok30 = nd30 <= 0.0f, ok31 = nd31 <= 0.0f;
     const f32x2 T01 = add2(S0, S1);
-    const f32x2 U2 = mul2(add2(T01, pk2(sqrtf(ok20 ? -nd0 : 1.0f), sqrtf(ok21 ? -nd1 : 1.0f))), c.half);
-    const f32x2 X3 = add2(add2(T01, S2), pk2(sqrtf(ok30 ? d30 : 1.0f), sqrtf(ok31 ? d31 : 1.0f)));
+    const f32x2 U2 = mul2(sub2(T01, nsqrt2_rn(ND, c.half)), c.half);
+    const f32x2 X3 = sub2(add2(T01, S2), nsqrt2_rn(ND3, c.half));
     const f32x2 Q = mul2(X3, c.r3);
     const f32x2 U3 = fma2(fma2(c.m3, Q, X3), c.r3, Q);
     float u10, u11, s10, s11, u20, u21, u30, u31;

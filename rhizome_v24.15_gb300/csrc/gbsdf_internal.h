@@ -128,8 +128,8 @@ void launch_active_bricks(const unsigned* brick_count, long long nbricks, unsign
 void launch_fill(float* g, long long n, float value, cudaStream_t st);
 // n_active < 0: the active-brick count is read on the device (one CTA per brick of the
 // lattice is launched and the surplus exits), so the launch needs no host round trip.
-// The band splat's error against FP64: kBandErrSamples voxels at fixed, evenly spread
-// lattice positions; those in the band (splat value <= 8h) get the FP64 distance to their
+// The band splat's error against FP64: kBandErrSamples voxels, one per equal stratum of
+// the lattice at a fixed golden-ratio offset; those in the band (splat value <= 8h) get the FP64 distance to their
 // brick's binned triangles (the splat's own candidates) and the largest difference, in
 // voxels, goes to DevState::band_err_bits / band_err_n.
 constexpr long long kBandErrSamples = 16384;

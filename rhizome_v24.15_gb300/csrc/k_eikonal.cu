@@ -601,14 +601,14 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
                 for (int hv = 0; hv < 2; ++hv) {
                     const float4 a = tvec(tile, rym, hv), b = tvec(tile, ryp, hv);
                     const float4 p = tvec(tile, rzm, hv), q = tvec(tile, rzp, hv);
-                    ay[4 * hv + 0] = fminf(fminf(a.x, b.x), kFarSentinel);
-                    ay[4 * hv + 1] = fminf(fminf(a.y, b.y), kFarSentinel);
-                    ay[4 * hv + 2] = fminf(fminf(a.z, b.z), kFarSentinel);
-                    ay[4 * hv + 3] = fminf(fminf(a.w, b.w), kFarSentinel);
-                    az[4 * hv + 0] = fminf(fminf(p.x, q.x), kFarSentinel);
-                    az[4 * hv + 1] = fminf(fminf(p.y, q.y), kFarSentinel);
-                    az[4 * hv + 2] = fminf(fminf(p.z, q.z), kFarSentinel);
-                    az[4 * hv + 3] = fminf(fminf(p.w, q.w), kFarSentinel);
+                    ay[4 * hv + 0] = min3f(a.x, b.x, kFarSentinel);
+                    ay[4 * hv + 1] = min3f(a.y, b.y, kFarSentinel);
+                    ay[4 * hv + 2] = min3f(a.z, b.z, kFarSentinel);
+                    ay[4 * hv + 3] = min3f(a.w, b.w, kFarSentinel);
+                    az[4 * hv + 0] = min3f(p.x, q.x, kFarSentinel);
+                    az[4 * hv + 1] = min3f(p.y, q.y, kFarSentinel);
+                    az[4 * hv + 2] = min3f(p.z, q.z, kFarSentinel);
+                    az[4 * hv + 3] = min3f(p.w, q.w, kFarSentinel);
                 }
                 const float nxt = (DIR > 0) ? ntile[tsw(rme, 0)] : ntile[tsw(rme, kXC - 1)];
 #pragma unroll
@@ -1305,7 +1305,7 @@ __global__ void clamp_kernel(float* __restrict__ g, const uint32_t* __restrict__
 // [F] cuda_rasterizer.cu:650-661, applied only when the verify loop came back clean
 // (on divergence the output stays untouched, cuda_rasterizer.cu:788-791). One CTA per
 // 4 rows; float4 loads and stores when the row length allows.
-// surf_tol (world units, 0 = off): voxels this close to the surface take the exact-
+// surf_tol (world units, negative = off): voxels this close to the surface take the exact-
 // arithmetic sign of a point on it (inside) -- the exact-signs modes.
 __global__ void __launch_bounds__(256) apply_kernel(const float* __restrict__ g, const uint32_t* __restrict__ sbits,
                                                     Lattice L, float* __restrict__ out, const DevState* ds,
@@ -1357,8 +1357,10 @@ void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lat
     GBSDF_COUNT_LAUNCH();
     // four lines per thread: 16-byte stores need an aligned destination (rows already are)
     if ((wsched == kWTmaVec || wsched == kWTmaVec2) && (reinterpret_cast<uintptr_t>(dst) & 15)) wsched = kWTmaPipe;
-    // packed pairs: the reference's update, at least two rows across the walk
-    if (wsched == kWTmaVec2 && (RULE != 0 || (axis == 2 ? dy : dz) < 2)) wsched = kWTmaVec;
+    // packed pairs: the reference's update, at least two rows across the walk, and a voxel
+    // size whose square-root operands stay where nsqrt2_rn is exact
+    const bool pair_ok = (RULE == 0) && pair_sqrt_ok(L.h);
+    if (wsched == kWTmaVec2 && (!pair_ok || (axis == 2 ? dy : dz) < 2)) wsched = kWTmaVec;
     if (axis != 0 && wsched == kWTmaVec2) {
         const int n_rows = (axis == 2) ? dy : dz;
         dim3 grid((dx + kWX - 1) / kWX, (n_rows + kWR - 1) / kWR);
@@ -1409,7 +1411,7 @@ void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lat
         cudaFuncSetAttribute(sweep_walk_kernel<1, RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kWSmem);
         sweep_walk_kernel<1, RULE, DIR><<<grid, kWThreads, kWSmem, st>>>(src, dst, L, round, ds);
-    } else if (xsched == kXTmaPipe2 && RULE == 0 && dy >= 2 && dz >= 2) {
+    } else if (xsched == kXTmaPipe2 && pair_ok && dy >= 2 && dz >= 2) {
         dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
         cudaFuncSetAttribute(sweep_x_pipe2_kernel<DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPSmem);
         sweep_x_pipe2_kernel<DIR><<<grid, kP2Threads, kPSmem, st>>>(src_map->map, dst, L, round, ds);

@@ -136,8 +136,10 @@ __global__ void legacy_combine_kernel(const float* __restrict__ d2, const uint32
     }
 }
 
-// Self-test: div3_rn against the IEEE quotient x / 3.0f for every non-NaN float, and
-// div3_pos for every finite non-negative one.
+// Self-test: div3_rn against the IEEE quotient x / 3.0f for every non-NaN float,
+// div3_pos for every finite non-negative one, and the packed square root nsqrt2_rn
+// against sqrtf on its range -- +0 and -0 and every float in [2^-100, 2^100] (the paired
+// updates' operands, pair_sqrt_ok).
 __global__ void selftest_div3_kernel(unsigned long long* __restrict__ mism) {
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     unsigned long long bad = 0;
@@ -147,7 +149,18 @@ __global__ void selftest_div3_kernel(unsigned long long* __restrict__ mism) {
         if (isnan(x)) continue;
         const float a = div3_rn(x), b = x / 3.0f;
         bad += (__float_as_uint(a) != __float_as_uint(b)) ? 1ull : 0ull;
-        if (i < 0x7f800000ull) bad += (__float_as_uint(div3_pos(x)) != __float_as_uint(b)) ? 1ull : 0ull;
+        if (i < 0x7f800000ull) {
+            bad += (__float_as_uint(div3_pos(x)) != __float_as_uint(b)) ? 1ull : 0ull;
+            if (i == 0 || (i >= 0x0d800000ull && i <= 0x71800000ull)) {
+                // lane 1 takes +0 at x = 0; the sign of a zero root is left open (the updates
+                // subtract it from a non-negative sum, where +0 and -0 give the same value)
+                float r0, r1;
+                up2(nsqrt2_rn(pk2(-x, i == 0 ? 0.0f : -x), pk2(0.5f, 0.5f)), r0, r1);
+                const unsigned want = __float_as_uint(-sqrtf(x)), mask = (i == 0) ? 0x7fffffffu : 0xffffffffu;
+                bad += ((__float_as_uint(r0) & mask) != (want & mask)) ? 1ull : 0ull;
+                bad += ((__float_as_uint(r1) & 0x7fffffffu) != (want & 0x7fffffffu)) ? 1ull : 0ull;
+            }
+        }
     }
     if (bad) atomicAdd(mism, bad);
 }

@@ -468,7 +468,11 @@ __global__ void __launch_bounds__(kBandErrWarps * 32)
     const long long k = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (k >= kBandErrSamples) return;
-    const long long v = (long long)(((double)k + 0.5) * (double)L.N / (double)kBandErrSamples);
+    // one voxel per stratum of N / kBandErrSamples, at a golden-ratio offset within it (an
+    // offset common to all strata would put every sample in one x column when the stratum
+    // is a multiple of the row length, as at 1024^3)
+    const double off = (double)k * 0.6180339887498949 - floor((double)k * 0.6180339887498949);
+    const long long v = (long long)(((double)k + off) * (double)L.N / (double)kBandErrSamples);
     if (v >= L.N) return;
     const float d = dist[v];
     if (!(d <= (float)kBandVoxels * L.h)) return;

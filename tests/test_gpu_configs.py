@@ -176,5 +176,8 @@ def test_blob_1024_exact_signs_matches_oracle(engine, oracle):
         lowered += int(np.count_nonzero(cg[sel] < cs[sel]))
     print(f"1024^3 blob: {len(tris)} triangles, signs and statistics equal to the oracle's ({n_lazy} voxels left "
           f"to the winding number, 4,096 sampled); {n_band} band voxels in four windows bit for bit "
-          f"({lowered} lowered by the eikonal); stated band error {res.stats['band_err_fp64']:.2e} voxel")
+          f"({lowered} lowered by the eikonal); stated band error {res.stats['band_err_fp64']:.2e} voxel "
+          f"({res.stats['band_err_samples']} samples)")
     assert n_band > 0
+    # coordinates reach 512 voxels from the origin: one FP32 ulp of a coordinate is 3.8e-5 voxel
+    assert res.stats["band_err_samples"] > 100 and 0.0 <= res.stats["band_err_fp64"] <= 1e-4
