@@ -103,7 +103,8 @@ typedef struct gbsdf_options {
     int32_t mlp_budget;    /* learned mode: most bricks proposed (0 = 1/16 of the bricks) */
     float mlp_threshold;   /* learned mode: risk probability above which a brick is proposed */
     int32_t wait_poll_limit; /* the eikonal's bounded waits on staged tiles: 0 = the default limit
-                                (2^22 polls), > 0 = that many polls, < 0 = no polling (every wait
+                                (2^17 polls, each suspending the thread for at most 20 us until
+                                the tile lands), > 0 = that many polls, < 0 = no polling (every wait
                                 gives up at once: exercises the failure path, which returns
                                 GBSDF_ECUDA with the output untouched) */
     const float* mlp_params; /* learned mode: GBSDF_MLP_PARAMS FP32 parameters in device memory */

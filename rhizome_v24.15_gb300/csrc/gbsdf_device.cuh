@@ -296,10 +296,11 @@ __device__ __forceinline__ float godunov_ref_sel(float ax, float ay, float az, f
 }
 
 // Reciprocal square root approximation (the MUFU unit; relative error below 2^-22.9 per
-// the PTX ISA's rsqrt.approx.f32).
+// the PTX ISA's rsqrt.approx). Subnormal operands flush to zero (the result is +inf):
+// nsqrt2_rn only takes zero and normal operands.
 __device__ __forceinline__ float rsqrt_approx(float a) {
     float r;
-    asm("rsqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
     return r;
 }
 
@@ -322,6 +323,36 @@ __device__ __forceinline__ f32x2 nsqrt2_rn(f32x2 NA, f32x2 half) {
     const f32x2 H = mul2(Y, half);
     const f32x2 H1 = fma2(H, fma2(NG, H, half), H);
     return fma2(fma2(NG, NG, NA), H1, NG);
+}
+
+// nsqrt2_rn for one value: the same operations on scalars.
+__device__ __forceinline__ float nsqrt_rn(float na) {
+    const float y = fminf(rsqrt_approx(fabsf(na)), 0x1p100f);
+    const float ng = na * y, hh = y * 0.5f;
+    const float h1 = __fmaf_rn(hh, __fmaf_rn(ng, hh, 0.5f), hh);
+    return __fmaf_rn(__fmaf_rn(ng, ng, na), h1, ng);
+}
+
+// godunov_ref without branches and with nsqrt_rn for the square roots (the roundings of
+// godunov_ref_pair's lanes): the 1D, 2D and 3D candidates are all formed and the
+// reference's conditions select one, so no lane waits for another's branch and the 2D
+// and 3D arithmetic overlap. m2h = -2h, na3 = -(3.0f * h * h). For voxel sizes with
+// pair_sqrt_ok.
+__device__ __forceinline__ float godunov_ref_nb(float ax, float ay, float az, float h, float m2h, float na3) {
+    const float s0 = min3f(ax, ay, az), s2 = max3f(ax, ay, az);
+    const float s1 = ax + ay + az - s0 - s2;
+    const float u1 = s0 + h;
+    const float d = s1 - s0;
+    const float dd = d * d;
+    const float nd = __fmaf_rn(m2h, h, dd);  // -disc
+    const float e1 = s2 - s1, e2 = s2 - s0;
+    const float nd3 = __fmaf_rn(__fmaf_rn(e2, e2, __fmaf_rn(e1, e1, dd)), 0.5f, na3);  // -disc3
+    const float t01 = s0 + s1;
+    const float u2 = (t01 - nsqrt_rn(nd)) * 0.5f;
+    const float u3 = div3_pos((t01 + s2) - nsqrt_rn(nd3));
+    const bool t2 = (u1 > s1) && (nd <= 0.0f);
+    const bool t3 = t2 && (u2 > s2) && (nd3 <= 0.0f);
+    return t3 ? u3 : (t2 ? u2 : u1);
 }
 
 // Voxel sizes for which every square-root operand of the paired updates lies in

@@ -336,7 +336,11 @@ constexpr int kTBox = kXC * kXHY * kXHZ;            // floats per staged tile (2
 constexpr int kTSlotBytes = 11264;                  // tile bytes rounded up to 1 KB
 constexpr int kTS = 4, kTD = 2;                     // ring slots, prefetch distance
 constexpr size_t kTSmem = (size_t)kTS * kTSlotBytes + 64 + 1024;
-constexpr int kWaitPolls = 1 << 22;
+// A tile wait polls the barrier at most kWaitPolls times; each poll suspends the waiting
+// thread until the phase completes or kWaitSuspendNs pass, so a wait ends within about
+// 2.6 s even when its copy never lands, and a thread whose tile is late does not spin.
+constexpr int kWaitPolls = 1 << 17;
+constexpr unsigned kWaitSuspendNs = 20000;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -350,9 +354,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(kWaitSuspendNs)
         : "memory");
     return ok != 0;
 }
@@ -383,8 +387,12 @@ __device__ __forceinline__ int tsw(int r, int j) { return r * 8 + ((((j >> 2) ^ 
 __device__ __forceinline__ float4 tvec(const float* tile, int r, int c) {
     return reinterpret_cast<const float4*>(tile)[r * 2 + ((c ^ (r >> 2)) & 1)];
 }
+// The first 1 KB-aligned byte of a dynamic shared-memory array (TMA tiles and their
+// swizzle want 1 KB alignment of the shared-window address). Offsetting the array's own
+// pointer, rather than rounding an integer, keeps the shared address space visible to the
+// compiler, so tile reads are shared-memory loads and not generic ones.
 __device__ __forceinline__ unsigned char* align1k(unsigned char* p) {
-    return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+    return p + ((1024u - (smem_u32(p) & 1023u)) & 1023u);
 }
 
 template <int RULE, int DIR>
@@ -527,7 +535,9 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }
 
-template <int RULE, int DIR>
+// NB: the reference's update without branches (godunov_ref_nb; RULE 0 at voxel sizes with
+// pair_sqrt_ok), identical results.
+template <int RULE, int DIR, bool NB = false>
 __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_constant__ CUtensorMap tm,
                                                                   float* __restrict__ dst, Lattice L, int round,
                                                                   DevState* ds) {
@@ -539,6 +549,7 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
     uint64_t* empty = full + kPS;
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
     const float h = L.h;
+    const float m2h = -2.0f * h, na3 = -(3.0f * h * h);
     const size_t plane = (size_t)dx * dy;
     const int tid = threadIdx.x;
     const int y0 = blockIdx.x * kXY, z0 = blockIdx.y * kXZ;
@@ -615,7 +626,9 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
                 for (int jj = 0; jj < kXC; ++jj) {
                     const int j = (DIR > 0) ? jj : (kXC - 1 - jj);
                     const float down = (DIR > 0) ? ((j + 1 < kXC) ? cur[j + 1] : nxt) : ((j > 0) ? cur[j - 1] : nxt);
-                    const float u = godunov<RULE>(fminf(prev, down), ay[j], az[j], h);
+                    float u;
+                    if constexpr (NB) u = godunov_ref_nb(fminf(prev, down), ay[j], az[j], h, m2h, na3);
+                    else u = godunov<RULE>(fminf(prev, down), ay[j], az[j], h);
                     const float out = (u < cur[j]) ? u : cur[j];
                     ch |= (u < cur[j]);
                     res[j] = out;
@@ -1417,9 +1430,15 @@ void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lat
         sweep_x_pipe2_kernel<DIR><<<grid, kP2Threads, kPSmem, st>>>(src_map->map, dst, L, round, ds);
     } else if (xsched == kXTmaPipe || xsched == kXTmaPipe2) {
         dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
-        cudaFuncSetAttribute(sweep_x_pipe_kernel<RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)kPSmem);
-        sweep_x_pipe_kernel<RULE, DIR><<<grid, kPThreads, kPSmem, st>>>(src_map->map, dst, L, round, ds);
+        if (pair_ok) {
+            cudaFuncSetAttribute(sweep_x_pipe_kernel<0, DIR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kPSmem);
+            sweep_x_pipe_kernel<0, DIR, true><<<grid, kPThreads, kPSmem, st>>>(src_map->map, dst, L, round, ds);
+        } else {
+            cudaFuncSetAttribute(sweep_x_pipe_kernel<RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kPSmem);
+            sweep_x_pipe_kernel<RULE, DIR><<<grid, kPThreads, kPSmem, st>>>(src_map->map, dst, L, round, ds);
+        }
     } else if (xsched == kXTmaRing) {
         dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
         cudaFuncSetAttribute(sweep_x_tma_kernel<RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,

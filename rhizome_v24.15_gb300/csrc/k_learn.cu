@@ -204,121 +204,448 @@ __global__ void brick_features_kernel(const float* __restrict__ base, Lattice L,
     }
 }
 
-// ---- MLP forward: one thread per sample, BF16 weights staged in shared memory ---------
-__global__ void __launch_bounds__(256) mlp_forward_kernel(const float* __restrict__ P, const float* __restrict__ X,
-                                                          long long B, float* __restrict__ logits) {
-    __shared__ __nv_bfloat16 sW1[kH * kF], sW2[kH * kH], sw3[kH];
-    __shared__ float sb1[kH], sb2[kH], sb3;
-    for (int i = threadIdx.x; i < kH * kF; i += blockDim.x) sW1[i] = __float2bfloat16_rn(P[oW1 + i]);
-    for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) sW2[i] = __float2bfloat16_rn(P[oW2 + i]);
+// ---- MLP forward on the tensor cores ------------------------------------------------
+// Warp-level mma.sync m16n8k16 (BF16 x BF16 -> FP32), one warp per 16 samples at a time.
+// Layer 1 (16 x 32 by 32 x 64) is 8 column tiles x 2 k-steps. Its FP32 accumulators, with
+// bias, ReLU and BF16 rounding, are layer 2's A operand as they stand: the accumulator
+// layout of two adjacent 8-column tiles (rows g and g+8, columns 2t and 2t+1 of each) is
+// the operand layout of one 16-deep k-step, so activations never leave registers. Layer
+// 2 (16 x 64 by 64 x 64) is 8 x 4 mma; the 64-wide output product is summed per thread and
+// across the 4 threads of a row. Products of BF16 values are exact in FP32; the sums run in
+// the tensor cores' FP32 accumulation order, not the sequential order of a scalar loop.
+// Weights are staged once per CTA as BF16 rows at padded strides (40 and 72 elements), at
+// which the 32 lanes' operand loads fall in 32 distinct banks.
+constexpr int kMmaThreads = 128;
+constexpr int kW1S = 40, kW2S = 72;
+
+// Two FP32 values rounded to BF16 (to nearest even) in one register, lo in the low half.
+__device__ __forceinline__ uint32_t pack_bf2(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__global__ void __launch_bounds__(kMmaThreads) mlp_forward_kernel(const float* __restrict__ P,
+                                                                 const float* __restrict__ X, long long B,
+                                                                 float* __restrict__ logits) {
+    __shared__ __align__(16) __nv_bfloat16 sW1[kH * kW1S];
+    __shared__ __align__(16) __nv_bfloat16 sW2[kH * kW2S];
+    __shared__ float sb1[kH], sb2[kH], sw3[kH];
+    __shared__ float sb3;
+    for (int i = threadIdx.x; i < kH * kF; i += blockDim.x)
+        sW1[(i / kF) * kW1S + (i % kF)] = __float2bfloat16_rn(P[oW1 + i]);
+    for (int i = threadIdx.x; i < kH * kH; i += blockDim.x)
+        sW2[(i / kH) * kW2S + (i % kH)] = __float2bfloat16_rn(P[oW2 + i]);
     for (int i = threadIdx.x; i < kH; i += blockDim.x) {
-        sw3[i] = __float2bfloat16_rn(P[ow3 + i]);
         sb1[i] = P[ob1 + i];
         sb2[i] = P[ob2 + i];
+        sw3[i] = bf(P[ow3 + i]);
     }
     if (threadIdx.x == 0) sb3 = P[ob3];
     __syncthreads();
-    const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= B) return;
-    float x[kF];
-    for (int i = 0; i < kF; ++i) x[i] = bf(X[s * kF + i]);
-    float h1[kH];
-    for (int j = 0; j < kH; ++j) {
-        float a = 0.0f;
-        for (int i = 0; i < kF; ++i) a = __fmaf_rn(__bfloat162float(sW1[j * kF + i]), x[i], a);
-        h1[j] = bf(fmaxf(a + sb1[j], 0.0f));
+    const uint32_t* w1 = reinterpret_cast<const uint32_t*>(sW1);
+    const uint32_t* w2 = reinterpret_cast<const uint32_t*>(sW2);
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const long long ntiles = (B + 15) / 16;
+    const long long wstride = (long long)gridDim.x * (kMmaThreads / 32);
+    for (long long tile = (long long)blockIdx.x * (kMmaThreads / 32) + (threadIdx.x >> 5); tile < ntiles;
+         tile += wstride) {
+        const long long r0 = tile * 16 + g, r1 = r0 + 8;
+        const bool v0 = r0 < B, v1 = r1 < B;
+        // layer 1 operand: the features rounded to BF16 (rows past the end read as 0)
+        uint32_t a[2][4];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const int c = 16 * s + 2 * t;
+            const float2 z2 = make_float2(0.0f, 0.0f);
+            const float2 x00 = v0 ? *reinterpret_cast<const float2*>(X + r0 * kF + c) : z2;
+            const float2 x10 = v1 ? *reinterpret_cast<const float2*>(X + r1 * kF + c) : z2;
+            const float2 x01 = v0 ? *reinterpret_cast<const float2*>(X + r0 * kF + c + 8) : z2;
+            const float2 x11 = v1 ? *reinterpret_cast<const float2*>(X + r1 * kF + c + 8) : z2;
+            a[s][0] = pack_bf2(x00.x, x00.y);
+            a[s][1] = pack_bf2(x10.x, x10.y);
+            a[s][2] = pack_bf2(x01.x, x01.y);
+            a[s][3] = pack_bf2(x11.x, x11.y);
+        }
+        float acc[8][4];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+            const int n = 8 * j + g;
+#pragma unroll
+            for (int s = 0; s < 2; ++s)
+                mma_bf16(acc[j], a[s], w1[(n * kW1S + 16 * s + 2 * t) >> 1], w1[(n * kW1S + 16 * s + 8 + 2 * t) >> 1]);
+        }
+        // bias, ReLU, BF16: the four k-steps of layer 2's operand
+        uint32_t hf[4][4];
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int j = 2 * s + q, col = 8 * j + 2 * t;
+                hf[s][2 * q] = pack_bf2(fmaxf(acc[j][0] + sb1[col], 0.0f), fmaxf(acc[j][1] + sb1[col + 1], 0.0f));
+                hf[s][2 * q + 1] =
+                    pack_bf2(fmaxf(acc[j][2] + sb1[col], 0.0f), fmaxf(acc[j][3] + sb1[col + 1], 0.0f));
+            }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+            const int n = 8 * j + g;
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+                mma_bf16(acc[j], hf[s], w2[(n * kW2S + 16 * s + 2 * t) >> 1], w2[(n * kW2S + 16 * s + 8 + 2 * t) >> 1]);
+        }
+        // output layer: this thread's 16 columns of rows g and g+8, then the row's 4 threads
+        float z0 = 0.0f, z1 = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int col = 8 * j + 2 * t;
+            z0 = __fmaf_rn(sw3[col], bf(fmaxf(acc[j][0] + sb2[col], 0.0f)), z0);
+            z0 = __fmaf_rn(sw3[col + 1], bf(fmaxf(acc[j][1] + sb2[col + 1], 0.0f)), z0);
+            z1 = __fmaf_rn(sw3[col], bf(fmaxf(acc[j][2] + sb2[col], 0.0f)), z1);
+            z1 = __fmaf_rn(sw3[col + 1], bf(fmaxf(acc[j][3] + sb2[col + 1], 0.0f)), z1);
+        }
+        z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
+        z1 += __shfl_xor_sync(0xffffffffu, z1, 1);
+        z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
+        z1 += __shfl_xor_sync(0xffffffffu, z1, 2);
+        if (t == 0) {
+            if (v0) logits[r0] = z0 + sb3;
+            if (v1) logits[r1] = z1 + sb3;
+        }
     }
-    float out = 0.0f;
-    for (int j = 0; j < kH; ++j) {
-        float a = 0.0f;
-        for (int i = 0; i < kH; ++i) a = __fmaf_rn(__bfloat162float(sW2[j * kH + i]), h1[i], a);
-        const float h2 = bf(fmaxf(a + sb2[j], 0.0f));
-        out = __fmaf_rn(__bfloat162float(sw3[j]), h2, out);
-    }
-    logits[s] = out + sb3;
 }
 
-// ---- MLP backward: weighted binary cross-entropy with logits ---------------------------
-// Each CTA accumulates the gradient of its samples in shared memory (per-thread rows,
-// reduced in a fixed order) and writes one partial; mlp_reduce_kernel sums the partials in
-// CTA order, so gradients are deterministic.
+// ---- MLP backward on the tensor cores: weighted binary cross-entropy with logits -----
+// One CTA of 4 warps takes kMlpBwdSamples = 64 samples, 16 per warp, and writes one
+// partial gradient; mlp_reduce_kernel sums the partials in CTA order, so gradients are
+// deterministic. Phase 1, each warp for its 16 samples: the forward pass as in
+// mlp_forward_kernel (mma), the loss and dL/dz, dZ2 = dL/dz * w3 where z2 > 0, and
+// dA1 = dZ2 W2 on the tensor cores straight from the accumulator layout (as the forward
+// pass chains its layers), dZ1 = dA1 where z1 > 0; the column sums for db1, db2, dw3, db3
+// by butterflies over the rows. The factors of the weight gradients go to shared memory
+// transposed, sample index fastest: A1, X (BF16, exactly the forward pass's rounded
+// values), dZ2 and dZ1 as BF16 high and low parts (hi = RN_bf16(v), lo = RN_bf16(v - hi),
+// so a product with a BF16 operand keeps about 16 bits). Phase 2, warp w: its 16 rows of
+// dW2 = dZ2^T A1 and dW1 = dZ1^T X over the 64 samples (mma, hi and lo terms).
 constexpr int kBwdThreads = 128;
+constexpr int kTS = 72;  // padded row stride (BF16) of the transposed factors, 64 samples + 8
+constexpr int kBwdSmemBytes =
+    (kH * kW1S + 2 * kH * kW2S + kH * kTS + kF * kTS + 4 * kH * kTS) * 2 + (3 * kH + 4 * (3 * kH + 2) + 4) * 4;
+static_assert(kMlpBwdSamples == 64, "one 64-sample step per CTA");
+
+__device__ __forceinline__ uint32_t ld_bf2(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// hi / lo BF16 split of v
+__device__ __forceinline__ void split_bf(float v, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+    hi = __float2bfloat16_rn(v);
+    lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+}
+
+// Sum over the 8 row groups (lanes with equal lane % 4): every lane ends with its column's total.
+__device__ __forceinline__ float rows_sum(float v) {
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 8);
+    v += __shfl_xor_sync(0xffffffffu, v, 16);
+    return v;
+}
+
 __global__ void __launch_bounds__(kBwdThreads) mlp_backward_kernel(const float* __restrict__ P,
                                                                    const float* __restrict__ X,
                                                                    const float* __restrict__ y,
                                                                    const float* __restrict__ wt, long long B,
                                                                    float* __restrict__ partial,
                                                                    float* __restrict__ loss_partial) {
-    __shared__ __nv_bfloat16 sW1[kH * kF], sW2[kH * kH], sw3[kH];
-    __shared__ float sb1[kH], sb2[kH], sb3;
-    __shared__ float acc[kMlpParams];
-    __shared__ float lred[kBwdThreads];
-    for (int i = threadIdx.x; i < kH * kF; i += blockDim.x) sW1[i] = __float2bfloat16_rn(P[oW1 + i]);
-    for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) sW2[i] = __float2bfloat16_rn(P[oW2 + i]);
+    extern __shared__ __align__(16) unsigned char bsm[];
+    __nv_bfloat16* sW1 = reinterpret_cast<__nv_bfloat16*>(bsm);   // [64][kW1S]  W1[j][c]
+    __nv_bfloat16* sW2 = sW1 + kH * kW1S;                          // [64][kW2S]  W2[j][i]
+    __nv_bfloat16* sW2T = sW2 + kH * kW2S;                         // [64][kW2S]  W2[j][i] at [i][j]
+    __nv_bfloat16* sA1T = sW2T + kH * kW2S;                        // [64 i][kTS] samples
+    __nv_bfloat16* sXT = sA1T + kH * kTS;                          // [32 c][kTS]
+    __nv_bfloat16* sD2h = sXT + kF * kTS;                          // [64 j][kTS]
+    __nv_bfloat16* sD2l = sD2h + kH * kTS;
+    __nv_bfloat16* sD1h = sD2l + kH * kTS;
+    __nv_bfloat16* sD1l = sD1h + kH * kTS;
+    float* sb1 = reinterpret_cast<float*>(sD1l + kH * kTS);
+    float* sb2 = sb1 + kH;
+    float* sw3 = sb2 + kH;
+    float* vred = sw3 + kH;  // [4 warps][db1 64 | db2 64 | dw3 64 | db3 | loss]
+    constexpr int kV = 3 * kH + 2;
+    for (int i = threadIdx.x; i < kH * kF; i += blockDim.x)
+        sW1[(i / kF) * kW1S + (i % kF)] = __float2bfloat16_rn(P[oW1 + i]);
+    for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) {
+        const __nv_bfloat16 v = __float2bfloat16_rn(P[oW2 + i]);
+        sW2[(i / kH) * kW2S + (i % kH)] = v;
+        sW2T[(i % kH) * kW2S + (i / kH)] = v;
+    }
     for (int i = threadIdx.x; i < kH; i += blockDim.x) {
-        sw3[i] = __float2bfloat16_rn(P[ow3 + i]);
         sb1[i] = P[ob1 + i];
         sb2[i] = P[ob2 + i];
+        sw3[i] = bf(P[ow3 + i]);
     }
-    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) acc[i] = 0.0f;
-    if (threadIdx.x == 0) sb3 = P[ob3];
     __syncthreads();
-    float loss = 0.0f;
-    // samples of this CTA, processed one sample per iteration by the whole CTA:
-    // thread j < 64 owns hidden unit j, which keeps every accumulation order fixed.
-    const long long first = (long long)blockIdx.x * kMlpBwdSamples;
-    const long long last = min(B, first + kMlpBwdSamples);
-    __shared__ float sx[kF], sh1[kH], sh2[kH], sd2[kH];
-    __shared__ float sdl;
-    for (long long s = first; s < last; ++s) {
-        const int j = threadIdx.x;
-        if (j < kF) sx[j] = bf(X[s * kF + j]);
-        __syncthreads();
-        if (j < kH) {
-            float a = 0.0f;
-            for (int i = 0; i < kF; ++i) a = __fmaf_rn(__bfloat162float(sW1[j * kF + i]), sx[i], a);
-            sh1[j] = a + sb1[j];  // pre-activation
-        }
-        __syncthreads();
-        if (j < kH) {
-            float a = 0.0f;
-            for (int i = 0; i < kH; ++i) a = __fmaf_rn(__bfloat162float(sW2[j * kH + i]), bf(fmaxf(sh1[i], 0.0f)), a);
-            sh2[j] = a + sb2[j];
-        }
-        __syncthreads();
-        if (j == 0) {
-            float z = sb3;
-            for (int i = 0; i < kH; ++i) z = __fmaf_rn(__bfloat162float(sw3[i]), bf(fmaxf(sh2[i], 0.0f)), z);
-            const float yy = y[s], ww = wt ? wt[s] : 1.0f;
-            // BCE with logits: w * (max(z,0) - z*y + log(1 + exp(-|z|)))
-            loss += ww * (fmaxf(z, 0.0f) - z * yy + log1pf(expf(-fabsf(z))));
-            const float p = 1.0f / (1.0f + expf(-z));
-            sdl = ww * (p - yy);
-            acc[ob3] += sdl;
-        }
-        __syncthreads();
-        if (j < kH) {
-            const float a2 = bf(fmaxf(sh2[j], 0.0f));
-            acc[ow3 + j] += sdl * a2;
-            const float d2 = (sh2[j] > 0.0f) ? sdl * __bfloat162float(sw3[j]) : 0.0f;
-            sd2[j] = d2;
-            acc[ob2 + j] += d2;
-            for (int i = 0; i < kH; ++i) acc[oW2 + j * kH + i] += d2 * bf(fmaxf(sh1[i], 0.0f));
-        }
-        __syncthreads();
-        if (j < kH) {
-            float d1 = 0.0f;
-            for (int i = 0; i < kH; ++i) d1 = __fmaf_rn(__bfloat162float(sW2[i * kH + j]), sd2[i], d1);
-            d1 = (sh1[j] > 0.0f) ? d1 : 0.0f;
-            acc[ob1 + j] += d1;
-            for (int i = 0; i < kF; ++i) acc[oW1 + j * kF + i] += d1 * sx[i];
-        }
-        __syncthreads();
+    const float b3 = P[ob3];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int q0 = 16 * warp + g, q1 = q0 + 8;  // this thread's two samples within the CTA's 64
+    const long long r0 = (long long)blockIdx.x * kMlpBwdSamples + q0, r1 = r0 + 8;
+    const bool v0 = r0 < B, v1 = r1 < B;
+    // ---- phase 1: forward, loss, back-propagation through the layers -----------------
+    uint32_t a[2][4];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const int c = 16 * s + 2 * t;
+        const float2 z2v = make_float2(0.0f, 0.0f);
+        const float2 x00 = v0 ? *reinterpret_cast<const float2*>(X + r0 * kF + c) : z2v;
+        const float2 x10 = v1 ? *reinterpret_cast<const float2*>(X + r1 * kF + c) : z2v;
+        const float2 x01 = v0 ? *reinterpret_cast<const float2*>(X + r0 * kF + c + 8) : z2v;
+        const float2 x11 = v1 ? *reinterpret_cast<const float2*>(X + r1 * kF + c + 8) : z2v;
+        a[s][0] = pack_bf2(x00.x, x00.y);
+        a[s][1] = pack_bf2(x10.x, x10.y);
+        a[s][2] = pack_bf2(x01.x, x01.y);
+        a[s][3] = pack_bf2(x11.x, x11.y);
+        const __nv_bfloat16* e0 = reinterpret_cast<const __nv_bfloat16*>(&a[s][0]);
+        const __nv_bfloat16* e1 = reinterpret_cast<const __nv_bfloat16*>(&a[s][1]);
+        const __nv_bfloat16* e2 = reinterpret_cast<const __nv_bfloat16*>(&a[s][2]);
+        const __nv_bfloat16* e3 = reinterpret_cast<const __nv_bfloat16*>(&a[s][3]);
+        sXT[c * kTS + q0] = e0[0];
+        sXT[(c + 1) * kTS + q0] = e0[1];
+        sXT[c * kTS + q1] = e1[0];
+        sXT[(c + 1) * kTS + q1] = e1[1];
+        sXT[(c + 8) * kTS + q0] = e2[0];
+        sXT[(c + 9) * kTS + q0] = e2[1];
+        sXT[(c + 8) * kTS + q1] = e3[0];
+        sXT[(c + 9) * kTS + q1] = e3[1];
     }
-    lred[threadIdx.x] = (threadIdx.x == 0) ? loss : 0.0f;
+    const uint32_t* w1 = reinterpret_cast<const uint32_t*>(sW1);
+    const uint32_t* w2 = reinterpret_cast<const uint32_t*>(sW2);
+    const uint32_t* w2t = reinterpret_cast<const uint32_t*>(sW2T);
+    float z1[8][4];  // layer-1 pre-activations
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        z1[j][0] = z1[j][1] = z1[j][2] = z1[j][3] = 0.0f;
+        const int n = 8 * j + g;
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+            mma_bf16(z1[j], a[s], w1[(n * kW1S + 16 * s + 2 * t) >> 1], w1[(n * kW1S + 16 * s + 8 + 2 * t) >> 1]);
+        const int col = 8 * j + 2 * t;
+        z1[j][0] += sb1[col];
+        z1[j][1] += sb1[col + 1];
+        z1[j][2] += sb1[col];
+        z1[j][3] += sb1[col + 1];
+    }
+    uint32_t hf[4][4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int j = 2 * s + q, col = 8 * j + 2 * t;
+            hf[s][2 * q] = pack_bf2(fmaxf(z1[j][0], 0.0f), fmaxf(z1[j][1], 0.0f));
+            hf[s][2 * q + 1] = pack_bf2(fmaxf(z1[j][2], 0.0f), fmaxf(z1[j][3], 0.0f));
+            const __nv_bfloat16* u = reinterpret_cast<const __nv_bfloat16*>(&hf[s][2 * q]);
+            const __nv_bfloat16* l = reinterpret_cast<const __nv_bfloat16*>(&hf[s][2 * q + 1]);
+            sA1T[col * kTS + q0] = u[0];
+            sA1T[(col + 1) * kTS + q0] = u[1];
+            sA1T[col * kTS + q1] = l[0];
+            sA1T[(col + 1) * kTS + q1] = l[1];
+        }
+    float z2[8][4];  // layer-2 pre-activations
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        z2[j][0] = z2[j][1] = z2[j][2] = z2[j][3] = 0.0f;
+        const int n = 8 * j + g;
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+            mma_bf16(z2[j], hf[s], w2[(n * kW2S + 16 * s + 2 * t) >> 1], w2[(n * kW2S + 16 * s + 8 + 2 * t) >> 1]);
+        const int col = 8 * j + 2 * t;
+        z2[j][0] += sb2[col];
+        z2[j][1] += sb2[col + 1];
+        z2[j][2] += sb2[col];
+        z2[j][3] += sb2[col + 1];
+    }
+    float zo0 = 0.0f, zo1 = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int col = 8 * j + 2 * t;
+        zo0 = __fmaf_rn(sw3[col], bf(fmaxf(z2[j][0], 0.0f)), zo0);
+        zo0 = __fmaf_rn(sw3[col + 1], bf(fmaxf(z2[j][1], 0.0f)), zo0);
+        zo1 = __fmaf_rn(sw3[col], bf(fmaxf(z2[j][2], 0.0f)), zo1);
+        zo1 = __fmaf_rn(sw3[col + 1], bf(fmaxf(z2[j][3], 0.0f)), zo1);
+    }
+    zo0 += __shfl_xor_sync(0xffffffffu, zo0, 1);
+    zo1 += __shfl_xor_sync(0xffffffffu, zo1, 1);
+    zo0 += __shfl_xor_sync(0xffffffffu, zo0, 2);
+    zo1 += __shfl_xor_sync(0xffffffffu, zo1, 2);
+    zo0 += b3;
+    zo1 += b3;
+    // loss and dL/dz (rows past the end contribute nothing)
+    float dz0 = 0.0f, dz1 = 0.0f, lsum = 0.0f;
+    if (v0) {
+        const float yy = y[r0], ww = wt ? wt[r0] : 1.0f;
+        lsum += ww * (fmaxf(zo0, 0.0f) - zo0 * yy + log1pf(expf(-fabsf(zo0))));
+        dz0 = ww * (1.0f / (1.0f + expf(-zo0)) - yy);
+    }
+    if (v1) {
+        const float yy = y[r1], ww = wt ? wt[r1] : 1.0f;
+        lsum += ww * (fmaxf(zo1, 0.0f) - zo1 * yy + log1pf(expf(-fabsf(zo1))));
+        dz1 = ww * (1.0f / (1.0f + expf(-zo1)) - yy);
+    }
+    // dZ2, its column sums (db2) and dw3 = sum dz * a2; dZ2 as layer-back A operand and
+    // transposed hi / lo factors
+    float* vr = vred + warp * kV;
+    uint32_t dh[4][4], dl[4][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int col = 8 * j + 2 * t;
+        float d[4];
+        d[0] = z2[j][0] > 0.0f ? dz0 * sw3[col] : 0.0f;
+        d[1] = z2[j][1] > 0.0f ? dz0 * sw3[col + 1] : 0.0f;
+        d[2] = z2[j][2] > 0.0f ? dz1 * sw3[col] : 0.0f;
+        d[3] = z2[j][3] > 0.0f ? dz1 * sw3[col + 1] : 0.0f;
+        const float c0 = rows_sum(d[0] + d[2]), c1 = rows_sum(d[1] + d[3]);
+        const float w0 = rows_sum(dz0 * bf(fmaxf(z2[j][0], 0.0f)) + dz1 * bf(fmaxf(z2[j][2], 0.0f)));
+        const float w1v = rows_sum(dz0 * bf(fmaxf(z2[j][1], 0.0f)) + dz1 * bf(fmaxf(z2[j][3], 0.0f)));
+        if (g == 0) {
+            vr[kH + col] = c0;
+            vr[kH + col + 1] = c1;
+            vr[2 * kH + col] = w0;
+            vr[2 * kH + col + 1] = w1v;
+        }
+        __nv_bfloat16 hi[4], lo[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) split_bf(d[e], hi[e], lo[e]);
+        sD2h[col * kTS + q0] = hi[0];
+        sD2h[(col + 1) * kTS + q0] = hi[1];
+        sD2h[col * kTS + q1] = hi[2];
+        sD2h[(col + 1) * kTS + q1] = hi[3];
+        sD2l[col * kTS + q0] = lo[0];
+        sD2l[(col + 1) * kTS + q0] = lo[1];
+        sD2l[col * kTS + q1] = lo[2];
+        sD2l[(col + 1) * kTS + q1] = lo[3];
+        const int s = j >> 1, q = j & 1;
+        dh[s][2 * q] = pack_bf2(__bfloat162float(hi[0]), __bfloat162float(hi[1]));
+        dh[s][2 * q + 1] = pack_bf2(__bfloat162float(hi[2]), __bfloat162float(hi[3]));
+        dl[s][2 * q] = pack_bf2(__bfloat162float(lo[0]), __bfloat162float(lo[1]));
+        dl[s][2 * q + 1] = pack_bf2(__bfloat162float(lo[2]), __bfloat162float(lo[3]));
+    }
+    {
+        const float d3 = rows_sum(dz0 + dz1);
+        const float ls = rows_sum(t == 0 ? lsum : 0.0f);
+        if (lane == 0) {
+            vr[3 * kH] = d3;
+            vr[3 * kH + 1] = ls;
+        }
+    }
+    // dA1 = dZ2 W2 (B operand: W2 transposed, rows i), dZ1 = dA1 where z1 > 0
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        const int n = 8 * m + g;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const uint32_t b0 = w2t[(n * kW2S + 16 * s + 2 * t) >> 1], b1 = w2t[(n * kW2S + 16 * s + 8 + 2 * t) >> 1];
+            mma_bf16(acc, dh[s], b0, b1);
+            mma_bf16(acc, dl[s], b0, b1);
+        }
+        const int col = 8 * m + 2 * t;
+        float d[4];
+        d[0] = z1[m][0] > 0.0f ? acc[0] : 0.0f;
+        d[1] = z1[m][1] > 0.0f ? acc[1] : 0.0f;
+        d[2] = z1[m][2] > 0.0f ? acc[2] : 0.0f;
+        d[3] = z1[m][3] > 0.0f ? acc[3] : 0.0f;
+        const float c0 = rows_sum(d[0] + d[2]), c1 = rows_sum(d[1] + d[3]);
+        if (g == 0) {
+            vr[col] = c0;
+            vr[col + 1] = c1;
+        }
+        __nv_bfloat16 hi[4], lo[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) split_bf(d[e], hi[e], lo[e]);
+        sD1h[col * kTS + q0] = hi[0];
+        sD1h[(col + 1) * kTS + q0] = hi[1];
+        sD1h[col * kTS + q1] = hi[2];
+        sD1h[(col + 1) * kTS + q1] = hi[3];
+        sD1l[col * kTS + q0] = lo[0];
+        sD1l[(col + 1) * kTS + q0] = lo[1];
+        sD1l[col * kTS + q1] = lo[2];
+        sD1l[(col + 1) * kTS + q1] = lo[3];
+    }
     __syncthreads();
-    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) partial[(long long)blockIdx.x * kMlpParams + i] = acc[i];
-    if (threadIdx.x == 0) loss_partial[blockIdx.x] = lred[0];
+    // ---- phase 2: this warp's 16 rows of dW2 and dW1 over the 64 samples -------------
+    float* out = partial + (long long)blockIdx.x * kMlpParams;
+    const int jr = 16 * warp + g;  // rows jr and jr + 8 of the slice
+    uint32_t ah[4][4], al[4][4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const int k = 16 * s + 2 * t;
+        ah[s][0] = ld_bf2(sD2h + jr * kTS + k);
+        ah[s][1] = ld_bf2(sD2h + (jr + 8) * kTS + k);
+        ah[s][2] = ld_bf2(sD2h + jr * kTS + k + 8);
+        ah[s][3] = ld_bf2(sD2h + (jr + 8) * kTS + k + 8);
+        al[s][0] = ld_bf2(sD2l + jr * kTS + k);
+        al[s][1] = ld_bf2(sD2l + (jr + 8) * kTS + k);
+        al[s][2] = ld_bf2(sD2l + jr * kTS + k + 8);
+        al[s][3] = ld_bf2(sD2l + (jr + 8) * kTS + k + 8);
+    }
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        const int n = 8 * m + g;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const uint32_t b0 = ld_bf2(sA1T + n * kTS + 16 * s + 2 * t), b1 = ld_bf2(sA1T + n * kTS + 16 * s + 8 + 2 * t);
+            mma_bf16(acc, ah[s], b0, b1);
+            mma_bf16(acc, al[s], b0, b1);
+        }
+        const int col = 8 * m + 2 * t;
+        out[oW2 + jr * kH + col] = acc[0];
+        out[oW2 + jr * kH + col + 1] = acc[1];
+        out[oW2 + (jr + 8) * kH + col] = acc[2];
+        out[oW2 + (jr + 8) * kH + col + 1] = acc[3];
+    }
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const int k = 16 * s + 2 * t;
+        ah[s][0] = ld_bf2(sD1h + jr * kTS + k);
+        ah[s][1] = ld_bf2(sD1h + (jr + 8) * kTS + k);
+        ah[s][2] = ld_bf2(sD1h + jr * kTS + k + 8);
+        ah[s][3] = ld_bf2(sD1h + (jr + 8) * kTS + k + 8);
+        al[s][0] = ld_bf2(sD1l + jr * kTS + k);
+        al[s][1] = ld_bf2(sD1l + (jr + 8) * kTS + k);
+        al[s][2] = ld_bf2(sD1l + jr * kTS + k + 8);
+        al[s][3] = ld_bf2(sD1l + (jr + 8) * kTS + k + 8);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        const int n = 8 * m + g;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const uint32_t b0 = ld_bf2(sXT + n * kTS + 16 * s + 2 * t), b1 = ld_bf2(sXT + n * kTS + 16 * s + 8 + 2 * t);
+            mma_bf16(acc, ah[s], b0, b1);
+            mma_bf16(acc, al[s], b0, b1);
+        }
+        const int col = 8 * m + 2 * t;
+        out[oW1 + jr * kF + col] = acc[0];
+        out[oW1 + jr * kF + col + 1] = acc[1];
+        out[oW1 + (jr + 8) * kF + col] = acc[2];
+        out[oW1 + (jr + 8) * kF + col + 1] = acc[3];
+    }
+    // the vector parts, summed over the 4 warps in order
+    for (int i = threadIdx.x; i < kV; i += blockDim.x) {
+        const float v = ((vred[i] + vred[kV + i]) + vred[2 * kV + i]) + vred[3 * kV + i];
+        if (i < kH) out[ob1 + i] = v;
+        else if (i < 2 * kH) out[ob2 + i - kH] = v;
+        else if (i < 3 * kH) out[ow3 + i - 2 * kH] = v;
+        else if (i == 3 * kH) out[ob3] = v;
+        else loss_partial[blockIdx.x] = v;
+    }
 }
 
 __global__ void mlp_reduce_kernel(const float* __restrict__ partial, const float* __restrict__ loss_partial,
@@ -470,8 +797,10 @@ void launch_brick_features(const float* dist, const uint32_t* S, const uint32_t*
 
 void launch_mlp_forward(const float* P, const float* X, long long B, float* logits, cudaStream_t st) {
     if (B <= 0) return;
+    const long long tiles = (B + 15) / 16;
+    const long long blocks = std::min<long long>((tiles + kMmaThreads / 32 - 1) / (kMmaThreads / 32), 152LL * 8);
     GBSDF_COUNT_LAUNCH();
-    mlp_forward_kernel<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(P, X, B, logits);
+    mlp_forward_kernel<<<(unsigned)blocks, kMmaThreads, 0, st>>>(P, X, B, logits);
 }
 
 int mlp_backward_parts(long long B) { return (int)((B + kMlpBwdSamples - 1) / kMlpBwdSamples); }
@@ -481,7 +810,8 @@ void launch_mlp_backward(const float* P, const float* X, const float* y, const f
     const int parts = mlp_backward_parts(B);
     if (parts <= 0) return;
     GBSDF_COUNT_LAUNCH();
-    mlp_backward_kernel<<<parts, kBwdThreads, 0, st>>>(P, X, y, wt, B, partial, loss_partial);
+    cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBwdSmemBytes);
+    mlp_backward_kernel<<<parts, kBwdThreads, kBwdSmemBytes, st>>>(P, X, y, wt, B, partial, loss_partial);
     GBSDF_COUNT_LAUNCH();
     mlp_reduce_kernel<<<(kMlpParams + 255) / 256, 256, 0, st>>>(partial, loss_partial, parts, grad, loss);
 }

@@ -137,9 +137,9 @@ __global__ void legacy_combine_kernel(const float* __restrict__ d2, const uint32
 }
 
 // Self-test: div3_rn against the IEEE quotient x / 3.0f for every non-NaN float,
-// div3_pos for every finite non-negative one, and the packed square root nsqrt2_rn
-// against sqrtf on its range -- +0 and -0 and every float in [2^-100, 2^100] (the paired
-// updates' operands, pair_sqrt_ok).
+// div3_pos for every finite non-negative one, and the square roots nsqrt2_rn (packed) and
+// nsqrt_rn against sqrtf on their range -- +0 and -0 and every float in [2^-100, 2^100]
+// (the updates' operands at voxel sizes with pair_sqrt_ok).
 __global__ void selftest_div3_kernel(unsigned long long* __restrict__ mism) {
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     unsigned long long bad = 0;
@@ -159,6 +159,7 @@ __global__ void selftest_div3_kernel(unsigned long long* __restrict__ mism) {
                 const unsigned want = __float_as_uint(-sqrtf(x)), mask = (i == 0) ? 0x7fffffffu : 0xffffffffu;
                 bad += ((__float_as_uint(r0) & mask) != (want & mask)) ? 1ull : 0ull;
                 bad += ((__float_as_uint(r1) & 0x7fffffffu) != (want & 0x7fffffffu)) ? 1ull : 0ull;
+                bad += ((__float_as_uint(nsqrt_rn(-x)) & mask) != (want & mask)) ? 1ull : 0ull;
             }
         }
     }
