@@ -296,42 +296,160 @@ constexpr int kSplatThreads = 128;
 constexpr int kSplatChunk = 64;
 constexpr unsigned kSplatCullMin = 256;  // triangles binned to a brick before culling starts
 
-// The staged chunk's triangles against one thread's 4 voxels (x, y, zb + 2k). CULL: skip
-// a triangle whose bounding-box distance^2 exceeds the voxel's best exact distance^2 by
-// more than both computations' rounding (a few ulps of the largest coordinate), which
-// cannot lower the minimum -- the result stays bit-identical.
-template <bool CULL>
-__device__ __forceinline__ void splat_chunk(const SplatTri* s, unsigned m, int x, int y, float px, float py,
-                                            const float wz[4], float bw, float band_sq, float best[4],
-                                            unsigned& evals) {
-    for (unsigned i = 0; i < m; ++i) {
-        const SplatTri& r = s[i];
-        if (x < r.fx0 || x > r.fx1 || y < r.fy0 || y > r.fy1) continue;
-        const float tx0 = r.bb[0], tx1 = r.bb[1], ty0 = r.bb[2], ty1 = r.bb[3], tz0 = r.bb[4], tz1 = r.bb[5];
-        const float bdx = (px < tx0) ? (tx0 - px) : ((px > tx1) ? (px - tx1) : 0.0f);
-        const float bdy = (py < ty0) ? (ty0 - py) : ((py > ty1) ? (py - ty1) : 0.0f);
-        const float bxy = bdx * bdx + bdy * bdy;
-        const f3 a = mk(r.v[0], r.v[1], r.v[2]), bb = mk(r.v[3], r.v[4], r.v[5]), c = mk(r.v[6], r.v[7], r.v[8]);
+// One staged triangle against one thread's K voxels (x, y, wz[k]). CULL: skip a triangle
+// whose bounding-box distance^2 exceeds the voxel's best exact distance^2 by more than both
+// computations' rounding (a few ulps of the largest coordinate), which cannot lower the
+// minimum -- the result stays bit-identical.
+template <bool CULL, int K>
+__device__ __forceinline__ void splat_tri(const SplatTri& r, int x, int y, float px, float py, const float (&wz)[K],
+                                          float bw, float band_sq, float (&best)[K], unsigned& evals) {
+    if (x < r.fx0 || x > r.fx1 || y < r.fy0 || y > r.fy1) return;
+    const float tx0 = r.bb[0], tx1 = r.bb[1], ty0 = r.bb[2], ty1 = r.bb[3], tz0 = r.bb[4], tz1 = r.bb[5];
+    const float bdx = (px < tx0) ? (tx0 - px) : ((px > tx1) ? (px - tx1) : 0.0f);
+    const float bdy = (py < ty0) ? (ty0 - py) : ((py > ty1) ? (py - ty1) : 0.0f);
+    const float bxy = bdx * bdx + bdy * bdy;
+    const f3 a = mk(r.v[0], r.v[1], r.v[2]), bb = mk(r.v[3], r.v[4], r.v[5]), c = mk(r.v[6], r.v[7], r.v[8]);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float z = wz[k];
-            if (z < tz0 - bw || z > tz1 + bw) continue;
-            const float bdz = (z < tz0) ? (tz0 - z) : ((z > tz1) ? (z - tz1) : 0.0f);
-            const float lb = bxy + bdz * bdz;
-            if (lb > band_sq) continue;
-            if constexpr (CULL) {
-                if (best[k] < band_sq) {
-                    const float sc = fmaxf(fmaxf(fmaxf(fabsf(px), fabsf(py)), fmaxf(fabsf(tx0), fabsf(tx1))),
-                                           fmaxf(fmaxf(fabsf(ty0), fabsf(ty1)), fmaxf(fabsf(tz0), fabsf(tz1))));
-                    const float dz = fmaxf(sc, fabsf(z)) * 3.814697265625e-6f;  // 2^-18 of the magnitude
-                    const float margin = 4.0f * dz * (sqrtf(best[k]) + dz) + best[k] * 1e-5f;
-                    if (lb > best[k] + margin) continue;
+    for (int k = 0; k < K; ++k) {
+        const float z = wz[k];
+        if (z < tz0 - bw || z > tz1 + bw) continue;
+        const float bdz = (z < tz0) ? (tz0 - z) : ((z > tz1) ? (z - tz1) : 0.0f);
+        const float lb = bxy + bdz * bdz;
+        if (lb > band_sq) continue;
+        if constexpr (CULL) {
+            if (best[k] < band_sq) {
+                const float sc = fmaxf(fmaxf(fmaxf(fabsf(px), fabsf(py)), fmaxf(fabsf(tx0), fabsf(tx1))),
+                                       fmaxf(fmaxf(fabsf(ty0), fabsf(ty1)), fmaxf(fabsf(tz0), fabsf(tz1))));
+                const float dz = fmaxf(sc, fabsf(z)) * 3.814697265625e-6f;  // 2^-18 of the magnitude
+                const float margin = 4.0f * dz * (sqrtf(best[k]) + dz) + best[k] * 1e-5f;
+                if (lb > best[k] + margin) continue;
+            }
+        }
+        const float d2 = ptd_sq(mk(px, py, z), a, bb, c);
+        ++evals;
+        if (d2 <= band_sq && d2 < best[k]) best[k] = d2;
+    }
+}
+
+// ---- dense bricks: per-sub-brick triangle lists ----------------------------------------
+// A brick with more than kSplatCullMin binned triangles is split into its eight 4^3
+// sub-bricks, one warp each (a lane owns 2 voxels of one column). A first pass over the
+// brick's list finds the sub-brick centre's nearest triangle T*: every lattice point v of
+// the sub-brick has d(v, T*) <= d(centre, T*) + R (R the half-diagonal of the sub-brick's
+// point box), so a triangle whose bounding box is farther than that from the point box
+// cannot be nearer than T* to any of its voxels. The second pass stages the list again and
+// each warp keeps, per chunk, only the triangles that pass this test (widened by 16 x 2^-18
+// of the coordinate magnitude for the rounding of both sides), then runs the per-voxel
+// update on them. Skipped triangles never hold a voxel's minimum, so the distances are the
+// sparse kernel's, bit for bit; the screening work drops from 512 voxel tests per triangle
+// to 8 exact distances plus the survivors' tests.
+constexpr int kDenseThreads = 256;
+
+__global__ void __launch_bounds__(kDenseThreads) splat_dense_kernel(
+    const SplatTri* __restrict__ stt, const unsigned long long* __restrict__ off, const unsigned* __restrict__ cnt,
+    const unsigned* __restrict__ list, const unsigned* __restrict__ active, Lattice L, float* __restrict__ dist,
+    DevState* ds) {
+    __shared__ SplatTri s[kSplatChunk];
+    __shared__ unsigned char keep_idx[kDenseThreads / 32][kSplatChunk];
+    if (blockIdx.x >= ds->active_bricks || ds->overflow) return;
+    const unsigned b = active[blockIdx.x];
+    const unsigned n = cnt[b];
+    if (n <= kSplatCullMin) return;  // splat_kernel's brick
+    const int nbx = L.nb[0], nby = L.nb[1];
+    const int bx = (int)(b % (unsigned)nbx), by = (int)((b / (unsigned)nbx) % (unsigned)nby),
+              bz = (int)(b / ((unsigned)nbx * (unsigned)nby));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int x0 = bx * kBrick + (warp & 1) * 4, y0 = by * kBrick + ((warp >> 1) & 1) * 4,
+              z0 = bz * kBrick + (warp >> 2) * 4;
+    const int x = x0 + (lane & 3), y = y0 + ((lane >> 2) & 3), zl = lane >> 4;
+    const float h = L.h;
+    const float bw = (float)kBandVoxels * h;
+    const float band_sq = bw * bw;
+    const float px = (float)(L.mn[0] + x) * h, py = (float)(L.mn[1] + y) * h;
+    float wz[2], best[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        wz[k] = (float)(L.mn[2] + z0 + zl + 2 * k) * h;
+        best[k] = __int_as_float(0x7f800000);
+    }
+    // the sub-brick's point box (the lattice coordinates its voxels compute) and centre
+    const float sx0 = (float)(L.mn[0] + x0) * h, sx1 = (float)(L.mn[0] + x0 + 3) * h;
+    const float sy0 = (float)(L.mn[1] + y0) * h, sy1 = (float)(L.mn[1] + y0 + 3) * h;
+    const float sz0 = (float)(L.mn[2] + z0) * h, sz1 = (float)(L.mn[2] + z0 + 3) * h;
+    const f3 ctr = mk(0.5f * (sx0 + sx1), 0.5f * (sy0 + sy1), 0.5f * (sz0 + sz1));
+    const float mag = fmaxf(fmaxf(fmaxf(fabsf(sx0), fabsf(sx1)), fmaxf(fabsf(sy0), fabsf(sy1))),
+                            fmaxf(fabsf(sz0), fabsf(sz1))) + bw;
+    const unsigned long long o = off[b];
+    const int* src = reinterpret_cast<const int*>(stt);
+    int* dsm = reinterpret_cast<int*>(s);
+    // pass 1: the centre's nearest triangle
+    float u2 = __int_as_float(0x7f800000);
+    for (unsigned c0 = 0; c0 < n; c0 += kSplatChunk) {
+        const unsigned m = min((unsigned)kSplatChunk, n - c0);
+        for (unsigned w = tid; w < m * 24u; w += kDenseThreads) {
+            const unsigned rec = w / 24u, word = w - rec * 24u;
+            dsm[w] = __ldg(src + (size_t)list[o + c0 + rec] * 24 + word);
+        }
+        __syncthreads();
+        for (unsigned i = lane; i < m; i += 32) {
+            const SplatTri& r = s[i];
+            u2 = fminf(u2, ptd_sq(ctr, mk(r.v[0], r.v[1], r.v[2]), mk(r.v[3], r.v[4], r.v[5]),
+                                  mk(r.v[6], r.v[7], r.v[8])));
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int sh = 16; sh > 0; sh >>= 1) u2 = fminf(u2, __shfl_xor_sync(0xffffffffu, u2, sh));
+    const float ex = sx1 - sx0, ey = sy1 - sy0, ez = sz1 - sz0;
+    const float ub = sqrtf(u2) + 0.5f * sqrtf(ex * ex + ey * ey + ez * ez) + 16.0f * mag * 3.814697265625e-6f;
+    const float ub2 = ub * ub;
+    // pass 2: per chunk, this warp's surviving triangles, then the per-voxel update
+    unsigned evals = 0;
+    for (unsigned c0 = 0; c0 < n; c0 += kSplatChunk) {
+        const unsigned m = min((unsigned)kSplatChunk, n - c0);
+        for (unsigned w = tid; w < m * 24u; w += kDenseThreads) {
+            const unsigned rec = w / 24u, word = w - rec * 24u;
+            dsm[w] = __ldg(src + (size_t)list[o + c0 + rec] * 24 + word);
+        }
+        __syncthreads();
+        unsigned nk = 0;
+        for (unsigned base = 0; base < m; base += 32) {
+            const unsigned i = base + lane;
+            bool keep = false;
+            if (i < m) {
+                const SplatTri& r = s[i];
+                if (!(x0 + 3 < r.fx0 || x0 > r.fx1 || y0 + 3 < r.fy0 || y0 > r.fy1)) {
+                    const float gx = fmaxf(fmaxf(r.bb[0] - sx1, sx0 - r.bb[1]), 0.0f);
+                    const float gy = fmaxf(fmaxf(r.bb[2] - sy1, sy0 - r.bb[3]), 0.0f);
+                    const float gz = fmaxf(fmaxf(r.bb[4] - sz1, sz0 - r.bb[5]), 0.0f);
+                    keep = gx * gx + gy * gy + gz * gz <= ub2;
                 }
             }
-            const float d2 = ptd_sq(mk(px, py, z), a, bb, c);
-            ++evals;
-            if (d2 <= band_sq && d2 < best[k]) best[k] = d2;
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            if (keep) keep_idx[warp][nk + __popc(bal & ((1u << lane) - 1u))] = (unsigned char)i;
+            nk += __popc(bal);
         }
+        __syncwarp();
+        for (unsigned j = 0; j < nk; ++j)
+            splat_tri<true, 2>(s[keep_idx[warp][j]], x, y, px, py, wz, bw, band_sq, best, evals);
+        __syncthreads();
+    }
+    unsigned found = 0;
+    if (x < L.dims[0] && y < L.dims[1]) {
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int z = z0 + zl + 2 * k;
+            if (z < L.dims[2] && best[k] != __int_as_float(0x7f800000)) {
+                dist[((size_t)z * L.dims[1] + y) * L.dims[0] + x] = sqrtf(best[k]);
+                ++found;
+            }
+        }
+    }
+    const unsigned fw = __reduce_add_sync(0xffffffffu, found);
+    const unsigned ew = __reduce_add_sync(0xffffffffu, evals);
+    if (lane == 0) {
+        if (fw) atomicAdd(&ds->band_voxels, (unsigned long long)fw);
+        if (ew) atomicAdd(&ds->splat_evals, (unsigned long long)ew);
     }
 }
 
@@ -361,9 +479,9 @@ __global__ void __launch_bounds__(kSplatThreads) splat_kernel(
     }
     const unsigned long long o = off[b];
     const unsigned n = cnt[b];
-    // culling pays where many triangles compete for a brick (dense meshes); with few, its
-    // test costs more than the evaluations it saves
-    const bool cull = n > kSplatCullMin;
+    // bricks with many triangles are splat_dense_kernel's (culling pays there; with few
+    // triangles its tests cost more than the evaluations they save)
+    if (n > kSplatCullMin) return;
     unsigned evals = 0;
     for (unsigned c0 = 0; c0 < n; c0 += kSplatChunk) {
         unsigned m = min((unsigned)kSplatChunk, n - c0);
@@ -376,10 +494,7 @@ __global__ void __launch_bounds__(kSplatThreads) splat_kernel(
             dsm[w] = __ldg(src + (size_t)t * 24 + word);
         }
         __syncthreads();
-        if (cull)
-            splat_chunk<true>(s, m, x, y, px, py, wz, bw, band_sq, best, evals);
-        else
-            splat_chunk<false>(s, m, x, y, px, py, wz, bw, band_sq, best, evals);
+        for (unsigned i = 0; i < m; ++i) splat_tri<false, 4>(s[i], x, y, px, py, wz, bw, band_sq, best, evals);
         __syncthreads();
     }
     unsigned found = 0;
@@ -520,6 +635,9 @@ void launch_splat(const SplatTri* stt, const unsigned long long* brick_off, cons
     GBSDF_COUNT_LAUNCH();
     splat_kernel<<<(unsigned)blocks, kSplatThreads, 0, st>>>(stt, brick_off, brick_count, brick_list, active, L,
                                                              dist, ds);
+    GBSDF_COUNT_LAUNCH();
+    splat_dense_kernel<<<(unsigned)blocks, kDenseThreads, 0, st>>>(stt, brick_off, brick_count, brick_list, active,
+                                                                   L, dist, ds);
 }
 
 }  // namespace gbsdf
