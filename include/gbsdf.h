@@ -114,7 +114,8 @@ typedef struct gbsdf_options {
                                staged by cp.async, 2 by TMA tiles on a CTA-barrier ring, 3 by TMA
                                tiles on a warp-specialised mbarrier pipeline, 4 the same with two
                                lines per thread updated in packed FP32 pairs (the reference's
-                               update at voxel sizes 2^-20 to 2^20; otherwise 3 runs); w = 1 y / z walks
+                               update at voxel sizes 2^-20 to 2^20; otherwise 3 runs), 5 the
+                               pipeline with 16-voxel chunks staged as 20-column boxes; w = 1 y / z walks
                                staged by cp.async, 2 by TMA batches on a pipeline, 3 the same
                                with four adjacent lines per thread, 4 the same with the lines'
                                updates in packed FP32 pairs (the reference's update at voxel

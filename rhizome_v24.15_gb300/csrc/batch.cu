@@ -348,7 +348,7 @@ int plan(gbsdf_batch& b, BErr& e) {
             j.xsched1 = plan1.x;
             j.wsched1 = plan1.w;
             const int xs_opt = b.sweep_schedule % 10, ws_opt = b.sweep_schedule / 10;
-            if (xs_opt >= kXCpAsync && xs_opt <= kXTmaPipe2) j.xsched = j.xsched1 = xs_opt;
+            if (xs_opt >= kXCpAsync && xs_opt <= kXTmaWide) j.xsched = j.xsched1 = xs_opt;
             if (ws_opt >= kWCpAsync && ws_opt <= kWTmaVec2) j.wsched = j.wsched1 = ws_opt;
         }
     // counting pass

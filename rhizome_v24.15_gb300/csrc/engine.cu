@@ -401,7 +401,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     SweepPlan plan;
     auto set_plan = [&](int phase) -> int {
         plan = tuned_sweep_plan(w.device, L, src, dst, map_of(src), w.ds, st, tune, phase);
-        if (xs_opt >= kXCpAsync && xs_opt <= kXTmaPipe2) plan.x = xs_opt;
+        if (xs_opt >= kXCpAsync && xs_opt <= kXTmaWide) plan.x = xs_opt;
         if (ws_opt >= kWCpAsync && ws_opt <= kWTmaVec2) plan.w = ws_opt;
         GB_CK(cudaGetLastError());
         return (int)GBSDF_OK;

@@ -242,16 +242,20 @@ struct GridMap {
     CUtensorMap map;   // x sweep tile: 8 (x) x 34 (y) x 10 (z), 32-byte swizzle
     CUtensorMap ymap;  // y walk batch: 40 (x) x 4 (y slices) x 18 (z rows)
     CUtensorMap zmap;  // z walk batch: 40 (x) x 18 (y rows) x 4 (z slices)
+    CUtensorMap wmap;  // wide x sweep tile: 20 (x) x 34 (y) x 10 (z), no swizzle
     bool valid;
     bool walk_valid;
+    bool wide_valid;
 };
 bool encode_grid_map(GridMap& m, const float* base, const Lattice& L);
 // Schedules of the x sweep (all give identical results): staged by per-thread cp.async
 // copies, by TMA tiles on a CTA-barrier ring, by TMA tiles on a warp-specialised mbarrier
 // pipeline, the same pipeline with two lines per thread updated in packed FP32 pairs (the
 // reference's update on lattices with at least two voxels along y and z; elsewhere it runs
-// as the pipeline). 0 picks the pipeline when a TMA descriptor is valid.
-enum XSchedule : int { kXAuto = 0, kXCpAsync = 1, kXTmaRing = 2, kXTmaPipe = 3, kXTmaPipe2 = 4 };
+// as the pipeline), or the pipeline with 16-voxel chunks staged as 20-column boxes (one
+// copy per chunk carries its downstream neighbour). 0 picks the pipeline when a TMA
+// descriptor is valid.
+enum XSchedule : int { kXAuto = 0, kXCpAsync = 1, kXTmaRing = 2, kXTmaPipe = 3, kXTmaPipe2 = 4, kXTmaWide = 5 };
 // Schedules of the y and z walks: cp.async slice ring, TMA batches on a warp-specialised
 // mbarrier pipeline (one line per thread in two rows, or four adjacent lines per thread,
 // or four adjacent lines per thread updated in packed FP32 pairs -- the reference's

@@ -844,6 +844,146 @@ __global__ void __launch_bounds__(kP2Threads, 4) sweep_x_pipe2_kernel(const __gr
     mark_changed(ch, &ds->changed[round]);
 }
 
+// ---- x sweeps, wide TMA tiles ----------------------------------------------------------
+// sweep_x_pipe_kernel's lines, warps and per-line arithmetic with 16-voxel chunks staged as
+// 20 (x) x 34 (y) x 10 (z) boxes: 80-byte rows, fewer and longer rows per copy than the
+// 32-byte rows of the 8-voxel chunks. No swizzle is needed: at a row pitch of 20 words, 8
+// lanes' 16-byte loads of 8 consecutive rows fall in 32 distinct banks. A box starts at
+// x = 16c (DIR > 0: its last 4 columns are the next chunk's first) or 16c - 4 (DIR < 0: its
+// first 4 columns are the previous chunk's last), 16-byte aligned either way (a negative
+// start reads the out-of-lattice fill), so a chunk's downstream neighbour arrives with it
+// and each chunk waits for one copy. A 2-slot ring; every wait bounded as in the pipeline.
+constexpr int kXW = 16;                                       // voxels per chunk
+constexpr int kXWB = kXW + 4;                                 // box columns
+constexpr int kXWS = 2;                                       // ring slots
+constexpr int kXWBox = kXWB * kXHY * kXHZ;                    // floats per box (6800)
+constexpr int kXWSlotBytes = (kXWBox * 4 + 1023) / 1024 * 1024;
+constexpr size_t kXWSmem = (size_t)kXWS * kXWSlotBytes + 64 + 1024;
+
+template <int RULE, int DIR, bool NB>
+__global__ void __launch_bounds__(kPThreads) sweep_x_wide_kernel(const __grid_constant__ CUtensorMap tm,
+                                                                  float* __restrict__ dst, Lattice L, int round,
+                                                                  DevState* ds) {
+    if (ds->stop) return;
+    const int polls = wait_poll_limit(ds);
+    extern __shared__ unsigned char tsm_raw[];
+    unsigned char* tsm = align1k(tsm_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kXWS * kXWSlotBytes);
+    uint64_t* empty = full + kXWS;
+    const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
+    const float h = L.h;
+    const float m2h = -2.0f * h, na3 = -(3.0f * h * h);
+    const size_t plane = (size_t)dx * dy;
+    const int tid = threadIdx.x;
+    const int y0 = blockIdx.x * kXY, z0 = blockIdx.y * kXZ;
+    const int nchunks = (dx + kXW - 1) / kXW;
+    if (tid == 0) {
+        for (int s = 0; s < kXWS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kXThreads / 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();  // the only CTA-wide barrier: the ring's barriers are initialised
+    if (tid >= kXThreads) {
+        if (tid != kXThreads) return;
+        int ci = 0;
+        for (; ci < nchunks; ++ci) {
+            const int s = ci % kXWS;
+            if (ci >= kXWS && !mbar_wait(&empty[s], ((ci / kXWS) - 1) & 1, polls)) break;
+            const int c = (DIR > 0) ? ci : (nchunks - 1 - ci);
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            mbar_expect_tx(&full[s], kXWBox * 4);
+            tma_load_3d(tsm + s * kXWSlotBytes, &tm, (DIR > 0) ? c * kXW : c * kXW - 4, y0 - 1, z0 - 1, &full[s]);
+        }
+        for (int k = max(0, ci - kXWS); k < ci; ++k) mbar_wait(&full[k % kXWS], (k / kXWS) & 1);
+        if (ci < nchunks) atomicAdd(&ds->wait_timeouts, 1ull);
+        return;
+    }
+    const int ty = tid & 31, tz = tid >> 5;
+    const int y = y0 + ty, z = z0 + tz;
+    const bool active = (y < dy) && (z < dz);
+    const int rme = (tz + 1) * kXHY + (ty + 1);
+    const int cb = (DIR > 0) ? 0 : 4;  // tile column of the chunk's first voxel
+    float prev = kFarSentinel;
+    bool ch = false;
+#pragma unroll 1
+    for (int ci = 0; ci < nchunks; ++ci) {
+        const bool ok = mbar_wait(&full[ci % kXWS], (ci / kXWS) & 1, polls);
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (ty == 0) atomicAdd(&ds->wait_timeouts, 1ull);
+            return;
+        }
+        const int c = (DIR > 0) ? ci : (nchunks - 1 - ci);
+        const int xc = c * kXW;
+        if (active) {
+            const float* tile = reinterpret_cast<const float*>(tsm + (ci % kXWS) * kXWSlotBytes);
+            const float* me = tile + rme * kXWB + cb;
+            const float* yl = tile + (rme - 1) * kXWB + cb;
+            const float* yh = tile + (rme + 1) * kXWB + cb;
+            const float* zl = tile + (rme - kXHY) * kXWB + cb;
+            const float* zh = tile + (rme + kXHY) * kXWB + cb;
+            float* drow = dst + (size_t)z * plane + (size_t)y * dx + xc;
+            if (xc + kXW <= dx) {
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) {
+                    const int q = (DIR > 0) ? qq : 3 - qq;
+                    const float4 m = *reinterpret_cast<const float4*>(me + 4 * q);
+                    const float4 a = *reinterpret_cast<const float4*>(yl + 4 * q);
+                    const float4 b = *reinterpret_cast<const float4*>(yh + 4 * q);
+                    const float4 p = *reinterpret_cast<const float4*>(zl + 4 * q);
+                    const float4 r = *reinterpret_cast<const float4*>(zh + 4 * q);
+                    const float cur[4] = {m.x, m.y, m.z, m.w};
+                    const float ay[4] = {min3f(a.x, b.x, kFarSentinel), min3f(a.y, b.y, kFarSentinel),
+                                         min3f(a.z, b.z, kFarSentinel), min3f(a.w, b.w, kFarSentinel)};
+                    const float az[4] = {min3f(p.x, r.x, kFarSentinel), min3f(p.y, r.y, kFarSentinel),
+                                         min3f(p.z, r.z, kFarSentinel), min3f(p.w, r.w, kFarSentinel)};
+                    // the quad's downstream neighbour beyond its last cell in walk order
+                    const int xe = (DIR > 0) ? xc + 4 * q + 4 : xc + 4 * q - 1;
+                    const float end = (xe >= 0 && xe < dx) ? me[(DIR > 0) ? 4 * q + 4 : 4 * q - 1] : kFarSentinel;
+                    float res[4];
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) {
+                        const int j = (DIR > 0) ? jj : 3 - jj;
+                        const float down = (DIR > 0) ? ((j < 3) ? cur[j + 1] : end) : ((j > 0) ? cur[j - 1] : end);
+                        float u;
+                        if constexpr (NB) u = godunov_ref_nb(fminf(prev, down), ay[j], az[j], h, m2h, na3);
+                        else u = godunov<RULE>(fminf(prev, down), ay[j], az[j], h);
+                        const bool lo = u < cur[j];
+                        res[j] = lo ? u : cur[j];
+                        ch |= lo;
+                        prev = res[j];
+                    }
+                    reinterpret_cast<float4*>(drow)[q] = make_float4(res[0], res[1], res[2], res[3]);
+                }
+            } else {
+                // the lattice's last, partial chunk
+#pragma unroll 1
+                for (int jj = 0; jj < kXW; ++jj) {
+                    const int j = (DIR > 0) ? jj : kXW - 1 - jj;
+                    const int x = xc + j;
+                    if (x >= dx) continue;
+                    const float cur = me[j];
+                    const float down = (x + DIR >= 0 && x + DIR < dx) ? me[j + DIR] : kFarSentinel;
+                    const float ayj = min3f(yl[j], yh[j], kFarSentinel);
+                    const float azj = min3f(zl[j], zh[j], kFarSentinel);
+                    float u;
+                    if constexpr (NB) u = godunov_ref_nb(fminf(prev, down), ayj, azj, h, m2h, na3);
+                    else u = godunov<RULE>(fminf(prev, down), ayj, azj, h);
+                    const bool lo = u < cur;
+                    const float out = lo ? u : cur;
+                    ch |= lo;
+                    drow[j] = out;
+                    prev = out;
+                }
+            }
+        }
+        __syncwarp();
+        if (ty == 0) mbar_arrive(&empty[ci % kXWS]);
+    }
+    mark_changed(ch, &ds->changed[round]);
+}
+
 // ---- y and z walks, TMA batches on a warp-specialised pipeline ------------------------
 // The lines, tile (32 x 16 lines, two per thread) and per-line arithmetic of
 // sweep_walk_kernel; the slices come in batches of 4, one cp.async.bulk.tensor copy per
@@ -1428,7 +1568,19 @@ void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lat
         dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
         cudaFuncSetAttribute(sweep_x_pipe2_kernel<DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPSmem);
         sweep_x_pipe2_kernel<DIR><<<grid, kP2Threads, kPSmem, st>>>(src_map->map, dst, L, round, ds);
-    } else if (xsched == kXTmaPipe || xsched == kXTmaPipe2) {
+    } else if (xsched == kXTmaWide && src_map->wide_valid) {
+        dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
+        if (pair_ok) {
+            cudaFuncSetAttribute(sweep_x_wide_kernel<0, DIR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kXWSmem);
+            sweep_x_wide_kernel<0, DIR, true><<<grid, kPThreads, kXWSmem, st>>>(src_map->wmap, dst, L, round, ds);
+        } else {
+            cudaFuncSetAttribute(sweep_x_wide_kernel<RULE, DIR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kXWSmem);
+            sweep_x_wide_kernel<RULE, DIR, false><<<grid, kPThreads, kXWSmem, st>>>(src_map->wmap, dst, L, round,
+                                                                                   ds);
+        }
+    } else if (xsched == kXTmaPipe || xsched == kXTmaPipe2 || xsched == kXTmaWide) {
         dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
         if (pair_ok) {
             cudaFuncSetAttribute(sweep_x_pipe_kernel<0, DIR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1488,6 +1640,7 @@ bool encode_box(CUtensorMap* m, const float* base, int dx, int dy, int dz, int b
 bool encode_grid_map(GridMap& m, const float* base, const Lattice& L) {
     m.valid = false;
     m.walk_valid = false;
+    m.wide_valid = false;
     // row and plane pitches must be multiples of 16 bytes, the base 16-byte aligned
     if ((L.dims[0] & 3) != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
     m.valid = encode_box(&m.map, base, L.dims[0], L.dims[1], L.dims[2]);
@@ -1496,6 +1649,8 @@ bool encode_grid_map(GridMap& m, const float* base, const Lattice& L) {
                               CU_TENSOR_MAP_SWIZZLE_NONE) &&
                    encode_box(&m.zmap, base, L.dims[0], L.dims[1], L.dims[2], kWPX, kWHR, kWPB,
                               CU_TENSOR_MAP_SWIZZLE_NONE);
+    m.wide_valid = m.valid && encode_box(&m.wmap, base, L.dims[0], L.dims[1], L.dims[2], kXWB, kXHY, kXHZ,
+                                         CU_TENSOR_MAP_SWIZZLE_NONE);
     return m.valid;
 }
 

@@ -72,7 +72,7 @@ SweepPlan tuned_sweep_plan(int device, const Lattice& L, const float* src, float
     };
     if (tma) {
         float best = 1e30f;
-        for (int cand : {kXCpAsync, kXTmaRing, kXTmaPipe, kXTmaPipe2}) {
+        for (int cand : {kXCpAsync, kXTmaRing, kXTmaPipe, kXTmaPipe2, kXTmaWide}) {
             const float ms = time_it(0, cand, plan.w);
             if (ms >= 0.0f && ms < best) {
                 best = ms;

@@ -18,7 +18,7 @@ def _mug():
     return meshgen.to_triangles(vf, f), mn, mx, 2.0
 
 
-@pytest.mark.parametrize("sched", [22, 33, 43, 44])
+@pytest.mark.parametrize("sched", [22, 33, 43, 44, 45])
 def test_tile_wait_timeout_reports_error_and_leaves_output(engine, oracle, sched):
     from gbsdf import _lib
 

@@ -1,5 +1,6 @@
 """The eikonal sweep schedules -- x sweep staged by cp.async, by TMA tiles on a CTA-barrier
-ring or on a warp-specialised mbarrier pipeline (one or two lines per thread); y / z walks staged by cp.async or by TMA
+ring or on a warp-specialised mbarrier pipeline (one or two lines per thread, or wide 16-voxel
+chunks); y / z walks staged by cp.async or by TMA
 batches on a pipeline (one or four lines per thread, the four lines' updates scalar or in
 packed FP32 pairs) -- and the autotuner's pick give
 bit-identical grids, equal to the oracle, on lattices whose rows do and do not admit TMA
@@ -22,7 +23,7 @@ def _case(dims):
 def test_schedules_identical(engine, oracle, dims):
     tris, mn, mx, h = _case(dims)
     outs = {}
-    scheds = (0, 1, 2, 3, 4, 13, 23, 33, 43, 44, 11, 21, 31, 41)
+    scheds = (0, 1, 2, 3, 4, 5, 13, 23, 33, 43, 44, 45, 11, 21, 31, 41, 15)
     for sched in scheds:
         out, res = engine.compute_mesh_sdf(tris, h, mn, mx, mode=engine.MODE_EXACT_SIGNS, path=engine.PATH_FAST,
                                            sweep_schedule=sched)
