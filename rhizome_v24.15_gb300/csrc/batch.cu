@@ -165,8 +165,9 @@ void place_learned(Job& j, Carver& c) {
 void place_phase1(Job& j, Carver& c) {
     const Lattice& L = j.L;
     const long long N = L.N, T = j.T;
-    j.A = c.take<float>((size_t)N * 4);
-    j.B = c.take<float>((size_t)N * 4);
+    // the grid copies also hold the eikonal's padded layout (rows of a multiple of 4 floats)
+    j.A = c.take<float>((size_t)std::max(N, padded_voxels(L)) * 4);
+    j.B = c.take<float>((size_t)std::max(N, padded_voxels(L)) * 4);
     j.S = c.take<uint32_t>((size_t)L.nwords * 4);
     j.U = c.take<uint32_t>((size_t)L.nwords * 4);
     j.t12 = c.take<float>((size_t)T * 48);
@@ -259,18 +260,24 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
         }
     };
     fixup_passes(learned ? j.E : nullptr);
-    // [D]: the reference's round loop, stopped on the device when a round changes nothing
-    float* src = j.A;
-    float* dst = j.B;
+    // [D]: the reference's round loop, stopped on the device when a round changes nothing;
+    // a lattice whose rows are not a multiple of 4 floats is swept in padded copies (B <->
+    // A), the result copied back into A
+    const Lattice Lp = padded(L);
+    const bool pad = Lp.px != L.dims[0];
+    float* src = pad ? j.B : j.A;
+    float* dst = pad ? j.A : j.B;
+    if (pad) launch_pad_rows(j.A, j.B, Lp, st);
     for (int r = 0; r < kMaxRounds; ++r) {
         for (int axis = 0; axis < 3; ++axis)
             for (int dir = 1; dir >= -1; dir -= 2) {
-                launch_sweep(0, axis, dir, r, src, dst, L, j.ds, st, src == j.A ? &j.map_a : &j.map_b,
+                launch_sweep(0, axis, dir, r, src, dst, Lp, j.ds, st, src == j.A ? &j.map_a : &j.map_b,
                              r == 0 ? j.xsched : j.xsched1, r == 0 ? j.wsched : j.wsched1);
                 std::swap(src, dst);
             }
         launch_end_round(r, r, kMaxRounds, j.ds, st);
     }
+    if (pad) launch_unpad_rows(j.B, j.A, Lp, st);
     launch_audit(j.A, L, j.ds, st);
     launch_clamp(j.A, j.S, L, j.ds, st);
     // [E]
@@ -339,10 +346,11 @@ int plan(gbsdf_batch& b, BErr& e) {
         if (j.pre_status == GBSDF_OK) {
             place_phase1(j, p1);
             if (learned_mode(b)) place_learned(j, p1);
-            encode_grid_map(j.map_a, j.A, j.L);
-            encode_grid_map(j.map_b, j.B, j.L);
-            const SweepPlan plan = tuned_sweep_plan(b.device, j.L, j.A, j.B, &j.map_a, j.ds, b.origin, false, 0);
-            const SweepPlan plan1 = tuned_sweep_plan(b.device, j.L, j.A, j.B, &j.map_a, j.ds, b.origin, false, 1);
+            const Lattice Lp = padded(j.L);
+            encode_grid_map(j.map_a, j.A, Lp);
+            encode_grid_map(j.map_b, j.B, Lp);
+            const SweepPlan plan = tuned_sweep_plan(b.device, Lp, j.A, j.B, &j.map_a, j.ds, b.origin, false, 0);
+            const SweepPlan plan1 = tuned_sweep_plan(b.device, Lp, j.A, j.B, &j.map_a, j.ds, b.origin, false, 1);
             j.xsched = plan.x;
             j.wsched = plan.w;
             j.xsched1 = plan1.x;

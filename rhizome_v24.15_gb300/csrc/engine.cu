@@ -47,6 +47,7 @@ Lattice make_lattice(const int32_t mn[3], const int32_t mx[3], float h) {
     L.nbricks = (long long)L.nb[0] * L.nb[1] * L.nb[2];
     L.nsx = (L.dims[0] + kStrip - 1) / kStrip;
     L.nstrips = (long long)L.nsx * L.dims[1];
+    L.px = L.dims[0];
     return L;
 }
 
@@ -296,8 +297,9 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     const float stol = exact_signs ? kSurfaceTolExactSigns : kSurfaceTolVoxels;
     const long long N = L.N;
     // ---- buffers
-    GB_CK(ensure(w.A, (size_t)N * 4));
-    GB_CK(ensure(w.B, (size_t)N * 4));
+    // the grid copies also hold the eikonal's padded layout (rows of a multiple of 4 floats)
+    GB_CK(ensure(w.A, (size_t)std::max(N, padded_voxels(L)) * 4));
+    GB_CK(ensure(w.B, (size_t)std::max(N, padded_voxels(L)) * 4));
     GB_CK(ensure(w.S, (size_t)L.nwords * 4));
     GB_CK(ensure(w.U, (size_t)L.nwords * 4));
     GB_CK(ensure(w.t9, (size_t)T * 36));
@@ -387,12 +389,18 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     GB_CK(cudaEventRecord(w.ev[5], st));
     // ---- [D]
     const int rule = ref_eikonal ? 0 : 1;
-    float* src = P<float>(w.A);
-    float* dst = P<float>(w.B);
-    // TMA descriptors of the two grid copies for the staged x sweeps
+    // The sweeps address rows of a multiple of 4 floats (TMA descriptors need 16-byte row
+    // pitches): a lattice whose rows are not is swept in padded copies -- the band field
+    // copied into B, the rounds ping-ponging B <-> A, the result copied back into A.
+    const Lattice Lp = padded(L);
+    const bool pad = Lp.px != L.dims[0];
+    float* src = pad ? P<float>(w.B) : P<float>(w.A);
+    float* dst = pad ? P<float>(w.A) : P<float>(w.B);
+    if (pad) launch_pad_rows(P<float>(w.A), P<float>(w.B), Lp, st);
+    // TMA descriptors of the two grid copies for the staged sweeps
     GridMap map_a, map_b;
-    encode_grid_map(map_a, P<float>(w.A), L);
-    encode_grid_map(map_b, P<float>(w.B), L);
+    encode_grid_map(map_a, P<float>(w.A), Lp);
+    encode_grid_map(map_b, P<float>(w.B), Lp);
     auto map_of = [&](const float* p) { return p == P<float>(w.A) ? &map_a : &map_b; };
     // sweep_schedule: 0 autotuned; else x schedule + 10 x walk schedule (a 0 digit: tuned).
     // The first round and the later ones have their own tuned plans (phase 0 / 1).
@@ -400,7 +408,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     const bool tune = xs_opt == 0 || ws_opt == 0;
     SweepPlan plan;
     auto set_plan = [&](int phase) -> int {
-        plan = tuned_sweep_plan(w.device, L, src, dst, map_of(src), w.ds, st, tune, phase);
+        plan = tuned_sweep_plan(w.device, Lp, src, dst, map_of(src), w.ds, st, tune, phase);
         if (xs_opt >= kXCpAsync && xs_opt <= kXTmaWide) plan.x = xs_opt;
         if (ws_opt >= kWCpAsync && ws_opt <= kWTmaVec2) plan.w = ws_opt;
         GB_CK(cudaGetLastError());
@@ -413,7 +421,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
                 if (int rcp = set_plan(1)) return rcp;
             for (int axis = 0; axis < 3; ++axis)
                 for (int dir = 1; dir >= -1; dir -= 2) {
-                    launch_sweep(rule, axis, dir, r, src, dst, L, w.ds, st, map_of(src), plan.x, plan.w);
+                    launch_sweep(rule, axis, dir, r, src, dst, Lp, w.ds, st, map_of(src), plan.x, plan.w);
                     std::swap(src, dst);
                 }
             launch_end_round(r, r, kMaxRounds, w.ds, st);
@@ -428,7 +436,8 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
                 GB_CK(cudaMemsetAsync(&w.ds->changed[r % 64], 0, sizeof(int), st));
                 for (int axis = 0; axis < 3; ++axis)
                     for (int dir = 1; dir >= -1; dir -= 2) {
-                        launch_sweep(rule, axis, dir, r % 64, src, dst, L, w.ds, st, map_of(src), plan.x, plan.w);
+                        launch_sweep(rule, axis, dir, r % 64, src, dst, Lp, w.ds, st, map_of(src), plan.x,
+                                     plan.w);
                         std::swap(src, dst);
                     }
                 launch_end_round(r % 64, r, cap, w.ds, st);
@@ -438,7 +447,8 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
             if (w.hs->stop) break;
         }
     }
-    // rounds are whole (6 sweeps, an even number), so the field is back in A
+    // rounds are whole (6 sweeps, an even number), so the field is back in the first source
+    if (pad) launch_unpad_rows(P<float>(w.B), P<float>(w.A), Lp, st);
     launch_audit(P<float>(w.A), L, w.ds, st);
     launch_clamp(P<float>(w.A), P<uint32_t>(w.S), L, w.ds, st);
     GB_CK(cudaGetLastError());

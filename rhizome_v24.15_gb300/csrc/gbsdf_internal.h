@@ -21,7 +21,18 @@ struct Lattice {
     long long nbricks;
     int nsx;            // parity strips per row: ceil(dims[0] / kStrip)
     long long nstrips;  // nsx * dims[1]
+    int px;             // row pitch (floats) of the distance grid the eikonal sweeps address:
+                        // dims[0], or dims[0] rounded up to 4 in the sweeps' padded copies
 };
+
+// The lattice as the eikonal sweeps see their padded grid copies: rows of a multiple of 4
+// floats (16 bytes, what a TMA descriptor needs); the pad columns are never lattice voxels.
+inline Lattice padded(const Lattice& L) {
+    Lattice P = L;
+    P.px = (L.dims[0] + 3) & ~3;
+    return P;
+}
+inline long long padded_voxels(const Lattice& L) { return (long long)((L.dims[0] + 3) & ~3) * L.dims[1] * L.dims[2]; }
 
 // Per-triangle record of the band splat (96 bytes): vertices, AABB, the
 // reference's clamped XY footprint and a conservative z range.
@@ -247,7 +258,10 @@ struct GridMap {
     bool walk_valid;
     bool wide_valid;
 };
-bool encode_grid_map(GridMap& m, const float* base, const Lattice& L);
+bool encode_grid_map(GridMap& m, const float* base, const Lattice& L);  // rows L.px floats apart
+// The eikonal's padded grid copy: `P` = padded(L); pad writes every element of the copy.
+void launch_pad_rows(const float* dense, float* pad, const Lattice& P, cudaStream_t st);
+void launch_unpad_rows(const float* pad, float* dense, const Lattice& P, cudaStream_t st);
 // Schedules of the x sweep (all give identical results): staged by per-thread cp.async
 // copies, by TMA tiles on a CTA-barrier ring, by TMA tiles on a warp-specialised mbarrier
 // pipeline, the same pipeline with two lines per thread updated in packed FP32 pairs (the

@@ -70,11 +70,11 @@ __global__ void __launch_bounds__(kWThreads) sweep_walk_kernel(const float* __re
     if (ds->stop) return;
     extern __shared__ float ring[];
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
-    const size_t plane = (size_t)dx * dy;
+    const size_t plane = (size_t)L.px * dy;
     const int n_walk = (AXIS == 2) ? dz : dy;
     const int n_rows = (AXIS == 2) ? dy : dz;
-    const size_t step_stride = (AXIS == 2) ? plane : (size_t)dx;
-    const size_t row_stride = (AXIS == 2) ? (size_t)dx : plane;
+    const size_t step_stride = (AXIS == 2) ? plane : (size_t)L.px;
+    const size_t row_stride = (AXIS == 2) ? (size_t)L.px : plane;
     const int tid = threadIdx.x, tx = tid & 31, tr = tid >> 5;
     const int x0 = blockIdx.x * kWX, r0 = blockIdx.y * kWR;
     const int x = x0 + tx;
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_kernel(const float* __restr
     extern __shared__ float xring[];
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
     const float h = L.h;
-    const size_t plane = (size_t)dx * dy;
+    const size_t plane = (size_t)L.px * dy;
     const int tid = threadIdx.x;
     const int ty = tid & 31, tz = tid >> 5;
     const int y0 = blockIdx.x * kXY, z0 = blockIdx.y * kXZ;
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_kernel(const float* __restr
     const int jcopy = tid & 7;
     long long loff[kXPer];    // line start relative to the CTA's first (halo) line
     unsigned lok = 0u, lexist = 0u;
-    const long long cta_base = (long long)(z0 - 1) * (long long)plane + (long long)(y0 - 1) * dx;
+    const long long cta_base = (long long)(z0 - 1) * (long long)plane + (long long)(y0 - 1) * L.px;
 #pragma unroll
     for (int k = 0; k < kXPer; ++k) {
         const int ln = (tid >> 3) + 32 * k;
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_kernel(const float* __restr
         const int yy = y0 - 1 + hy, zz = z0 - 1 + hz;
         const bool ex = ln < kXLines;
         const bool ok = ex && yy >= 0 && yy < dy && zz >= 0 && zz < dz;
-        loff[k] = ok ? ((long long)zz * (long long)plane + (long long)yy * dx - cta_base) : 0;
+        loff[k] = ok ? ((long long)zz * (long long)plane + (long long)yy * L.px - cta_base) : 0;
         lok |= (ok ? 1u : 0u) << k;
         lexist |= (ex ? 1u : 0u) << k;
     }
@@ -306,8 +306,8 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_kernel(const float* __restr
                     prev = out;
                 }
             }
-            float* drow = dst + (size_t)z * plane + (size_t)y * dx + xc;
-            if (((dx & 3) == 0) && xc + kXC <= dx) {
+            float* drow = dst + (size_t)z * plane + (size_t)y * L.px + xc;
+            if (((L.px & 3) == 0) && xc + kXC <= dx) {
                 reinterpret_cast<float4*>(drow)[0] = make_float4(res[0], res[1], res[2], res[3]);
                 reinterpret_cast<float4*>(drow)[1] = make_float4(res[4], res[5], res[6], res[7]);
             } else {
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_tma_kernel(const __grid_con
     __shared__ int s_ok;
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
     const float h = L.h;
-    const size_t plane = (size_t)dx * dy;
+    const size_t plane = (size_t)L.px * dy;
     const int tid = threadIdx.x, ty = tid & 31, tz = tid >> 5;
     const int y0 = blockIdx.x * kXY, z0 = blockIdx.y * kXZ;
     const int y = y0 + ty, z = z0 + tz;
@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_tma_kernel(const __grid_con
                 prev = out;
             }
         }
-        float* drow = dst + (size_t)z * plane + (size_t)y * dx + xc;
+        float* drow = dst + (size_t)z * plane + (size_t)y * L.px + xc;
         if (xc + kXC <= dx) {
             reinterpret_cast<float4*>(drow)[0] = make_float4(res[0], res[1], res[2], res[3]);
             reinterpret_cast<float4*>(drow)[1] = make_float4(res[4], res[5], res[6], res[7]);
@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
     const float h = L.h;
     const float m2h = -2.0f * h, na3 = -(3.0f * h * h);
-    const size_t plane = (size_t)dx * dy;
+    const size_t plane = (size_t)L.px * dy;
     const int tid = threadIdx.x;
     const int y0 = blockIdx.x * kXY, z0 = blockIdx.y * kXZ;
     const int nchunks = (dx + kXC - 1) / kXC;
@@ -655,7 +655,7 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
                     prev = out;
                 }
             }
-            float* drow = dst + (size_t)z * plane + (size_t)y * dx + xc;
+            float* drow = dst + (size_t)z * plane + (size_t)y * L.px + xc;
             if (xc + kXC <= dx) {
                 reinterpret_cast<float4*>(drow)[0] = make_float4(res[0], res[1], res[2], res[3]);
                 reinterpret_cast<float4*>(drow)[1] = make_float4(res[4], res[5], res[6], res[7]);
@@ -694,7 +694,7 @@ __global__ void __launch_bounds__(kP2Threads, 4) sweep_x_pipe2_kernel(const __gr
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kPS * kTSlotBytes);
     uint64_t* empty = full + kPS;
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
-    const size_t plane = (size_t)dx * dy;
+    const size_t plane = (size_t)L.px * dy;
     const int tid = threadIdx.x;
     const int y0 = blockIdx.x * kXY, z0 = blockIdx.y * kXZ;
     const int nchunks = (dx + kXC - 1) / kXC;
@@ -748,8 +748,8 @@ __global__ void __launch_bounds__(kP2Threads, 4) sweep_x_pipe2_kernel(const __gr
             // both lines' chunks are whole (line b may be outside the lattice: it then
             // reads the NaN fill and its results are not stored). The chunk is walked in
             // two 4-voxel halves, so only one half's operands are live at a time.
-            float* da = dst + (size_t)za * plane + (size_t)y * dx + xc;
-            float* db = dst + (size_t)zb * plane + (size_t)y * dx + xc;
+            float* da = dst + (size_t)za * plane + (size_t)y * L.px + xc;
+            float* db = dst + (size_t)zb * plane + (size_t)y * L.px + xc;
             const float nxta = (DIR > 0) ? ntile[tsw(rma, 0)] : ntile[tsw(rma, kXC - 1)];
             const float nxtb = (DIR > 0) ? ntile[tsw(rmb, 0)] : ntile[tsw(rmb, kXC - 1)];
             float4 ma = tvec(tile, rma, (DIR > 0) ? 0 : 1), mb = tvec(tile, rmb, (DIR > 0) ? 0 : 1);
@@ -824,7 +824,7 @@ __global__ void __launch_bounds__(kP2Threads, 4) sweep_x_pipe2_kernel(const __gr
                     res[j] = out;
                     prev = out;
                 }
-                float* drow = dst + (size_t)z * plane + (size_t)y * dx + xc;
+                float* drow = dst + (size_t)z * plane + (size_t)y * L.px + xc;
                 if (xc + kXC <= dx) {
                     reinterpret_cast<float4*>(drow)[0] = make_float4(res[0], res[1], res[2], res[3]);
                     reinterpret_cast<float4*>(drow)[1] = make_float4(res[4], res[5], res[6], res[7]);
@@ -873,7 +873,7 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_wide_kernel(const __grid_co
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
     const float h = L.h;
     const float m2h = -2.0f * h, na3 = -(3.0f * h * h);
-    const size_t plane = (size_t)dx * dy;
+    const size_t plane = (size_t)L.px * dy;
     const int tid = threadIdx.x;
     const int y0 = blockIdx.x * kXY, z0 = blockIdx.y * kXZ;
     const int nchunks = (dx + kXW - 1) / kXW;
@@ -923,7 +923,7 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_wide_kernel(const __grid_co
             const float* yh = tile + (rme + 1) * kXWB + cb;
             const float* zl = tile + (rme - kXHY) * kXWB + cb;
             const float* zh = tile + (rme + kXHY) * kXWB + cb;
-            float* drow = dst + (size_t)z * plane + (size_t)y * dx + xc;
+            float* drow = dst + (size_t)z * plane + (size_t)y * L.px + xc;
             if (xc + kXW <= dx) {
 #pragma unroll
                 for (int qq = 0; qq < 4; ++qq) {
@@ -1010,11 +1010,11 @@ __global__ void __launch_bounds__(kWPThreads) sweep_walk_pipe_kernel(const __gri
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kWPS * kWPSlotBytes);
     uint64_t* empty = full + kWPS;
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
-    const size_t plane = (size_t)dx * dy;
+    const size_t plane = (size_t)L.px * dy;
     const int n_walk = (AXIS == 2) ? dz : dy;
     const int n_rows = (AXIS == 2) ? dy : dz;
-    const size_t step_stride = (AXIS == 2) ? plane : (size_t)dx;
-    const size_t row_stride = (AXIS == 2) ? (size_t)dx : plane;
+    const size_t step_stride = (AXIS == 2) ? plane : (size_t)L.px;
+    const size_t row_stride = (AXIS == 2) ? (size_t)L.px : plane;
     // shared-memory strides of a batch: box order is (x, y, z), x fastest
     constexpr int kSliceS = (AXIS == 2) ? kWHR * kWPX : kWPX;   // next slice
     constexpr int kRowS = (AXIS == 2) ? kWPX : kWPB * kWPX;     // next row
@@ -1148,11 +1148,11 @@ __global__ void __launch_bounds__(kWVThreads) sweep_walk_vec_kernel(const __grid
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kWVS * kWPSlotBytes);
     uint64_t* empty = full + kWVS;
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
-    const size_t plane = (size_t)dx * dy;
+    const size_t plane = (size_t)L.px * dy;
     const int n_walk = (AXIS == 2) ? dz : dy;
     const int n_rows = (AXIS == 2) ? dy : dz;
-    const size_t step_stride = (AXIS == 2) ? plane : (size_t)dx;
-    const size_t row_stride = (AXIS == 2) ? (size_t)dx : plane;
+    const size_t step_stride = (AXIS == 2) ? plane : (size_t)L.px;
+    const size_t row_stride = (AXIS == 2) ? (size_t)L.px : plane;
     constexpr int kSliceS = (AXIS == 2) ? kWHR * kWPX : kWPX;
     constexpr int kRowS = (AXIS == 2) ? kWPX : kWPB * kWPX;
     const int tid = threadIdx.x;
@@ -1272,11 +1272,11 @@ __global__ void __launch_bounds__(kWVThreads) sweep_walk_vec2_kernel(const __gri
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + kWVS * kWPSlotBytes);
     uint64_t* empty = full + kWVS;
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
-    const size_t plane = (size_t)dx * dy;
+    const size_t plane = (size_t)L.px * dy;
     const int n_walk = (AXIS == 2) ? dz : dy;
     const int n_rows = (AXIS == 2) ? dy : dz;
-    const size_t step_stride = (AXIS == 2) ? plane : (size_t)dx;
-    const size_t row_stride = (AXIS == 2) ? (size_t)dx : plane;
+    const size_t step_stride = (AXIS == 2) ? plane : (size_t)L.px;
+    const size_t row_stride = (AXIS == 2) ? (size_t)L.px : plane;
     constexpr int kSliceS = (AXIS == 2) ? kWHR * kWPX : kWPX;
     constexpr int kRowS = (AXIS == 2) ? kWPX : kWPB * kWPX;
     const int tid = threadIdx.x;
@@ -1622,12 +1622,13 @@ EncodeTiledFn tiled_encoder() {
     return fn;
 }
 
-bool encode_box(CUtensorMap* m, const float* base, int dx, int dy, int dz, int bx = kXC, int by = kXHY,
+// A 3D tiled descriptor of a grid of dx x dy x dz voxels whose rows are px floats apart.
+bool encode_box(CUtensorMap* m, const float* base, int dx, int dy, int dz, int px, int bx = kXC, int by = kXHY,
                 int bz = kXHZ, CUtensorMapSwizzle sw = CU_TENSOR_MAP_SWIZZLE_32B) {
     EncodeTiledFn fn = tiled_encoder();
     if (!fn) return false;
     const cuuint64_t gdim[3] = {(cuuint64_t)dx, (cuuint64_t)dy, (cuuint64_t)dz};
-    const cuuint64_t gstride[2] = {(cuuint64_t)dx * 4, (cuuint64_t)dx * dy * 4};
+    const cuuint64_t gstride[2] = {(cuuint64_t)px * 4, (cuuint64_t)px * dy * 4};
     const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
     const cuuint32_t estr[3] = {1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), gdim, gstride, box, estr,
@@ -1642,14 +1643,13 @@ bool encode_grid_map(GridMap& m, const float* base, const Lattice& L) {
     m.walk_valid = false;
     m.wide_valid = false;
     // row and plane pitches must be multiples of 16 bytes, the base 16-byte aligned
-    if ((L.dims[0] & 3) != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
-    m.valid = encode_box(&m.map, base, L.dims[0], L.dims[1], L.dims[2]);
+    if ((L.px & 3) != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
+    const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
+    m.valid = encode_box(&m.map, base, dx, dy, dz, L.px);
     m.walk_valid = m.valid &&
-                   encode_box(&m.ymap, base, L.dims[0], L.dims[1], L.dims[2], kWPX, kWPB, kWHR,
-                              CU_TENSOR_MAP_SWIZZLE_NONE) &&
-                   encode_box(&m.zmap, base, L.dims[0], L.dims[1], L.dims[2], kWPX, kWHR, kWPB,
-                              CU_TENSOR_MAP_SWIZZLE_NONE);
-    m.wide_valid = m.valid && encode_box(&m.wmap, base, L.dims[0], L.dims[1], L.dims[2], kXWB, kXHY, kXHZ,
+                   encode_box(&m.ymap, base, dx, dy, dz, L.px, kWPX, kWPB, kWHR, CU_TENSOR_MAP_SWIZZLE_NONE) &&
+                   encode_box(&m.zmap, base, dx, dy, dz, L.px, kWPX, kWHR, kWPB, CU_TENSOR_MAP_SWIZZLE_NONE);
+    m.wide_valid = m.valid && encode_box(&m.wmap, base, dx, dy, dz, L.px, kXWB, kXHY, kXHZ,
                                          CU_TENSOR_MAP_SWIZZLE_NONE);
     return m.valid;
 }
@@ -1674,7 +1674,8 @@ int selftest_tma_tile(unsigned long long* mism_dev) {
     if (cudaMalloc(&g, n * 4) != cudaSuccess) return 1;
     int rc = 0;
     CUtensorMap m;
-    if (cudaMemcpy(g, hv.data(), n * 4, cudaMemcpyHostToDevice) != cudaSuccess || !encode_box(&m, g, dx, dy, dz)) {
+    if (cudaMemcpy(g, hv.data(), n * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        !encode_box(&m, g, dx, dy, dz, dx)) {
         rc = 1;
     } else {
         const int pts[5][3] = {{0, -1, -1}, {8, 5, 3}, {40, 31, 7}, {16, 10, 0}, {32, -1, 12}};
@@ -1686,6 +1687,38 @@ int selftest_tma_tile(unsigned long long* mism_dev) {
     cudaGetLastError();
     cudaFree(g);
     return rc;
+}
+
+namespace {
+// Dense x-fastest grid (rows of dims[0]) <-> the sweeps' padded copy (rows of px floats;
+// pad columns written as 0, never read as voxels). One thread per padded / dense element.
+__global__ void pad_rows_kernel(const float* __restrict__ dense, float* __restrict__ pad, Lattice L) {
+    const long long n = (long long)L.px * L.dims[1] * L.dims[2];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const long long row = i / L.px;
+        const int x = (int)(i - row * L.px);
+        pad[i] = (x < L.dims[0]) ? dense[row * L.dims[0] + x] : 0.0f;
+    }
+}
+__global__ void unpad_rows_kernel(const float* __restrict__ pad, float* __restrict__ dense, Lattice L) {
+    const long long n = L.N;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const long long row = i / L.dims[0];
+        dense[i] = pad[row * L.px + (i - row * L.dims[0])];
+    }
+}
+}  // namespace
+
+void launch_pad_rows(const float* dense, float* pad, const Lattice& P, cudaStream_t st) {
+    const long long n = (long long)P.px * P.dims[1] * P.dims[2];
+    GBSDF_COUNT_LAUNCH();
+    pad_rows_kernel<<<(unsigned)std::min<long long>((n + 255) / 256, 152LL * 16), 256, 0, st>>>(dense, pad, P);
+}
+void launch_unpad_rows(const float* pad, float* dense, const Lattice& P, cudaStream_t st) {
+    GBSDF_COUNT_LAUNCH();
+    unpad_rows_kernel<<<(unsigned)std::min<long long>((P.N + 255) / 256, 152LL * 16), 256, 0, st>>>(pad, dense, P);
 }
 
 void launch_end_round(int slot, int round, int cap, DevState* ds, cudaStream_t st) {

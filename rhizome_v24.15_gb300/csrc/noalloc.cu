@@ -301,6 +301,7 @@ extern "C" int gbsdf_legacy_sdf_noalloc(const gbsdf_tri* tris_dev, int64_t n_tri
     L.N = N;
     L.wx = (int)((dims[0] + 31) / 32);
     L.nwords = words;
+    L.px = L.dims[0];
     const float* t12 = reinterpret_cast<const float*>(tris_dev);
     const long long T = n_tris;
     const long long ntiles = (T + kNaTile - 1) / kNaTile;

@@ -27,7 +27,7 @@ std::mutex g_tune_mu;
 std::map<Key, SweepPlan> g_tuned;
 
 Key key_of(int device, const Lattice& L, int phase) {
-    return Key{device, (L.dims[0] & 3) == 0 ? 1 : 0, (int)std::lround(std::log2((double)L.N)),
+    return Key{device, (L.px & 3) == 0 ? 1 : 0, (int)std::lround(std::log2((double)L.N)),
                (int)std::lround(std::log2((double)L.dims[0])), phase};
 }
 
@@ -44,7 +44,7 @@ SweepPlan tuned_sweep_plan(int device, const Lattice& L, const float* src, float
         auto it = g_tuned.find(k);
         if (it != g_tuned.end()) return it->second;
     }
-    plan = SweepPlan{tma ? kXTmaPipe : kXCpAsync, wtma ? kWTmaPipe : kWCpAsync};
+    plan = SweepPlan{tma ? kXTmaPipe : kXCpAsync, wtma ? kWTmaVec2 : kWCpAsync};
     if (!measure) return plan;
     cudaEvent_t a, b;
     if (cudaEventCreate(&a) != cudaSuccess) {
