@@ -122,6 +122,16 @@ def make_workload(dims=None, h=None, name=WORKLOAD):
     return tris, mn, mx, h
 
 
+_X_SCHED = {1: "sweep_x_kernel", 2: "sweep_x_tma_kernel", 3: "sweep_x_pipe_kernel", 4: "sweep_x_pipe2_kernel",
+            5: "sweep_x_wide_kernel"}
+_W_SCHED = {1: "sweep_walk_kernel", 2: "sweep_walk_pipe_kernel", 3: "sweep_walk_vec_kernel", 4: "sweep_walk_vec2_kernel"}
+
+
+def _sweep_kernels(sched):
+    """Kernel names of a build's last-round sweep schedule (x + 10 w)."""
+    return f"{_X_SCHED.get(int(sched) % 10, '?')} (x) / {_W_SCHED.get(int(sched) // 10, '?')} (y, z)"
+
+
 def run_batched(gbsdf, torch, dev, mode, steps, warmup, local, mlp):
     """The 64-mesh batched workload: one planned batch (one CUDA graph per run) against
     64 sequential single-mesh calls, device-resident triangles and outputs, timed on the
@@ -513,7 +523,7 @@ def main():
                        "l2": "inputs larger than L2 (2.6 GB grid per step)"},
             "e2e": None if e2e is None else {"value": e2e, "unit": UNIT, "ms_per_step": e2e_ms,
                                              "h2d_bytes_per_step": int(T * 48), "d2h_bytes_per_step": int(N * 4)},
-            "roofline": {"kernel": "eikonal directional sweep (sweep_x_pipe / sweep_walk_vec, autotuned)",
+            "roofline": {"kernel": "eikonal directional sweeps, autotuned: " + _sweep_kernels(s0["sweep_schedule"]),
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "alg_bytes_per_launch": alg_bytes, "launch_ms": per_launch_ms,

@@ -239,7 +239,7 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
     launch_fwn_build(j.t9, T, L, j.fwn, j.ds, st);
     // [init] + [A]: one CTA per brick of the lattice, the surplus over the active count exits
     launch_fill(j.A, N, kFarSentinel, st);
-    launch_splat(j.stt, j.boff, j.bcount, j.blist, j.active, -1, L, j.A, j.ds, st);
+    launch_splat(j.stt, j.boff, j.bcount, j.blist, j.active, -1, -1, L, j.A, j.ds, st);
     launch_band_error(j.stt, j.boff, j.bcount, j.blist, L, j.A, j.ds, st);
     // [B]
     launch_parity(j.ptt, j.soff, j.scount, j.slist, L, j.S, j.U, j.ds, xs ? 1 : 0, st);

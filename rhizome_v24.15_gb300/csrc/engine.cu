@@ -346,6 +346,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     const long long brick_pairs = (long long)w.hs->brick_pairs;
     const long long strip_pairs = (long long)w.hs->strip_pairs;
     const long long n_active = (long long)w.hs->active_bricks;
+    const long long n_dense = (long long)w.hs->dense_bricks;
     GB_CK(ensure(w.blist, (size_t)std::max<long long>(brick_pairs, 1) * 4));
     GB_CK(ensure(w.slist, (size_t)std::max<long long>(strip_pairs, 1) * 4));
     Fwn fwn_s{};
@@ -364,7 +365,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     // ---- [init] + [A]
     launch_fill(P<float>(w.A), N, kFarSentinel, st);
     launch_splat(P<SplatTri>(w.stt), P<unsigned long long>(w.boff), P<unsigned>(w.bcount), P<unsigned>(w.blist),
-                 P<unsigned>(w.active), n_active, L, P<float>(w.A), w.ds, st);
+                 P<unsigned>(w.active), n_active, n_dense, L, P<float>(w.A), w.ds, st);
     launch_band_error(P<SplatTri>(w.stt), P<unsigned long long>(w.boff), P<unsigned>(w.bcount), P<unsigned>(w.blist), L,
                       P<float>(w.A), w.ds, st);
     GB_CK(cudaGetLastError());

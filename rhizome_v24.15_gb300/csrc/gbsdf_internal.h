@@ -62,6 +62,7 @@ struct DevState {
     unsigned long long csr_entries;    // entries of the reference's supercell CSR (guard)
     unsigned long long invalid_tris;   // non-finite or out-of-range coordinates
     unsigned long long active_bricks;
+    unsigned long long dense_bricks;   // bricks with more binned triangles than the dense-splat threshold
     unsigned long long band_voxels;
     unsigned long long splat_evals;    // exact point-triangle evaluations
     unsigned long long unknown_columns;
@@ -146,9 +147,11 @@ void launch_fill(float* g, long long n, float value, cudaStream_t st);
 constexpr long long kBandErrSamples = 16384;
 void launch_band_error(const SplatTri* stt, const unsigned long long* brick_off, const unsigned* brick_count,
                        const unsigned* brick_list, const Lattice& L, const float* dist, DevState* ds, cudaStream_t st);
+// n_active / n_dense: the sparse / dense brick counts (< 0: read on the device, one CTA per
+// brick of the lattice launched and the surplus exits).
 void launch_splat(const SplatTri* stt, const unsigned long long* brick_off, const unsigned* brick_count,
-                  const unsigned* brick_list, const unsigned* active, long long n_active, const Lattice& L,
-                  float* dist, DevState* ds, cudaStream_t st);
+                  const unsigned* brick_list, const unsigned* active, long long n_active, long long n_dense,
+                  const Lattice& L, float* dist, DevState* ds, cudaStream_t st);
 void launch_parity(const ParTri* ptt, const unsigned long long* strip_off, const unsigned* strip_count,
                    const unsigned* strip_list, const Lattice& L, uint32_t* sbits, uint32_t* ubits, DevState* ds,
                    int signed_crossings, cudaStream_t st);

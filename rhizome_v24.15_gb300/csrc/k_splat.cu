@@ -269,17 +269,30 @@ void scan_rec(const void* in, bool in_is_u64, unsigned long long* out, long long
     }
 }
 
+constexpr int kSplatThreads = 128;
+constexpr int kSplatChunk = 64;
+constexpr unsigned kSplatCullMin = 256;  // triangles binned to a brick before culling starts
+
+// The bricks with binned triangles: those with at most kSplatCullMin from the front of
+// `active` (ds->active_bricks of them, splat_kernel's), the others from the back
+// (ds->dense_bricks, splat_dense_kernel's).
 __global__ void active_bricks_kernel(const unsigned* __restrict__ cnt, long long nb, unsigned* __restrict__ active,
                                      DevState* ds) {
-    long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    bool a = (b < nb) && cnt[b] > 0;
-    unsigned m = __ballot_sync(0xffffffffu, a);
-    if (m == 0) return;
-    int lane = threadIdx.x & 31;
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(&ds->active_bricks, (unsigned long long)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (a) active[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)b;
+    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned n = (b < nb) ? cnt[b] : 0u;
+    const bool sparse = n > 0 && n <= kSplatCullMin, dense = n > kSplatCullMin;
+    const unsigned ms = __ballot_sync(0xffffffffu, sparse), md = __ballot_sync(0xffffffffu, dense);
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    unsigned long long bs = 0, bd = 0;
+    if (lane == 0) {
+        if (ms) bs = atomicAdd(&ds->active_bricks, (unsigned long long)__popc(ms));
+        if (md) bd = atomicAdd(&ds->dense_bricks, (unsigned long long)__popc(md));
+    }
+    bs = __shfl_sync(0xffffffffu, bs, 0);
+    bd = __shfl_sync(0xffffffffu, bd, 0);
+    if (sparse) active[bs + __popc(ms & below)] = (unsigned)b;
+    if (dense) active[nb - 1 - (long long)(bd + __popc(md & below))] = (unsigned)b;
 }
 
 __global__ void fill_kernel(float4* __restrict__ g4, long long n4, float value) {
@@ -292,9 +305,6 @@ __global__ void fill_tail_kernel(float* __restrict__ g, long long from, long lon
     if (i < n) g[i] = value;
 }
 
-constexpr int kSplatThreads = 128;
-constexpr int kSplatChunk = 64;
-constexpr unsigned kSplatCullMin = 256;  // triangles binned to a brick before culling starts
 
 // One staged triangle against one thread's K voxels (x, y, wz[k]). CULL: skip a triangle
 // whose bounding-box distance^2 exceeds the voxel's best exact distance^2 by more than both
@@ -351,10 +361,9 @@ __global__ void __launch_bounds__(kDenseThreads) splat_dense_kernel(
     DevState* ds) {
     __shared__ SplatTri s[kSplatChunk];
     __shared__ unsigned char keep_idx[kDenseThreads / 32][kSplatChunk];
-    if (blockIdx.x >= ds->active_bricks || ds->overflow) return;
-    const unsigned b = active[blockIdx.x];
+    if (blockIdx.x >= ds->dense_bricks || ds->overflow) return;
+    const unsigned b = active[L.nbricks - 1 - (long long)blockIdx.x];
     const unsigned n = cnt[b];
-    if (n <= kSplatCullMin) return;  // splat_kernel's brick
     const int nbx = L.nb[0], nby = L.nb[1];
     const int bx = (int)(b % (unsigned)nbx), by = (int)((b / (unsigned)nbx) % (unsigned)nby),
               bz = (int)(b / ((unsigned)nbx * (unsigned)nby));
@@ -628,16 +637,20 @@ void launch_band_error(const SplatTri* stt, const unsigned long long* brick_off,
 }
 
 void launch_splat(const SplatTri* stt, const unsigned long long* brick_off, const unsigned* brick_count,
-                  const unsigned* brick_list, const unsigned* active, long long n_active, const Lattice& L,
-                  float* dist, DevState* ds, cudaStream_t st) {
+                  const unsigned* brick_list, const unsigned* active, long long n_active, long long n_dense,
+                  const Lattice& L, float* dist, DevState* ds, cudaStream_t st) {
     const long long blocks = n_active < 0 ? L.nbricks : n_active;
-    if (blocks <= 0) return;
-    GBSDF_COUNT_LAUNCH();
-    splat_kernel<<<(unsigned)blocks, kSplatThreads, 0, st>>>(stt, brick_off, brick_count, brick_list, active, L,
-                                                             dist, ds);
-    GBSDF_COUNT_LAUNCH();
-    splat_dense_kernel<<<(unsigned)blocks, kDenseThreads, 0, st>>>(stt, brick_off, brick_count, brick_list, active,
-                                                                   L, dist, ds);
+    if (blocks > 0) {
+        GBSDF_COUNT_LAUNCH();
+        splat_kernel<<<(unsigned)blocks, kSplatThreads, 0, st>>>(stt, brick_off, brick_count, brick_list, active, L,
+                                                                 dist, ds);
+    }
+    const long long dblocks = n_dense < 0 ? L.nbricks : n_dense;
+    if (dblocks > 0) {
+        GBSDF_COUNT_LAUNCH();
+        splat_dense_kernel<<<(unsigned)dblocks, kDenseThreads, 0, st>>>(stt, brick_off, brick_count, brick_list,
+                                                                        active, L, dist, ds);
+    }
 }
 
 }  // namespace gbsdf
