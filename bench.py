@@ -122,6 +122,72 @@ def make_workload(dims=None, h=None, name=WORKLOAD):
     return tris, mn, mx, h
 
 
+def run_learned_report(gbsdf, torch, dev, mlp):
+    """Learned proposals on the two defective workloads -- the 512^3 vessel tree (holes,
+    jitter, duplicated vertices) and the 1024^3 spherical-harmonic blob (1% holes) -- with
+    exact-signs mode's grid as the sign truth (it equals the FP64 winding number off the
+    surface). Per workload: plain (reference) mode; learned mode with no brick proposed
+    (every score -inf: the plain signs through the learned pipeline); learned mode with
+    the shipped network. `recall` = the share of the no-proposal run's sign errors (voxels
+    more than 1e-3 voxel off the surface) that the proposals fix; `exact_decisions` = voxels
+    the exact winding kernel decided (columns through holes, patch boxes, proposed bricks),
+    against the lattice's voxel count; times are host wall-clock per build (device-resident
+    buffers, one warm-up build first)."""
+    from gbsdf import learn, meshgen
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, (time.perf_counter() - t0) * 1e3
+
+    rep = {}
+    for name in ("vessel_c3_512", "blob_c5_1024"):
+        tris, mn, mx, h = meshgen.workload(name)
+        dims = mx.astype(np.int64) - mn + 1
+        n = int(np.prod(dims))
+        td = torch.from_numpy(tris).to(dev)
+        truth = torch.empty(n, dtype=torch.float32, device=dev)
+        out = torch.empty_like(truth)
+        off = None
+
+        def run(buf, **kw):
+            return gbsdf.compute_mesh_sdf(td, h, mn, mx, out=buf, path=gbsdf.PATH_FAST, raise_on_error=False, **kw)[1]
+
+        def errors():
+            return int(((torch.signbit(out) != torch.signbit(truth)) & off).sum().item())
+
+        rt, tt = timed(lambda: run(truth, mode=gbsdf.MODE_EXACT_SIGNS))
+        off = truth.abs() > 1e-3 * h
+        rp, tp = timed(lambda: run(out, mode=gbsdf.MODE_REFERENCE))
+        plain = {"status": rp.status, "ms": tp}
+        if rp.ok:
+            plain["sign_errors"] = errors()
+            plain["exact_decisions"] = int(rp.stats["fixup_voxels"] + rp.stats["patched_voxels"])
+        low = torch.full((int(np.prod(learn.brick_grid(mn, mx))),), -1e30, dtype=torch.float32, device=dev)
+        r0, t0 = timed(lambda: run(out, mode=gbsdf.MODE_LEARNED, brick_scores=low))
+        e0 = errors() if r0.ok else None
+        rl, tl = timed(lambda: run(out, mode=gbsdf.MODE_LEARNED, mlp_params=mlp))
+        el = errors() if rl.ok else None
+        decided = int(rl.stats["fixup_voxels"] + rl.stats["patched_voxels"] + rl.stats["proposed"] * 512)
+        rep[name] = {
+            "voxels": n, "triangles": int(len(tris)),
+            "exact_signs": {"ms": tt, "exact_decisions": int(rt.stats["fixup_voxels"] + rt.stats["patched_voxels"])},
+            "plain": plain,
+            "learned_no_proposals": {"status": r0.status, "ms": t0, "sign_errors": e0,
+                                     "escalated": int(r0.stats["escalated"])},
+            "learned": {"status": rl.status, "ms": tl, "sign_errors": el, "escalated": int(rl.stats["escalated"]),
+                        "proposed_bricks": int(rl.stats["proposed"]), "exact_decisions": decided,
+                        "exact_decisions_saved": 1.0 - decided / n,
+                        "recall": (None if not e0 or el is None else (e0 - el) / e0)},
+        }
+        del truth, out, td, low
+        torch.cuda.empty_cache()
+    return rep
+
+
 _X_SCHED = {1: "sweep_x_kernel", 2: "sweep_x_tma_kernel", 3: "sweep_x_pipe_kernel", 4: "sweep_x_pipe2_kernel",
             5: "sweep_x_wide_kernel"}
 _W_SCHED = {1: "sweep_walk_kernel", 2: "sweep_walk_pipe_kernel", 3: "sweep_walk_vec_kernel", 4: "sweep_walk_vec2_kernel"}
@@ -548,6 +614,8 @@ def main():
         line["iso_surface"] = run_iso(gbsdf, out_dev, dims, h, mn, args.steps)
     if not args.no_batch and mode in (gbsdf.MODE_REFERENCE, gbsdf.MODE_EXACT_SIGNS):
         line["batched"] = run_batched(gbsdf, torch, dev, mode, args.steps, args.warmup, local, mlp)
+    if rank == 0 and world == 1 and not args.no_batch and args.workload == WORKLOAD:
+        line["learned_report"] = run_learned_report(gbsdf, torch, dev, mlp)
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == WORKLOAD:
         line["reference_gpu"] = run_reference_gpu(tris, mn, mx, h)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -114,9 +114,10 @@ def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE
     on the host when None. ``MODE_LEARNED`` takes the sign-risk model's parameters
     (``mlp_params``; the shipped model when None), the most bricks it may propose and the
     probability threshold; ``brick_scores`` (one logit per 8^3 brick, x fastest) replaces
-    the network's scores. ``sweep_schedule``: x + 10 w, x (1-3) a fixed x-sweep schedule and
-    w (1-3) a fixed y / z walk schedule, a 0 digit autotuned (identical results). ``host_output``: 0 lets a page-locked host output be written
-    directly by the sign-apply kernel, 1 stages it in device memory and copies.
+    the network's scores. ``sweep_schedule``: x + 10 w, x (1-5) a fixed x-sweep schedule and
+    w (1-4) a fixed y / z walk schedule, a 0 digit autotuned (identical results).
+    ``host_output``: 0 lets a page-locked host output be written directly by the sign-apply
+    kernel, 1 stages it in device memory and copies.
     ``winding_eval``: 0 clustered exact winding decisions, 1 triangle-by-triangle sums.
     ``wait_poll_limit``: the eikonal's staged-tile waits (0 default; < 0 gives up at once,
     which exercises the failure path). Returns ``(out, Result)``."""
