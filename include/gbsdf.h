@@ -128,7 +128,10 @@ typedef struct gbsdf_options {
     int32_t winding_eval;   /* exact winding decisions: 0 = clustered (far clusters by a dipole
                                with a rigorous error bound, undecided voxels summed exactly;
                                same decisions), 1 = every voxel summed triangle by triangle */
-    int32_t reserved;
+    int32_t splat_dense_cut; /* binned triangles per 8^3 brick above which the band splat takes the
+                                brick with its sub-brick kernel: 0 = autotuned per lattice class
+                                (gbsdf_stats.splat_dense_cut reports it), > 0 = that cut.
+                                Identical results at every cut. */
 } gbsdf_options;
 
 /* Learned sign-risk model: parameter count and brick feature count. */
@@ -145,7 +148,8 @@ typedef struct gbsdf_stats {
     int32_t probes;
     int32_t sites;
     int32_t patch_rounds;
-    int32_t pad0;
+    int32_t splat_dense_cut; /* binned triangles per 8^3 brick above which the band splat takes the
+                                brick with its sub-brick kernel (autotuned per lattice class) */
     int64_t unknown_columns;
     int64_t fixup_voxels;
     int64_t far_residual;

@@ -71,6 +71,7 @@ struct Job {
     float* out = nullptr;
     Lattice L{};
     int pre_status = GBSDF_OK;  // argument checks (the mesh is left out of the graph)
+    unsigned dense_cut = kDenseCutDefault;  // the splat's tile cut: the class's tuned value if timed
     // device buffers (offsets into the arenas)
     float *A = nullptr, *B = nullptr, *t12 = nullptr, *t9 = nullptr;
     uint32_t *S = nullptr, *U = nullptr;
@@ -123,6 +124,7 @@ struct gbsdf_batch {
     int mode = GBSDF_MODE_REFERENCE;
     int num_sms = 0;
     int sweep_schedule = 0;
+    int dense_cut = 0;  // gbsdf_options.splat_dense_cut
     bool out_dev = false;
     bool tris_dev = false;
     std::vector<gbsdf::Job> jobs;
@@ -223,7 +225,7 @@ void enqueue_counts(gbsdf_batch& b, Job& j, cudaStream_t st) {
     launch_prep(j.t12, T, L, j.stt, j.ptt, j.bcount, j.scount, j.ds, st);
     launch_exclusive_scan(j.bcount, j.boff, L.nbricks, j.scan, 0, st);
     launch_exclusive_scan(j.scount, j.soff, L.nstrips, j.scan, 0, st);
-    launch_active_bricks(j.bcount, L.nbricks, j.active, j.ds, st);
+    launch_active_bricks(j.bcount, L.nbricks, j.active, j.ds, st, j.dense_cut);
     launch_pack_tri9(j.t12, T, j.t9, st);
 }
 
@@ -353,6 +355,8 @@ int plan(gbsdf_batch& b, BErr& e) {
             const SweepPlan plan1 = tuned_sweep_plan(b.device, Lp, j.A, j.B, &j.map_a, j.ds, b.origin, false, 1);
             j.xsched = plan.x;
             j.wsched = plan.w;
+            if (const unsigned cut = b.dense_cut > 0 ? (unsigned)b.dense_cut : tuned_dense_cut(b.device, j.L, j.T))
+                j.dense_cut = cut;
             j.xsched1 = plan1.x;
             j.wsched1 = plan1.w;
             const int xs_opt = b.sweep_schedule % 10, ws_opt = b.sweep_schedule / 10;
@@ -456,6 +460,7 @@ void fill_stats(const Job& j, int status, float ms, unsigned long long launches,
     s->probes = h.probes;
     s->sites = h.total_sites;
     s->patch_rounds = h.patch_rounds;
+    s->splat_dense_cut = (int32_t)j.dense_cut;
     s->unknown_columns = (long long)h.unknown_columns;
     s->fixup_voxels = (long long)h.fixup_voxels;
     s->patched_voxels = (long long)h.patched_voxels;
@@ -564,6 +569,7 @@ int gbsdf_batch_create(const gbsdf_mesh_desc* meshes, int32_t n_meshes, int32_t 
     b->device = o.device;
     b->mode = o.mode;
     b->sweep_schedule = o.sweep_schedule;
+    b->dense_cut = o.splat_dense_cut;
     if (o.mode == GBSDF_MODE_LEARNED) {
         const float pthr = (o.mlp_threshold > 0.0f && o.mlp_threshold < 1.0f) ? o.mlp_threshold : 0.5f;
         b->mlp_params = o.mlp_params;

@@ -331,7 +331,10 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
                           P<unsigned long long>(w.scan), 0, st);
     launch_exclusive_scan(P<unsigned>(w.scount), P<unsigned long long>(w.soff), L.nstrips,
                           P<unsigned long long>(w.scan), 0, st);
-    launch_active_bricks(P<unsigned>(w.bcount), L.nbricks, P<unsigned>(w.active), w.ds, st);
+    // the splat's tile cut: the class's tuned value, else the default (and timed below)
+    const unsigned cut_known = o.splat_dense_cut > 0 ? (unsigned)o.splat_dense_cut : tuned_dense_cut(w.device, L, T);
+    unsigned dense_cut = cut_known ? cut_known : kDenseCutDefault;
+    launch_active_bricks(P<unsigned>(w.bcount), L.nbricks, P<unsigned>(w.active), w.ds, st, dense_cut);
     launch_pack_tri9(P<float>(w.t12), T, P<float>(w.t9), st);
     GB_CK(cudaGetLastError());
     GB_CK(cudaMemcpyAsync(w.hs, w.ds, sizeof(DevState), cudaMemcpyDeviceToHost, st));
@@ -345,8 +348,8 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
                      (unsigned long long)w.hs->csr_entries);
     const long long brick_pairs = (long long)w.hs->brick_pairs;
     const long long strip_pairs = (long long)w.hs->strip_pairs;
-    const long long n_active = (long long)w.hs->active_bricks;
-    const long long n_dense = (long long)w.hs->dense_bricks;
+    long long n_active = (long long)w.hs->active_bricks;
+    long long n_dense = (long long)w.hs->dense_bricks;
     GB_CK(ensure(w.blist, (size_t)std::max<long long>(brick_pairs, 1) * 4));
     GB_CK(ensure(w.slist, (size_t)std::max<long long>(strip_pairs, 1) * 4));
     Fwn fwn_s{};
@@ -361,6 +364,43 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     launch_bin_fill(P<SplatTri>(w.stt), P<ParTri>(w.ptt), T, L, P<unsigned long long>(w.boff), P<unsigned>(w.bcur),
                     P<unsigned>(w.blist), P<unsigned long long>(w.soff), P<unsigned>(w.scur), P<unsigned>(w.slist),
                     st);
+    if (!cut_known && o.sweep_schedule == 0) {
+        // the class's first autotuned build: time the splat stage at each candidate cut on
+        // this build's own lists (identical results at every cut), keep the fastest
+        auto split = [&](unsigned cut) -> int {
+            GB_CK(cudaMemsetAsync(&w.ds->active_bricks, 0, 2 * sizeof(unsigned long long), st));
+            launch_active_bricks(P<unsigned>(w.bcount), L.nbricks, P<unsigned>(w.active), w.ds, st, cut);
+            GB_CK(cudaMemcpyAsync(&w.hs->active_bricks, &w.ds->active_bricks, 2 * sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToHost, st));
+            GB_CK(cudaStreamSynchronize(st));
+            n_active = (long long)w.hs->active_bricks;
+            n_dense = (long long)w.hs->dense_bricks;
+            return (int)GBSDF_OK;
+        };
+        float best_ms = 1e30f;
+        unsigned best = dense_cut;
+        for (unsigned cut : {128u, 256u, 512u, 1024u}) {
+            if (int rcs = split(cut)) return rcs;
+            launch_fill(P<float>(w.A), N, kFarSentinel, st);
+            GB_CK(cudaEventRecord(w.ev[10], st));  // events 10 and 11: the tuner's own
+            launch_splat(P<SplatTri>(w.stt), P<unsigned long long>(w.boff), P<unsigned>(w.bcount),
+                         P<unsigned>(w.blist), P<unsigned>(w.active), n_active, n_dense, L, P<float>(w.A), w.ds, st);
+            GB_CK(cudaEventRecord(w.ev[11], st));
+            GB_CK(cudaEventSynchronize(w.ev[11]));
+            float ms = 0.0f;
+            GB_CK(cudaEventElapsedTime(&ms, w.ev[10], w.ev[11]));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = cut;
+            }
+        }
+        set_tuned_dense_cut(w.device, L, T, best);
+        dense_cut = best;
+        if (int rcs = split(best)) return rcs;
+        // the timed splats counted into the build's statistics: start them again
+        GB_CK(cudaMemsetAsync(&w.ds->band_voxels, 0, sizeof(unsigned long long), st));
+        GB_CK(cudaMemsetAsync(&w.ds->splat_evals, 0, sizeof(unsigned long long), st));
+    }
     GB_CK(cudaEventRecord(w.ev[2], st));
     // ---- [init] + [A]
     launch_fill(P<float>(w.A), N, kFarSentinel, st);
@@ -564,6 +604,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         stats->probes = h.probes;
         stats->sites = h.total_sites;
         stats->patch_rounds = h.patch_rounds;
+        stats->splat_dense_cut = (int32_t)dense_cut;
         stats->unknown_columns = (long long)h.unknown_columns;
         stats->fixup_voxels = (long long)h.fixup_voxels;
         stats->patched_voxels = (long long)h.patched_voxels;

@@ -135,8 +135,15 @@ void launch_bin_fill(const SplatTri* stt, const ParTri* ptt, long long T, const 
                      const unsigned long long* strip_off, unsigned* strip_cur, unsigned* strip_list,
                      cudaStream_t st, DevState* ds = nullptr, unsigned long long cap_b = ~0ull,
                      unsigned long long cap_s = ~0ull);
+// The bricks with binned triangles: those with at most `dense_cut` from the front of
+// `active` (DevState::active_bricks), the others from the back (DevState::dense_bricks).
+constexpr unsigned kDenseCutDefault = 256;
 void launch_active_bricks(const unsigned* brick_count, long long nbricks, unsigned* active, DevState* ds,
-                          cudaStream_t st);
+                          cudaStream_t st, unsigned dense_cut);
+// The splat's tile cut of a lattice class (device, voxels, triangles; by octave): 0 when not
+// yet timed. The first fast-path build of a class times the candidates (engine.cu).
+unsigned tuned_dense_cut(int device, const Lattice& L, long long T);
+void set_tuned_dense_cut(int device, const Lattice& L, long long T, unsigned cut);
 void launch_fill(float* g, long long n, float value, cudaStream_t st);
 // n_active < 0: the active-brick count is read on the device (one CTA per brick of the
 // lattice is launched and the surplus exits), so the launch needs no host round trip.

@@ -271,16 +271,15 @@ void scan_rec(const void* in, bool in_is_u64, unsigned long long* out, long long
 
 constexpr int kSplatThreads = 128;
 constexpr int kSplatChunk = 64;
-constexpr unsigned kSplatCullMin = 256;  // triangles binned to a brick before culling starts
 
-// The bricks with binned triangles: those with at most kSplatCullMin from the front of
+// The bricks with binned triangles: those with at most `dense_cut` from the front of
 // `active` (ds->active_bricks of them, splat_kernel's), the others from the back
 // (ds->dense_bricks, splat_dense_kernel's).
 __global__ void active_bricks_kernel(const unsigned* __restrict__ cnt, long long nb, unsigned* __restrict__ active,
-                                     DevState* ds) {
+                                     DevState* ds, unsigned dense_cut) {
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned n = (b < nb) ? cnt[b] : 0u;
-    const bool sparse = n > 0 && n <= kSplatCullMin, dense = n > kSplatCullMin;
+    const bool sparse = n > 0 && n <= dense_cut, dense = n > dense_cut;
     const unsigned ms = __ballot_sync(0xffffffffu, sparse), md = __ballot_sync(0xffffffffu, dense);
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
@@ -342,7 +341,7 @@ __device__ __forceinline__ void splat_tri(const SplatTri& r, int x, int y, float
 }
 
 // ---- dense bricks: per-sub-brick triangle lists ----------------------------------------
-// A brick with more than kSplatCullMin binned triangles is split into its eight 4^3
+// A brick with more than the tile cut's binned triangles is split into its eight 4^3
 // sub-bricks, one warp each (a lane owns 2 voxels of one column). A first pass over the
 // brick's list finds the sub-brick centre's nearest triangle T*: every lattice point v of
 // the sub-brick has d(v, T*) <= d(centre, T*) + R (R the half-diagonal of the sub-brick's
@@ -488,9 +487,6 @@ __global__ void __launch_bounds__(kSplatThreads) splat_kernel(
     }
     const unsigned long long o = off[b];
     const unsigned n = cnt[b];
-    // bricks with many triangles are splat_dense_kernel's (culling pays there; with few
-    // triangles its tests cost more than the evaluations they save)
-    if (n > kSplatCullMin) return;
     unsigned evals = 0;
     for (unsigned c0 = 0; c0 < n; c0 += kSplatChunk) {
         unsigned m = min((unsigned)kSplatChunk, n - c0);
@@ -565,9 +561,10 @@ void launch_bin_fill(const SplatTri* stt, const ParTri* ptt, long long T, const 
 }
 
 void launch_active_bricks(const unsigned* brick_count, long long nbricks, unsigned* active, DevState* ds,
-                          cudaStream_t st) {
+                          cudaStream_t st, unsigned dense_cut) {
     GBSDF_COUNT_LAUNCH();
-    active_bricks_kernel<<<(unsigned)((nbricks + 255) / 256), 256, 0, st>>>(brick_count, nbricks, active, ds);
+    active_bricks_kernel<<<(unsigned)((nbricks + 255) / 256), 256, 0, st>>>(brick_count, nbricks, active, ds,
+                                                                            dense_cut);
 }
 
 void launch_fill(float* g, long long n, float value, cudaStream_t st) {

@@ -1,6 +1,6 @@
-// tune.cu — the sweep-schedule autotuner.
+// tune.cu — the autotuner: sweep schedules, and the band splat's tile cut per lattice class.
 //
-// The x sweep has four schedules and the y / z walks four, all with identical results
+// The x sweep has five schedules and the y / z walks four, all with identical results
 // (internal header, XSchedule / WSchedule). Which is fastest depends on the lattice (row
 // length, CTAs per wave), the device and the field: the first round sweeps a band in a far
 // field, where most updates are one-dimensional, later rounds a field where most warps
@@ -11,6 +11,12 @@
 // and remembers the winners per phase. A class is (device, row pitch a multiple of 16
 // bytes, round(log2 voxels), round(log2 row length)). Timing writes only the destination
 // copy, which the next sweep rewrites whole, and one change-flag slot.
+//
+// The band splat takes a brick either whole in one CTA (splat_kernel) or as eight 4^3
+// sub-bricks, one warp each, behind a per-sub-brick triangle bound (splat_dense_kernel);
+// the cut between them (binned triangles per brick) is tuned per class of (device,
+// round(log2 voxels), round(log2 triangles)) by the engine's first build of the class,
+// which times the splat stage at each candidate cut (same results at every cut).
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -32,6 +38,26 @@ Key key_of(int device, const Lattice& L, int phase) {
 }
 
 }  // namespace
+
+namespace {
+using CutKey = std::tuple<int, int, int>;
+std::map<CutKey, unsigned> g_cuts;
+CutKey cut_key(int device, const Lattice& L, long long T) {
+    return CutKey{device, (int)std::lround(std::log2((double)L.N)),
+                  (int)std::lround(std::log2((double)std::max(T, 1LL)))};
+}
+}  // namespace
+
+unsigned tuned_dense_cut(int device, const Lattice& L, long long T) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_cuts.find(cut_key(device, L, T));
+    return it == g_cuts.end() ? 0u : it->second;
+}
+
+void set_tuned_dense_cut(int device, const Lattice& L, long long T, unsigned cut) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_cuts[cut_key(device, L, T)] = cut;
+}
 
 SweepPlan tuned_sweep_plan(int device, const Lattice& L, const float* src, float* dst, const GridMap* src_map,
                            DevState* ds, cudaStream_t st, bool measure, int phase) {

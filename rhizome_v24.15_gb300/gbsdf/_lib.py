@@ -24,7 +24,7 @@ class Options(C.Structure):
                 ("max_rounds", C.c_int32), ("mlp_budget", C.c_int32), ("mlp_threshold", C.c_float),
                 ("wait_poll_limit", C.c_int32), ("mlp_params", C.c_void_p), ("brick_scores", C.c_void_p),
                 ("sweep_schedule", C.c_int32), ("host_output", C.c_int32),
-                ("winding_eval", C.c_int32), ("reserved", C.c_int32)]
+                ("winding_eval", C.c_int32), ("splat_dense_cut", C.c_int32)]
 
 
 MLP_PARAMS, MLP_FEATURES = 6337, 32
@@ -36,7 +36,7 @@ class Stats(C.Structure):
                 ("ms_fixup", C.c_float), ("ms_eikonal", C.c_float), ("ms_verify", C.c_float),
                 ("ms_apply", C.c_float), ("ms_d2h", C.c_float),
                 ("eikonal_rounds", C.c_int32), ("extra_rounds", C.c_int32), ("probes", C.c_int32),
-                ("sites", C.c_int32), ("patch_rounds", C.c_int32), ("pad0", C.c_int32),
+                ("sites", C.c_int32), ("patch_rounds", C.c_int32), ("splat_dense_cut", C.c_int32),
                 ("unknown_columns", C.c_int64), ("fixup_voxels", C.c_int64), ("far_residual", C.c_int64),
                 ("safe_clamped", C.c_int64), ("patched_voxels", C.c_int64), ("fp64_rechecks", C.c_int64),
                 ("band_voxels", C.c_int64), ("splat_evals", C.c_int64), ("gwn_pairs", C.c_int64),
@@ -46,7 +46,7 @@ class Stats(C.Structure):
                 ("band_err_samples", C.c_int64)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad0"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class MeshDesc(C.Structure):

@@ -108,7 +108,7 @@ def _set_learned(o, mode, device, mlp_params, mlp_budget, mlp_threshold, brick_s
 def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE_REFERENCE, path=PATH_AUTO,
                      device=0, max_rounds=0, raise_on_error=True, mlp_params=None, mlp_budget=None,
                      mlp_threshold=None, brick_scores=None, sweep_schedule=0, host_output=0, winding_eval=0,
-                     wait_poll_limit=0):
+                     wait_poll_limit=0, splat_dense_cut=0):
     """Run the engine. ``tris``: (T,12) float32 numpy array (host) or CUDA tensor.
     ``out``: float32 buffer of N voxels (numpy = host, CUDA tensor = device); allocated
     on the host when None. ``MODE_LEARNED`` takes the sign-risk model's parameters
@@ -119,6 +119,8 @@ def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE
     ``host_output``: 0 lets a page-locked host output be written directly by the sign-apply
     kernel, 1 stages it in device memory and copies.
     ``winding_eval``: 0 clustered exact winding decisions, 1 triangle-by-triangle sums.
+    ``splat_dense_cut``: binned triangles per brick above which the splat uses its sub-brick
+    kernel (0 = autotuned per lattice class; identical results at every cut).
     ``wait_poll_limit``: the eikonal's staged-tile waits (0 default; < 0 gives up at once,
     which exercises the failure path). Returns ``(out, Result)``."""
     mn = np.asarray(min_coord, np.int64).reshape(3)
@@ -139,6 +141,7 @@ def compute_mesh_sdf(tris, voxel_size, min_coord, max_coord, out=None, mode=MODE
     o.sweep_schedule = int(sweep_schedule)
     o.host_output = int(host_output)
     o.winding_eval = int(winding_eval)
+    o.splat_dense_cut = int(splat_dense_cut)
     o.wait_poll_limit = int(wait_poll_limit)
     keep = _set_learned(o, mode, device, mlp_params, mlp_budget, mlp_threshold, brick_scores)  # noqa: F841
     st = _lib.Stats()
