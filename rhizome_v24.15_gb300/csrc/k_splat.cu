@@ -353,112 +353,142 @@ __device__ __forceinline__ void splat_tri(const SplatTri& r, int x, int y, float
 // sparse kernel's, bit for bit; the screening work drops from 512 voxel tests per triangle
 // to 8 exact distances plus the survivors' tests.
 constexpr int kDenseThreads = 256;
+constexpr int kDenseSlices = 8;  // CTAs per dense brick, each on an eighth of its triangle list
 
+// One slice of one dense brick's list per CTA (grid: dense bricks x kDenseSlices, the
+// bricks visited grid-stride). The slice's own nearest triangle to each sub-brick centre
+// bounds the slice: a voxel's nearest triangle of the whole list is, within its slice,
+// nearer than any other, so it survives its slice's test, and the minimum over the slices
+// (an atomic minimum on the distance's bits, which order like unsigned integers for
+// non-negative floats) is the whole list's. The band voxels of these bricks are counted
+// afterwards by dense_count_kernel, once each.
 __global__ void __launch_bounds__(kDenseThreads) splat_dense_kernel(
     const SplatTri* __restrict__ stt, const unsigned long long* __restrict__ off, const unsigned* __restrict__ cnt,
     const unsigned* __restrict__ list, const unsigned* __restrict__ active, Lattice L, float* __restrict__ dist,
     DevState* ds) {
     __shared__ SplatTri s[kSplatChunk];
     __shared__ unsigned char keep_idx[kDenseThreads / 32][kSplatChunk];
-    if (blockIdx.x >= ds->dense_bricks || ds->overflow) return;
-    const unsigned b = active[L.nbricks - 1 - (long long)blockIdx.x];
-    const unsigned n = cnt[b];
+    if (ds->overflow) return;
+    const unsigned long long nd = ds->dense_bricks;
     const int nbx = L.nb[0], nby = L.nb[1];
-    const int bx = (int)(b % (unsigned)nbx), by = (int)((b / (unsigned)nbx) % (unsigned)nby),
-              bz = (int)(b / ((unsigned)nbx * (unsigned)nby));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int x0 = bx * kBrick + (warp & 1) * 4, y0 = by * kBrick + ((warp >> 1) & 1) * 4,
-              z0 = bz * kBrick + (warp >> 2) * 4;
-    const int x = x0 + (lane & 3), y = y0 + ((lane >> 2) & 3), zl = lane >> 4;
     const float h = L.h;
     const float bw = (float)kBandVoxels * h;
     const float band_sq = bw * bw;
-    const float px = (float)(L.mn[0] + x) * h, py = (float)(L.mn[1] + y) * h;
-    float wz[2], best[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        wz[k] = (float)(L.mn[2] + z0 + zl + 2 * k) * h;
-        best[k] = __int_as_float(0x7f800000);
-    }
-    // the sub-brick's point box (the lattice coordinates its voxels compute) and centre
-    const float sx0 = (float)(L.mn[0] + x0) * h, sx1 = (float)(L.mn[0] + x0 + 3) * h;
-    const float sy0 = (float)(L.mn[1] + y0) * h, sy1 = (float)(L.mn[1] + y0 + 3) * h;
-    const float sz0 = (float)(L.mn[2] + z0) * h, sz1 = (float)(L.mn[2] + z0 + 3) * h;
-    const f3 ctr = mk(0.5f * (sx0 + sx1), 0.5f * (sy0 + sy1), 0.5f * (sz0 + sz1));
-    const float mag = fmaxf(fmaxf(fmaxf(fabsf(sx0), fabsf(sx1)), fmaxf(fabsf(sy0), fabsf(sy1))),
-                            fmaxf(fabsf(sz0), fabsf(sz1))) + bw;
-    const unsigned long long o = off[b];
     const int* src = reinterpret_cast<const int*>(stt);
     int* dsm = reinterpret_cast<int*>(s);
-    // pass 1: the centre's nearest triangle
-    float u2 = __int_as_float(0x7f800000);
-    for (unsigned c0 = 0; c0 < n; c0 += kSplatChunk) {
-        const unsigned m = min((unsigned)kSplatChunk, n - c0);
-        for (unsigned w = tid; w < m * 24u; w += kDenseThreads) {
-            const unsigned rec = w / 24u, word = w - rec * 24u;
-            dsm[w] = __ldg(src + (size_t)list[o + c0 + rec] * 24 + word);
-        }
-        __syncthreads();
-        for (unsigned i = lane; i < m; i += 32) {
-            const SplatTri& r = s[i];
-            u2 = fminf(u2, ptd_sq(ctr, mk(r.v[0], r.v[1], r.v[2]), mk(r.v[3], r.v[4], r.v[5]),
-                                  mk(r.v[6], r.v[7], r.v[8])));
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int sh = 16; sh > 0; sh >>= 1) u2 = fminf(u2, __shfl_xor_sync(0xffffffffu, u2, sh));
-    const float ex = sx1 - sx0, ey = sy1 - sy0, ez = sz1 - sz0;
-    const float ub = sqrtf(u2) + 0.5f * sqrtf(ex * ex + ey * ey + ez * ez) + 16.0f * mag * 3.814697265625e-6f;
-    const float ub2 = ub * ub;
-    // pass 2: per chunk, this warp's surviving triangles, then the per-voxel update
     unsigned evals = 0;
-    for (unsigned c0 = 0; c0 < n; c0 += kSplatChunk) {
-        const unsigned m = min((unsigned)kSplatChunk, n - c0);
-        for (unsigned w = tid; w < m * 24u; w += kDenseThreads) {
-            const unsigned rec = w / 24u, word = w - rec * 24u;
-            dsm[w] = __ldg(src + (size_t)list[o + c0 + rec] * 24 + word);
-        }
-        __syncthreads();
-        unsigned nk = 0;
-        for (unsigned base = 0; base < m; base += 32) {
-            const unsigned i = base + lane;
-            bool keep = false;
-            if (i < m) {
-                const SplatTri& r = s[i];
-                if (!(x0 + 3 < r.fx0 || x0 > r.fx1 || y0 + 3 < r.fy0 || y0 > r.fy1)) {
-                    const float gx = fmaxf(fmaxf(r.bb[0] - sx1, sx0 - r.bb[1]), 0.0f);
-                    const float gy = fmaxf(fmaxf(r.bb[2] - sy1, sy0 - r.bb[3]), 0.0f);
-                    const float gz = fmaxf(fmaxf(r.bb[4] - sz1, sz0 - r.bb[5]), 0.0f);
-                    keep = gx * gx + gy * gy + gz * gz <= ub2;
-                }
-            }
-            const unsigned bal = __ballot_sync(0xffffffffu, keep);
-            if (keep) keep_idx[warp][nk + __popc(bal & ((1u << lane) - 1u))] = (unsigned char)i;
-            nk += __popc(bal);
-        }
-        __syncwarp();
-        for (unsigned j = 0; j < nk; ++j)
-            splat_tri<true, 2>(s[keep_idx[warp][j]], x, y, px, py, wz, bw, band_sq, best, evals);
-        __syncthreads();
-    }
-    unsigned found = 0;
-    if (x < L.dims[0] && y < L.dims[1]) {
+    for (unsigned long long di = blockIdx.x; di < nd; di += gridDim.x) {
+        const unsigned b = active[L.nbricks - 1 - (long long)di];
+        const unsigned n = cnt[b];
+        const unsigned lo = (unsigned)((unsigned long long)n * blockIdx.y / kDenseSlices);
+        const unsigned hi = (unsigned)((unsigned long long)n * (blockIdx.y + 1) / kDenseSlices);
+        const int bx = (int)(b % (unsigned)nbx), by = (int)((b / (unsigned)nbx) % (unsigned)nby),
+                  bz = (int)(b / ((unsigned)nbx * (unsigned)nby));
+        const int x0 = bx * kBrick + (warp & 1) * 4, y0 = by * kBrick + ((warp >> 1) & 1) * 4,
+                  z0 = bz * kBrick + (warp >> 2) * 4;
+        const int x = x0 + (lane & 3), y = y0 + ((lane >> 2) & 3), zl = lane >> 4;
+        const float px = (float)(L.mn[0] + x) * h, py = (float)(L.mn[1] + y) * h;
+        float wz[2], best[2];
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-            const int z = z0 + zl + 2 * k;
-            if (z < L.dims[2] && best[k] != __int_as_float(0x7f800000)) {
-                dist[((size_t)z * L.dims[1] + y) * L.dims[0] + x] = sqrtf(best[k]);
-                ++found;
+            wz[k] = (float)(L.mn[2] + z0 + zl + 2 * k) * h;
+            best[k] = __int_as_float(0x7f800000);
+        }
+        // the sub-brick's point box (the lattice coordinates its voxels compute) and centre
+        const float sx0 = (float)(L.mn[0] + x0) * h, sx1 = (float)(L.mn[0] + x0 + 3) * h;
+        const float sy0 = (float)(L.mn[1] + y0) * h, sy1 = (float)(L.mn[1] + y0 + 3) * h;
+        const float sz0 = (float)(L.mn[2] + z0) * h, sz1 = (float)(L.mn[2] + z0 + 3) * h;
+        const f3 ctr = mk(0.5f * (sx0 + sx1), 0.5f * (sy0 + sy1), 0.5f * (sz0 + sz1));
+        const float mag = fmaxf(fmaxf(fmaxf(fabsf(sx0), fabsf(sx1)), fmaxf(fabsf(sy0), fabsf(sy1))),
+                                fmaxf(fabsf(sz0), fabsf(sz1))) + bw;
+        const unsigned long long o = off[b];
+        // pass 1: the centre's nearest triangle of the slice
+        float u2 = __int_as_float(0x7f800000);
+        for (unsigned c0 = lo; c0 < hi; c0 += kSplatChunk) {
+            const unsigned m = min((unsigned)kSplatChunk, hi - c0);
+            for (unsigned w = tid; w < m * 24u; w += kDenseThreads) {
+                const unsigned rec = w / 24u, word = w - rec * 24u;
+                dsm[w] = __ldg(src + (size_t)list[o + c0 + rec] * 24 + word);
             }
+            __syncthreads();
+            for (unsigned i = lane; i < m; i += 32) {
+                const SplatTri& r = s[i];
+                u2 = fminf(u2, ptd_sq(ctr, mk(r.v[0], r.v[1], r.v[2]), mk(r.v[3], r.v[4], r.v[5]),
+                                      mk(r.v[6], r.v[7], r.v[8])));
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int sh = 16; sh > 0; sh >>= 1) u2 = fminf(u2, __shfl_xor_sync(0xffffffffu, u2, sh));
+        const float ex = sx1 - sx0, ey = sy1 - sy0, ez = sz1 - sz0;
+        const float ub = sqrtf(u2) + 0.5f * sqrtf(ex * ex + ey * ey + ez * ez) + 16.0f * mag * 3.814697265625e-6f;
+        const float ub2 = ub * ub;
+        // pass 2: per chunk, this warp's surviving triangles, then the per-voxel update
+        for (unsigned c0 = lo; c0 < hi; c0 += kSplatChunk) {
+            const unsigned m = min((unsigned)kSplatChunk, hi - c0);
+            for (unsigned w = tid; w < m * 24u; w += kDenseThreads) {
+                const unsigned rec = w / 24u, word = w - rec * 24u;
+                dsm[w] = __ldg(src + (size_t)list[o + c0 + rec] * 24 + word);
+            }
+            __syncthreads();
+            unsigned nk = 0;
+            for (unsigned base = 0; base < m; base += 32) {
+                const unsigned i = base + lane;
+                bool keep = false;
+                if (i < m) {
+                    const SplatTri& r = s[i];
+                    if (!(x0 + 3 < r.fx0 || x0 > r.fx1 || y0 + 3 < r.fy0 || y0 > r.fy1)) {
+                        const float gx = fmaxf(fmaxf(r.bb[0] - sx1, sx0 - r.bb[1]), 0.0f);
+                        const float gy = fmaxf(fmaxf(r.bb[2] - sy1, sy0 - r.bb[3]), 0.0f);
+                        const float gz = fmaxf(fmaxf(r.bb[4] - sz1, sz0 - r.bb[5]), 0.0f);
+                        keep = gx * gx + gy * gy + gz * gz <= ub2;
+                    }
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                if (keep) keep_idx[warp][nk + __popc(bal & ((1u << lane) - 1u))] = (unsigned char)i;
+                nk += __popc(bal);
+            }
+            __syncwarp();
+            for (unsigned j = 0; j < nk; ++j)
+                splat_tri<true, 2>(s[keep_idx[warp][j]], x, y, px, py, wz, bw, band_sq, best, evals);
+            __syncthreads();
+        }
+        if (x < L.dims[0] && y < L.dims[1]) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int z = z0 + zl + 2 * k;
+                if (z < L.dims[2] && best[k] != __int_as_float(0x7f800000))
+                    atomicMin(reinterpret_cast<unsigned*>(dist) + ((size_t)z * L.dims[1] + y) * L.dims[0] + x,
+                              __float_as_uint(sqrtf(best[k])));
+            }
+        }
+    }
+    const unsigned ew = __reduce_add_sync(0xffffffffu, evals);
+    if (lane == 0 && ew) atomicAdd(&ds->splat_evals, (unsigned long long)ew);
+}
+
+// The band voxels of the dense bricks (the splat's atomic minima leave them below the far
+// sentinel), counted once each.
+__global__ void __launch_bounds__(256) dense_count_kernel(const unsigned* __restrict__ active, Lattice L,
+                                                          const float* __restrict__ dist, DevState* ds) {
+    if (ds->overflow) return;
+    const unsigned long long nd = ds->dense_bricks;
+    const int nbx = L.nb[0], nby = L.nb[1];
+    unsigned found = 0;
+    for (unsigned long long di = blockIdx.x; di < nd; di += gridDim.x) {
+        const unsigned b = active[L.nbricks - 1 - (long long)di];
+        const int bx = (int)(b % (unsigned)nbx), by = (int)((b / (unsigned)nbx) % (unsigned)nby),
+                  bz = (int)(b / ((unsigned)nbx * (unsigned)nby));
+        for (int v = threadIdx.x; v < kBrick * kBrick * kBrick; v += blockDim.x) {
+            const int x = bx * kBrick + (v & 7), y = by * kBrick + ((v >> 3) & 7), z = bz * kBrick + (v >> 6);
+            if (x < L.dims[0] && y < L.dims[1] && z < L.dims[2] &&
+                dist[((size_t)z * L.dims[1] + y) * L.dims[0] + x] < kFarSentinel)
+                ++found;
         }
     }
     const unsigned fw = __reduce_add_sync(0xffffffffu, found);
-    const unsigned ew = __reduce_add_sync(0xffffffffu, evals);
-    if (lane == 0) {
-        if (fw) atomicAdd(&ds->band_voxels, (unsigned long long)fw);
-        if (ew) atomicAdd(&ds->splat_evals, (unsigned long long)ew);
-    }
+    if ((threadIdx.x & 31) == 0 && fw) atomicAdd(&ds->band_voxels, (unsigned long long)fw);
 }
 
 __global__ void __launch_bounds__(kSplatThreads) splat_kernel(
@@ -642,11 +672,14 @@ void launch_splat(const SplatTri* stt, const unsigned long long* brick_off, cons
         splat_kernel<<<(unsigned)blocks, kSplatThreads, 0, st>>>(stt, brick_off, brick_count, brick_list, active, L,
                                                                  dist, ds);
     }
-    const long long dblocks = n_dense < 0 ? L.nbricks : n_dense;
+    // dense bricks: known count, or read on the device with a grid-stride over at most 4096
+    const long long dblocks = n_dense < 0 ? std::min<long long>(L.nbricks, 4096) : n_dense;
     if (dblocks > 0) {
         GBSDF_COUNT_LAUNCH();
-        splat_dense_kernel<<<(unsigned)dblocks, kDenseThreads, 0, st>>>(stt, brick_off, brick_count, brick_list,
-                                                                        active, L, dist, ds);
+        splat_dense_kernel<<<dim3((unsigned)dblocks, kDenseSlices), kDenseThreads, 0, st>>>(
+            stt, brick_off, brick_count, brick_list, active, L, dist, ds);
+        GBSDF_COUNT_LAUNCH();
+        dense_count_kernel<<<(unsigned)std::min<long long>(dblocks, 1024), 256, 0, st>>>(active, L, dist, ds);
     }
 }
 
