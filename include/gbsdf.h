@@ -174,6 +174,11 @@ typedef struct gbsdf_stats {
     double band_err_fp64;      /* largest |FP32 band distance - FP64 distance| over the sampled band
                                   voxels, in voxels (fast path; 0 when no band voxel was sampled) */
     int64_t band_err_samples;  /* band voxels sampled for band_err_fp64 */
+    float ms_sweeps;           /* fast path: the directional sweeps of the eikonal stage alone (from
+                                  the first sweep's launch to the last's end, round bookkeeping
+                                  included; without the padded copies, audit and clamp that
+                                  ms_eikonal also holds) */
+    int32_t reserved;
 } gbsdf_stats;
 
 /* Fill `opt` with defaults: reference mode, AUTO path, device 0, host triangles. */
@@ -396,8 +401,11 @@ int gbsdf_legacy_sdf_noalloc(const gbsdf_tri* tris_dev, int64_t n_tris, float vo
  * general one for every non-NaN float input, the one for non-negative arguments for every
  * finite non-negative float -- and the packed square root of the paired updates with
  * sqrtf on zero and every float in [2^-100, 2^100]; which = 1: the x sweep's TMA tile layout (32-byte swizzle,
- * out-of-lattice fill) is checked element by element on five boxes of a test grid.
- * *result = number of mismatches (0 expected). */
+ * out-of-lattice fill) is checked element by element on five boxes of a test grid;
+ * which = 2: the branch-free and packed-lane forms of the reference's Godunov update used
+ * by the sweeps are compared bit for bit with the reference's branching form on 2^30
+ * generated neighbour triples at eight voxel sizes (ties, far sentinels and the 1D / 2D
+ * boundary included). *result = number of mismatches (0 expected). */
 int gbsdf_selftest(int32_t which, int32_t device, uint64_t* result, char* err, size_t errlen);
 
 /* Library version string. */

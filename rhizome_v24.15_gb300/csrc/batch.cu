@@ -167,7 +167,7 @@ void place_learned(Job& j, Carver& c) {
 void place_phase1(Job& j, Carver& c) {
     const Lattice& L = j.L;
     const long long N = L.N, T = j.T;
-    // the grid copies also hold the eikonal's padded layout (rows of a multiple of 4 floats)
+    // the grid copies also hold the eikonal's padded layout (rows of a multiple of 8 floats)
     j.A = c.take<float>((size_t)std::max(N, padded_voxels(L)) * 4);
     j.B = c.take<float>((size_t)std::max(N, padded_voxels(L)) * 4);
     j.S = c.take<uint32_t>((size_t)L.nwords * 4);
@@ -263,7 +263,7 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
     };
     fixup_passes(learned ? j.E : nullptr);
     // [D]: the reference's round loop, stopped on the device when a round changes nothing;
-    // a lattice whose rows are not a multiple of 4 floats is swept in padded copies (B <->
+    // a lattice whose rows are not a multiple of 8 floats is swept in padded copies (B <->
     // A), the result copied back into A
     const Lattice Lp = padded(L);
     const bool pad = Lp.px != L.dims[0];
@@ -279,8 +279,8 @@ void enqueue_build(gbsdf_batch& b, Job& j, cudaStream_t st) {
             }
         launch_end_round(r, r, kMaxRounds, j.ds, st);
     }
-    if (pad) launch_unpad_rows(j.B, j.A, Lp, st);
-    launch_audit(j.A, L, j.ds, st);
+    if (pad) launch_unpad_rows(j.B, j.A, Lp, st, j.ds);  // with the audit's count
+    else launch_audit(j.A, L, j.ds, st);
     launch_clamp(j.A, j.S, L, j.ds, st);
     // [E]
     for (int gen = 0; gen < kProbeGens; ++gen) {

@@ -62,7 +62,7 @@ struct Workspace {
     int device = -1;
     int num_sms = 0;
     cudaStream_t st = nullptr;
-    cudaEvent_t ev[12] = {};
+    cudaEvent_t ev[14] = {};
     std::mutex mu;
     Buf A, B, S, U, t12, t9, stt, ptt, bcount, bcur, boff, active, blist, scount, scur, soff, slist, scan, list,
         recheck, hb, verts, idx, flags, fpos, S2, U2, fbase, fX, logits, opencnt, ekeys, ecnt, mparts, mlossp, phist, E, fwc, fwt, fwo, fwn, fwu, fwf, fwoff,
@@ -297,7 +297,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     const float stol = exact_signs ? kSurfaceTolExactSigns : kSurfaceTolVoxels;
     const long long N = L.N;
     // ---- buffers
-    // the grid copies also hold the eikonal's padded layout (rows of a multiple of 4 floats)
+    // the grid copies also hold the eikonal's padded layout (rows of a multiple of 8 floats)
     GB_CK(ensure(w.A, (size_t)std::max(N, padded_voxels(L)) * 4));
     GB_CK(ensure(w.B, (size_t)std::max(N, padded_voxels(L)) * 4));
     GB_CK(ensure(w.S, (size_t)L.nwords * 4));
@@ -430,39 +430,53 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     GB_CK(cudaEventRecord(w.ev[5], st));
     // ---- [D]
     const int rule = ref_eikonal ? 0 : 1;
-    // The sweeps address rows of a multiple of 4 floats (TMA descriptors need 16-byte row
-    // pitches): a lattice whose rows are not is swept in padded copies -- the band field
-    // copied into B, the rounds ping-ponging B <-> A, the result copied back into A.
+    // The sweeps address rows of a multiple of 8 floats (padded(L)): a lattice whose rows are
+    // not is swept in padded copies. Where the band field's own rows are 16-byte multiples and
+    // the first x sweep reads its source through a TMA descriptor, that sweep reads A through a
+    // descriptor of A's dense rows and writes the padded copy into B; the rounds ping-pong
+    // B <-> A, and the result (back in A, padded) is copied dense into B, which then takes A's
+    // place. Otherwise the band field is first copied into B, the rounds ping-pong B <-> A and
+    // the result is copied back into A.
     const Lattice Lp = padded(L);
     const bool pad = Lp.px != L.dims[0];
-    float* src = pad ? P<float>(w.B) : P<float>(w.A);
-    float* dst = pad ? P<float>(w.A) : P<float>(w.B);
-    if (pad) launch_pad_rows(P<float>(w.A), P<float>(w.B), Lp, st);
-    // TMA descriptors of the two grid copies for the staged sweeps
-    GridMap map_a, map_b;
+    GridMap map_a, map_b, map_dense;
     encode_grid_map(map_a, P<float>(w.A), Lp);
     encode_grid_map(map_b, P<float>(w.B), Lp);
+    const bool dense_map = pad && encode_grid_map(map_dense, P<float>(w.A), L);
     auto map_of = [&](const float* p) { return p == P<float>(w.A) ? &map_a : &map_b; };
+    float* src = P<float>(w.A);
+    float* dst = P<float>(w.B);
     // sweep_schedule: 0 autotuned; else x schedule + 10 x walk schedule (a 0 digit: tuned).
-    // The first round and the later ones have their own tuned plans (phase 0 / 1).
+    // The first round and the later ones have their own tuned plans (phase 0 / 1); phase 0
+    // times the candidates on the band field in A (through the dense descriptor where the
+    // first sweep will read it so), writing only B.
     const int xs_opt = o.sweep_schedule % 10, ws_opt = o.sweep_schedule / 10;
     const bool tune = xs_opt == 0 || ws_opt == 0;
     SweepPlan plan;
-    auto set_plan = [&](int phase) -> int {
-        plan = tuned_sweep_plan(w.device, Lp, src, dst, map_of(src), w.ds, st, tune, phase);
+    auto set_plan = [&](int phase, const GridMap* m) -> int {
+        plan = tuned_sweep_plan(w.device, Lp, src, dst, m, w.ds, st, tune, phase);
         if (xs_opt >= kXCpAsync && xs_opt <= kXTmaWide) plan.x = xs_opt;
         if (ws_opt >= kWCpAsync && ws_opt <= kWTmaVec2) plan.w = ws_opt;
         GB_CK(cudaGetLastError());
         return (int)GBSDF_OK;
     };
-    if (int rcp = set_plan(0)) return rcp;
+    if (int rcp = set_plan(0, dense_map ? &map_dense : map_of(src))) return rcp;
+    const bool fused_pad = dense_map && plan.x != kXCpAsync;
+    if (pad && !fused_pad) {
+        launch_pad_rows(P<float>(w.A), P<float>(w.B), Lp, st);
+        std::swap(src, dst);
+    }
+    const GridMap* lead = fused_pad ? &map_dense : nullptr;  // the first sweep's source descriptor
+    GB_CK(cudaEventRecord(w.ev[12], st));  // events 12 and 13: the directional sweeps alone
     if (ref_eikonal) {
         for (int r = 0; r < kMaxRounds; ++r) {
             if (r == 1)
-                if (int rcp = set_plan(1)) return rcp;
+                if (int rcp = set_plan(1, map_of(src))) return rcp;
             for (int axis = 0; axis < 3; ++axis)
                 for (int dir = 1; dir >= -1; dir -= 2) {
-                    launch_sweep(rule, axis, dir, r, src, dst, Lp, w.ds, st, map_of(src), plan.x, plan.w);
+                    launch_sweep(rule, axis, dir, r, src, dst, Lp, w.ds, st, lead ? lead : map_of(src), plan.x,
+                                 plan.w);
+                    lead = nullptr;
                     std::swap(src, dst);
                 }
             launch_end_round(r, r, kMaxRounds, w.ds, st);
@@ -473,12 +487,13 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         for (int r0 = 0; r0 < cap; r0 += batch) {
             for (int r = r0; r < std::min(cap, r0 + batch); ++r) {
                 if (r == 1)
-                    if (int rcp = set_plan(1)) return rcp;
+                    if (int rcp = set_plan(1, map_of(src))) return rcp;
                 GB_CK(cudaMemsetAsync(&w.ds->changed[r % 64], 0, sizeof(int), st));
                 for (int axis = 0; axis < 3; ++axis)
                     for (int dir = 1; dir >= -1; dir -= 2) {
-                        launch_sweep(rule, axis, dir, r % 64, src, dst, Lp, w.ds, st, map_of(src), plan.x,
-                                     plan.w);
+                        launch_sweep(rule, axis, dir, r % 64, src, dst, Lp, w.ds, st, lead ? lead : map_of(src),
+                                     plan.x, plan.w);
+                        lead = nullptr;
                         std::swap(src, dst);
                     }
                 launch_end_round(r % 64, r, cap, w.ds, st);
@@ -488,9 +503,17 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
             if (w.hs->stop) break;
         }
     }
+    GB_CK(cudaEventRecord(w.ev[13], st));
     // rounds are whole (6 sweeps, an even number), so the field is back in the first source
-    if (pad) launch_unpad_rows(P<float>(w.B), P<float>(w.A), Lp, st);
-    launch_audit(P<float>(w.A), L, w.ds, st);
+    // (the copy back also takes the audit's count of voxels still at the far sentinel)
+    if (fused_pad) {
+        launch_unpad_rows(P<float>(w.A), P<float>(w.B), Lp, st, w.ds);
+        std::swap(w.A, w.B);  // equal sizes; the field is in A again from here on
+    } else if (pad) {
+        launch_unpad_rows(P<float>(w.B), P<float>(w.A), Lp, st, w.ds);
+    } else {
+        launch_audit(P<float>(w.A), L, w.ds, st);
+    }
     launch_clamp(P<float>(w.A), P<uint32_t>(w.S), L, w.ds, st);
     GB_CK(cudaGetLastError());
     GB_CK(cudaEventRecord(w.ev[6], st));
@@ -588,6 +611,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         stats->ms_parity = ev_ms(w.ev[3], w.ev[4]);
         stats->ms_fixup = ev_ms(w.ev[4], w.ev[5]);
         stats->ms_eikonal = ev_ms(w.ev[5], w.ev[6]);
+        stats->ms_sweeps = ev_ms(w.ev[12], w.ev[13]);
         stats->ms_verify = ev_ms(w.ev[6], w.ev[7]);
         stats->ms_apply = ev_ms(w.ev[7], w.ev[8]);
         stats->ms_d2h = ev_ms(w.ev[8], w.ev[9]);
@@ -1053,7 +1077,7 @@ int gbsdf_selftest(int32_t which, int32_t device, uint64_t* result, char* err, s
     Err e{err, errlen};
     if (err && errlen) err[0] = 0;
     if (!result) return e.set(GBSDF_EINVAL, "null result");
-    if (which != 0 && which != 1) return e.set(GBSDF_EINVAL, "unknown self-test %d", which);
+    if (which < 0 || which > 2) return e.set(GBSDF_EINVAL, "unknown self-test %d", which);
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) {
         cudaGetLastError();
@@ -1064,8 +1088,9 @@ int gbsdf_selftest(int32_t which, int32_t device, uint64_t* result, char* err, s
     GB_CK(cudaMalloc(&d, sizeof(unsigned long long)));
     cudaError_t rc = cudaMemset(d, 0, sizeof(unsigned long long));
     if (rc == cudaSuccess) {
-        if (which == 0) {
-            launch_selftest_div3(d, 0);
+        if (which == 0 || which == 2) {
+            if (which == 0) launch_selftest_div3(d, 0);
+            else launch_selftest_godunov(d, 0);
             rc = cudaGetLastError();
         } else if (selftest_tma_tile(d) != 0) {
             cudaFree(d);

@@ -355,6 +355,46 @@ __device__ __forceinline__ float godunov_ref_nb(float ax, float ay, float az, fl
     return t3 ? u3 : (t2 ? u2 : u1);
 }
 
+// Constants of godunov_ref_nbp for one voxel size.
+struct GodunovOneConsts {
+    float h, m2h, na3, r3;
+    f32x2 half, half_r3;  // (1/2, 1/2), (1/2, RN(1/3))
+};
+__device__ __forceinline__ GodunovOneConsts godunov_one_consts(float h) {
+    const float r3 = 0.333333343267440796f;
+    return GodunovOneConsts{h, -2.0f * h, -(3.0f * h * h), r3, pk2(0.5f, 0.5f), pk2(0.5f, r3)};
+}
+
+// godunov_ref_nb for one voxel with the operations of its 2D and 3D candidates paired on
+// packed FP32 lanes where they are independent: (d, e2) = (s1 - s0, s2 - s0), the two
+// square roots in one nsqrt2_rn, (t01 - r2, t012 - r3) and (x2 / 2, x3 * RN(1/3)). Each lane
+// is the scalar operation of godunov_ref_nb on the same operands, so the result is the same
+// bit for bit. For a serial chain (the x sweep's one line per thread), where no second
+// voxel is at hand to pair with. Voxel sizes with pair_sqrt_ok.
+__device__ __forceinline__ float godunov_ref_nbp(float ax, float ay, float az, const GodunovOneConsts& c) {
+    const float s0 = min3f(ax, ay, az), s2 = max3f(ax, ay, az);
+    const float s1 = ax + ay + az - s0 - s2;
+    const float u1 = s0 + c.h;
+    float d, e2;
+    up2(sub2(pk2(s1, s2), pk2(s0, s0)), d, e2);
+    const float dd = d * d;
+    const float nd = __fmaf_rn(c.m2h, c.h, dd);  // -disc
+    const float e1 = s2 - s1;
+    const float nd3 = __fmaf_rn(__fmaf_rn(e2, e2, __fmaf_rn(e1, e1, dd)), 0.5f, c.na3);  // -disc3
+    const float t01 = s0 + s1;
+    const f32x2 X = sub2(pk2(t01, t01 + s2), nsqrt2_rn(pk2(nd, nd3), c.half));  // (t01 + r2, t012 + r3)
+    float u2, q, x3;
+    up2(mul2(X, c.half_r3), u2, q);
+    {
+        float x2;
+        up2(X, x2, x3);
+    }
+    const float u3 = __fmaf_rn(__fmaf_rn(-3.0f, q, x3), c.r3, q);  // div3_pos(x3)
+    const bool t2 = (u1 > s1) && (nd <= 0.0f);
+    const bool t3 = t2 && (u2 > s2) && (nd3 <= 0.0f);
+    return t3 ? u3 : (t2 ? u2 : u1);
+}
+
 // Voxel sizes for which every square-root operand of the paired updates lies in
 // nsqrt2_rn's checked range, {0} and [2^-100, 2^100]: a non-zero discriminant
 // 2h*h - d*d is at least 2^(2e-45) with e = floor(log2 h) (the granularity of the exact

@@ -535,9 +535,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// NB: the reference's update without branches (godunov_ref_nb; RULE 0 at voxel sizes with
-// pair_sqrt_ok), identical results.
-template <int RULE, int DIR, bool NB = false>
+// NB: the reference's update without branches, RULE 0 at voxel sizes with pair_sqrt_ok
+// (1: godunov_ref_nb; 2: godunov_ref_nbp, its 2D and 3D arithmetic paired on packed FP32
+// lanes, 57-59 instructions per voxel against 66), identical results.
+template <int RULE, int DIR, int NB = 0>
 __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_constant__ CUtensorMap tm,
                                                                   float* __restrict__ dst, Lattice L, int round,
                                                                   DevState* ds) {
@@ -550,6 +551,7 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
     const int dx = L.dims[0], dy = L.dims[1], dz = L.dims[2];
     const float h = L.h;
     const float m2h = -2.0f * h, na3 = -(3.0f * h * h);
+    const GodunovOneConsts gc = godunov_one_consts(h);
     const size_t plane = (size_t)L.px * dy;
     const int tid = threadIdx.x;
     const int y0 = blockIdx.x * kXY, z0 = blockIdx.y * kXZ;
@@ -627,7 +629,8 @@ __global__ void __launch_bounds__(kPThreads) sweep_x_pipe_kernel(const __grid_co
                     const int j = (DIR > 0) ? jj : (kXC - 1 - jj);
                     const float down = (DIR > 0) ? ((j + 1 < kXC) ? cur[j + 1] : nxt) : ((j > 0) ? cur[j - 1] : nxt);
                     float u;
-                    if constexpr (NB) u = godunov_ref_nb(fminf(prev, down), ay[j], az[j], h, m2h, na3);
+                    if constexpr (NB == 2) u = godunov_ref_nbp(fminf(prev, down), ay[j], az[j], gc);
+                    else if constexpr (NB == 1) u = godunov_ref_nb(fminf(prev, down), ay[j], az[j], h, m2h, na3);
                     else u = godunov<RULE>(fminf(prev, down), ay[j], az[j], h);
                     const float out = (u < cur[j]) ? u : cur[j];
                     ch |= (u < cur[j]);
@@ -1583,9 +1586,9 @@ void launch_sweep_t(int axis, int round, const float* src, float* dst, const Lat
     } else if (xsched == kXTmaPipe || xsched == kXTmaPipe2 || xsched == kXTmaWide) {
         dim3 grid((dy + kXY - 1) / kXY, (dz + kXZ - 1) / kXZ);
         if (pair_ok) {
-            cudaFuncSetAttribute(sweep_x_pipe_kernel<0, DIR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            cudaFuncSetAttribute(sweep_x_pipe_kernel<0, DIR, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kPSmem);
-            sweep_x_pipe_kernel<0, DIR, true><<<grid, kPThreads, kPSmem, st>>>(src_map->map, dst, L, round, ds);
+            sweep_x_pipe_kernel<0, DIR, 2><<<grid, kPThreads, kPSmem, st>>>(src_map->map, dst, L, round, ds);
         } else {
             cudaFuncSetAttribute(sweep_x_pipe_kernel<RULE, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kPSmem);
@@ -1691,34 +1694,74 @@ int selftest_tma_tile(unsigned long long* mism_dev) {
 
 namespace {
 // Dense x-fastest grid (rows of dims[0]) <-> the sweeps' padded copy (rows of px floats;
-// pad columns written as 0, never read as voxels). One thread per padded / dense element.
+// pad columns written as 0, never read as voxels). One warp per row at a time, no index
+// division; 16-byte copies where dims[0] is a multiple of 4 (both rows' starts are then
+// 16-byte aligned and a quad is wholly voxels or wholly pad).
+template <bool VEC>
 __global__ void pad_rows_kernel(const float* __restrict__ dense, float* __restrict__ pad, Lattice L) {
-    const long long n = (long long)L.px * L.dims[1] * L.dims[2];
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const long long row = i / L.px;
-        const int x = (int)(i - row * L.px);
-        pad[i] = (x < L.dims[0]) ? dense[row * L.dims[0] + x] : 0.0f;
+    const long long nrows = (long long)L.dims[1] * L.dims[2];
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31, dx = L.dims[0], px = L.px;
+    for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrows; r += nw) {
+        const float* s = dense + r * dx;
+        float* d = pad + r * px;
+        if constexpr (VEC) {
+            for (int q = lane; q < (px >> 2); q += 32)
+                reinterpret_cast<float4*>(d)[q] =
+                    (4 * q < dx) ? reinterpret_cast<const float4*>(s)[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else {
+            for (int x = lane; x < px; x += 32) d[x] = (x < dx) ? s[x] : 0.0f;
+        }
     }
 }
-__global__ void unpad_rows_kernel(const float* __restrict__ pad, float* __restrict__ dense, Lattice L) {
-    const long long n = L.N;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const long long row = i / L.dims[0];
-        dense[i] = pad[row * L.px + (i - row * L.dims[0])];
+// The copy back, counting on the way the voxels still at the far sentinel (the audit,
+// [D2]) when `far` is not null.
+template <bool VEC>
+__global__ void unpad_rows_kernel(const float* __restrict__ pad, float* __restrict__ dense, Lattice L,
+                                  unsigned long long* __restrict__ far) {
+    const long long nrows = (long long)L.dims[1] * L.dims[2];
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31, dx = L.dims[0], px = L.px;
+    unsigned c = 0;
+    for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrows; r += nw) {
+        const float* s = pad + r * px;
+        float* d = dense + r * dx;
+        if constexpr (VEC) {
+            for (int q = lane; q < (dx >> 2); q += 32) {
+                const float4 v = reinterpret_cast<const float4*>(s)[q];
+                reinterpret_cast<float4*>(d)[q] = v;
+                c += (v.x >= 1e29f) + (v.y >= 1e29f) + (v.z >= 1e29f) + (v.w >= 1e29f);
+            }
+        } else {
+            for (int x = lane; x < dx; x += 32) {
+                const float v = s[x];
+                d[x] = v;
+                c += (v >= 1e29f);
+            }
+        }
     }
+    if (far) {
+        c = __reduce_add_sync(0xffffffffu, c);
+        if (lane == 0 && c) atomicAdd(far, (unsigned long long)c);
+    }
+}
+
+unsigned row_copy_blocks(const Lattice& P) {
+    const long long nrows = (long long)P.dims[1] * P.dims[2];
+    return (unsigned)std::max<long long>(1, std::min<long long>((nrows + 7) / 8, 152LL * 16));
 }
 }  // namespace
 
 void launch_pad_rows(const float* dense, float* pad, const Lattice& P, cudaStream_t st) {
-    const long long n = (long long)P.px * P.dims[1] * P.dims[2];
     GBSDF_COUNT_LAUNCH();
-    pad_rows_kernel<<<(unsigned)std::min<long long>((n + 255) / 256, 152LL * 16), 256, 0, st>>>(dense, pad, P);
+    if ((P.dims[0] & 3) == 0) pad_rows_kernel<true><<<row_copy_blocks(P), 256, 0, st>>>(dense, pad, P);
+    else pad_rows_kernel<false><<<row_copy_blocks(P), 256, 0, st>>>(dense, pad, P);
 }
-void launch_unpad_rows(const float* pad, float* dense, const Lattice& P, cudaStream_t st) {
+void launch_unpad_rows(const float* pad, float* dense, const Lattice& P, cudaStream_t st, DevState* audit_ds) {
     GBSDF_COUNT_LAUNCH();
-    unpad_rows_kernel<<<(unsigned)std::min<long long>((P.N + 255) / 256, 152LL * 16), 256, 0, st>>>(pad, dense, P);
+    unsigned long long* far = audit_ds ? &audit_ds->far_residual : nullptr;
+    if ((P.dims[0] & 3) == 0) unpad_rows_kernel<true><<<row_copy_blocks(P), 256, 0, st>>>(pad, dense, P, far);
+    else unpad_rows_kernel<false><<<row_copy_blocks(P), 256, 0, st>>>(pad, dense, P, far);
 }
 
 void launch_end_round(int slot, int round, int cap, DevState* ds, cudaStream_t st) {

@@ -166,6 +166,55 @@ __global__ void selftest_div3_kernel(unsigned long long* __restrict__ mism) {
     if (bad) atomicAdd(mism, bad);
 }
 
+// Self-test of the reference update's branch-free forms: godunov_ref_nb, godunov_ref_nbp
+// (one voxel, packed lanes) and both lanes of godunov_ref_pair against godunov_ref (the
+// reference's branches, sqrtf, div3_rn) on 2^30 generated neighbour triples. Eight voxel
+// sizes across the range of pair_sqrt_ok; neighbours a random base up to 600 h plus up to
+// 2 h each, with ties, exact 1D / 2D boundaries (s1 = s0 + h), far sentinels and zeros
+// mixed in, so every branch of the reference rule is taken.
+__device__ __forceinline__ uint32_t st_mix(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ void st_triple(uint32_t i, float h, float* v) {
+    const uint32_t r1 = st_mix(i * 4u + 1u), r2 = st_mix(i * 4u + 2u), r3 = st_mix(i * 4u + 3u);
+    const float base = h * 600.0f * (float)(r1 >> 8) * 0x1p-24f;
+    v[0] = base + h * 2.0f * (float)(r2 & 0xffffu) * 0x1p-16f;
+    v[1] = base + h * 2.0f * (float)(r2 >> 16) * 0x1p-16f;
+    v[2] = base + h * 2.0f * (float)(r3 & 0xffffu) * 0x1p-16f;
+    const uint32_t k = (r3 >> 16) & 15u, a = (r3 >> 20) % 3u, b = (a + 1u + ((r3 >> 22) & 1u)) % 3u;
+    if (k == 0) v[a] = kFarSentinel;
+    else if (k == 1) v[a] = v[b];
+    else if (k == 2) v[a] = v[b] = v[3 - a - b];
+    else if (k == 3) v[a] = v[b] + h;
+    else if (k == 4) v[a] = 0.0f;
+    else if (k == 5) v[a] = v[b] = kFarSentinel;
+}
+__global__ void selftest_godunov_kernel(unsigned long long* __restrict__ mism) {
+    const float hs[8] = {0.1f, 1.0f, 0.37f, 0x1p-20f, 0x1p20f, 3.3e-3f, 25.0f, 0.0625f};
+    const uint32_t stride = gridDim.x * blockDim.x;
+    unsigned long long bad = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (1u << 30); i += stride) {
+        const float h = hs[st_mix(i ^ 0x5bd1e995u) & 7u];
+        float a[3], b[3];
+        st_triple(i, h, a);
+        st_triple(i ^ 0x2545f491u, h, b);
+        const float ra = godunov_ref(a[0], a[1], a[2], h), rb = godunov_ref(b[0], b[1], b[2], h);
+        const float nb = godunov_ref_nb(a[0], a[1], a[2], h, -2.0f * h, -(3.0f * h * h));
+        const float nbp = godunov_ref_nbp(a[0], a[1], a[2], godunov_one_consts(h));
+        float p0, p1;
+        godunov_ref_pair(a[0], a[1], a[2], b[0], b[1], b[2], godunov_pair_consts(h), p0, p1);
+        const unsigned w = __float_as_uint(ra);
+        bad += (__float_as_uint(nb) != w) + (__float_as_uint(nbp) != w) + (__float_as_uint(p0) != w) +
+               (__float_as_uint(p1) != __float_as_uint(rb));
+    }
+    if (bad) atomicAdd(mism, bad);
+}
+
 __global__ void iota_kernel(long long* __restrict__ list, long long n, long long from) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) list[i] = from + i;
@@ -214,6 +263,11 @@ void launch_legacy_combine(const float* d2, const uint32_t* sbits, const Lattice
 void launch_selftest_div3(unsigned long long* mism, cudaStream_t st) {
     GBSDF_COUNT_LAUNCH();
     selftest_div3_kernel<<<152 * 16, 256, 0, st>>>(mism);
+}
+
+void launch_selftest_godunov(unsigned long long* mism, cudaStream_t st) {
+    GBSDF_COUNT_LAUNCH();
+    selftest_godunov_kernel<<<152 * 16, 256, 0, st>>>(mism);
 }
 
 void launch_iota(long long* list, long long n, long long from, cudaStream_t st) {

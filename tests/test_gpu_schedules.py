@@ -4,7 +4,9 @@ chunks); y / z walks staged by cp.async or by TMA
 batches on a pipeline (one or four lines per thread, the four lines' updates scalar or in
 packed FP32 pairs) -- and the autotuner's pick give
 bit-identical grids, equal to the oracle, on lattices whose rows are and are not a multiple
-of 4 floats (the latter swept in padded copies)."""
+of 8 floats (the latter swept in padded copies: 44-voxel rows padded by the first x sweep
+itself, which reads the band field through a descriptor of its dense rows, except under the
+cp.async x schedule; 97-voxel rows, whose dense pitch no descriptor takes, copied first)."""
 import numpy as np
 import pytest
 
@@ -31,7 +33,7 @@ def test_schedules_identical(engine, oracle, dims):
         outs[sched] = out
         ran = res.stats["sweep_schedule"]
         x, w = ran % 10, ran // 10
-        # every lattice has TMA descriptors (rows not a multiple of 4 floats are swept in
+        # every lattice has TMA descriptors (rows not a multiple of 8 floats are swept in
         # padded copies), so a forced schedule runs as asked
         if sched % 10:
             assert x == sched % 10
