@@ -605,7 +605,7 @@ def main():
                                     "ms_verify", "ms_apply")},
             "pipeline": {k: s0[k] for k in ("eikonal_rounds", "probes", "sites", "patch_rounds", "patched_voxels",
                                              "unknown_columns", "band_voxels", "splat_evals", "gwn_pairs",
-                                             "fp64_rechecks", "sweep_schedule")},
+                                             "fp64_rechecks", "sweep_schedule", "sweep_schedule_first")},
             "plain": plain,
             "learned": learned,
             "precision": {"band_err_fp64_vox": s0["band_err_fp64"], "band_err_samples": s0["band_err_samples"],

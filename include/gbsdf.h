@@ -178,7 +178,8 @@ typedef struct gbsdf_stats {
                                   the first sweep's launch to the last's end, round bookkeeping
                                   included; without the padded copies, audit and clamp that
                                   ms_eikonal also holds) */
-    int32_t reserved;
+    int32_t sweep_schedule_first; /* the schedules of the first round (x + 10 x walk), which the
+                                     autotuner picks apart from the later rounds' (sweep_schedule) */
 } gbsdf_stats;
 
 /* Fill `opt` with defaults: reference mode, AUTO path, device 0, host triangles. */

@@ -447,20 +447,22 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     float* src = P<float>(w.A);
     float* dst = P<float>(w.B);
     // sweep_schedule: 0 autotuned; else x schedule + 10 x walk schedule (a 0 digit: tuned).
-    // The first round and the later ones have their own tuned plans (phase 0 / 1); phase 0
-    // times the candidates on the band field in A (through the dense descriptor where the
-    // first sweep will read it so), writing only B.
+    // The first round runs the default plan (phase 0, not measured: timed on the band field
+    // alone, before any sweep has filled the far field, the candidates' order did not hold
+    // for the round, and on the 860 x 860 x 880 mug some builds picked a plan 0.9 ms slower);
+    // the later rounds run the plan tuned on the field after the first round (phase 1).
     const int xs_opt = o.sweep_schedule % 10, ws_opt = o.sweep_schedule / 10;
     const bool tune = xs_opt == 0 || ws_opt == 0;
     SweepPlan plan;
-    auto set_plan = [&](int phase, const GridMap* m) -> int {
-        plan = tuned_sweep_plan(w.device, Lp, src, dst, m, w.ds, st, tune, phase);
+    auto set_plan = [&](int phase, const GridMap* m, bool measure) -> int {
+        plan = tuned_sweep_plan(w.device, Lp, src, dst, m, w.ds, st, measure, phase);
         if (xs_opt >= kXCpAsync && xs_opt <= kXTmaWide) plan.x = xs_opt;
         if (ws_opt >= kWCpAsync && ws_opt <= kWTmaVec2) plan.w = ws_opt;
         GB_CK(cudaGetLastError());
         return (int)GBSDF_OK;
     };
-    if (int rcp = set_plan(0, dense_map ? &map_dense : map_of(src))) return rcp;
+    if (int rcp = set_plan(0, dense_map ? &map_dense : map_of(src), false)) return rcp;
+    const SweepPlan plan0 = plan;
     const bool fused_pad = dense_map && plan.x != kXCpAsync;
     if (pad && !fused_pad) {
         launch_pad_rows(P<float>(w.A), P<float>(w.B), Lp, st);
@@ -471,7 +473,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
     if (ref_eikonal) {
         for (int r = 0; r < kMaxRounds; ++r) {
             if (r == 1)
-                if (int rcp = set_plan(1, map_of(src))) return rcp;
+                if (int rcp = set_plan(1, map_of(src), tune)) return rcp;
             for (int axis = 0; axis < 3; ++axis)
                 for (int dir = 1; dir >= -1; dir -= 2) {
                     launch_sweep(rule, axis, dir, r, src, dst, Lp, w.ds, st, lead ? lead : map_of(src), plan.x,
@@ -487,7 +489,7 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         for (int r0 = 0; r0 < cap; r0 += batch) {
             for (int r = r0; r < std::min(cap, r0 + batch); ++r) {
                 if (r == 1)
-                    if (int rcp = set_plan(1, map_of(src))) return rcp;
+                    if (int rcp = set_plan(1, map_of(src), tune)) return rcp;
                 GB_CK(cudaMemsetAsync(&w.ds->changed[r % 64], 0, sizeof(int), st));
                 for (int axis = 0; axis < 3; ++axis)
                     for (int dir = 1; dir >= -1; dir -= 2) {
@@ -646,8 +648,12 @@ int run_fast(Workspace& w, long long T, const Lattice& L, const gbsdf_options& o
         stats->winding_certified = (long long)h.fwn_certified;
         stats->winding_summed = (long long)h.fwn_fallback_total;
         // x schedule + 10 x walk schedule of the last round's sweeps
-        stats->sweep_schedule = (map_a.valid ? (plan.x == kXAuto ? kXTmaPipe : plan.x) : kXCpAsync) +
-                                10 * (map_a.walk_valid ? (plan.w == kWAuto ? kWTmaPipe : plan.w) : kWCpAsync);
+        auto code = [&](const SweepPlan& p) {
+            return (map_a.valid ? (p.x == kXAuto ? kXTmaPipe : p.x) : kXCpAsync) +
+                   10 * (map_a.walk_valid ? (p.w == kWAuto ? kWTmaPipe : p.w) : kWCpAsync);
+        };
+        stats->sweep_schedule = code(plan);
+        stats->sweep_schedule_first = code(plan0);
     }
     return status;
 }

@@ -4,11 +4,13 @@
 // (internal header, XSchedule / WSchedule). Which is fastest depends on the lattice (row
 // length, CTAs per wave), the device and the field: the first round sweeps a band in a far
 // field, where most updates are one-dimensional, later rounds a field where most warps
-// need the 2D and 3D updates. So the first build of a lattice class times each candidate
-// twice on that build's own buffers -- phase 0 on the band field about to be swept, phase 1
-// on the field after the first round -- one warm-up and two timed launches each (x sweeps
-// for the x schedules, z walks for the walk schedules), CUDA events on the build's stream,
-// and remembers the winners per phase. A class is (device, row pitch a multiple of 16
+// need the 2D and 3D updates. The first build of a lattice class times each candidate on
+// that build's own buffers on the field after the first round (phase 1) -- one warm-up and
+// two timed launches each (x sweeps for the x schedules, z walks for the walk schedules),
+// CUDA events on the build's stream -- and remembers the winners for the later rounds. The
+// first round (phase 0) runs the default plan: timed on the band field alone the
+// candidates' order did not hold over the round. A caller may still ask for a measured
+// phase-0 plan (measure = true with phase 0). A class is (device, row pitch a multiple of 16
 // bytes, round(log2 voxels), round(log2 row length)). Timing writes only the destination
 // copy, which the next sweep rewrites whole, and one change-flag slot.
 //

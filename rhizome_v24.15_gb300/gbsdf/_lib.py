@@ -43,7 +43,7 @@ class Stats(C.Structure):
                 ("brick_pairs", C.c_int64), ("csr_entries", C.c_int64), ("kernel_launches", C.c_int64),
                 ("proposed", C.c_int64), ("sweep_schedule", C.c_int64), ("winding_certified", C.c_int64),
                 ("winding_summed", C.c_int64), ("escalated", C.c_int64), ("band_err_fp64", C.c_double),
-                ("band_err_samples", C.c_int64), ("ms_sweeps", C.c_float), ("reserved", C.c_int32)]
+                ("band_err_samples", C.c_int64), ("ms_sweeps", C.c_float), ("sweep_schedule_first", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

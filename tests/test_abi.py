@@ -62,7 +62,7 @@ def test_struct_layouts():
 
     assert C.sizeof(_lib.Options) == 64
     # 2 int32 + 10 float + 6 int32 + 11 int64 + 6 int64, escalated, band_err_fp64 (double), band_err_samples,
-    # ms_sweeps (float) + reserved (int32)
+    # ms_sweeps (float) + sweep_schedule_first (int32)
     assert C.sizeof(_lib.Stats) == 8 + 40 + 24 + 88 + 64 + 8
 
 
