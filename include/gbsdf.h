@@ -121,7 +121,9 @@ typedef struct gbsdf_options {
                                updates in packed FP32 pairs (the reference's update at voxel
                                sizes 2^-20 to 2^20; otherwise 3 runs); a 0 digit (and
                                0 overall) = autotuned (the first build of a lattice class times
-                               the candidates). TMA needs rows of a multiple of 4 voxels. */
+                               the candidates for the rounds after the first; the first round
+                               takes 3 + 10 x 4). Every lattice can take the TMA schedules: the
+                               sweeps run in copies with rows padded to a multiple of 8 voxels. */
     int32_t host_output;    /* host outputs: 0 = a page-locked output is written by the sign-apply
                                kernel through its device mapping (no staging copy), others are
                                staged in device memory and copied; 1 = always stage and copy */
@@ -163,9 +165,9 @@ typedef struct gbsdf_stats {
     int64_t csr_entries;   /* entries of the reference's supercell CSR */
     int64_t kernel_launches; /* CUDA kernels this call launched */
     int64_t proposed;      /* learned mode: bricks the network proposed for the exact winding number */
-    int64_t sweep_schedule; /* schedules that ran: x schedule (1-4) + 10 x walk schedule
-                               (1 cp.async, 2 TMA pipeline, 3 TMA pipeline, 4 lines/thread,
-                               4 the same in packed pairs) */
+    int64_t sweep_schedule; /* schedules that ran in the rounds after the first: x schedule (1-5)
+                               + 10 x walk schedule (1-4), numbered as in
+                               gbsdf_options.sweep_schedule */
     int64_t winding_certified; /* exact winding decisions settled by the cluster bound */
     int64_t winding_summed;    /* ... and by the triangle-by-triangle sum */
     int64_t escalated;         /* learned mode: 1 when the stratified verify diverged and the signs
@@ -178,8 +180,9 @@ typedef struct gbsdf_stats {
                                   the first sweep's launch to the last's end, round bookkeeping
                                   included; without the padded copies, audit and clamp that
                                   ms_eikonal also holds) */
-    int32_t sweep_schedule_first; /* the schedules of the first round (x + 10 x walk), which the
-                                     autotuner picks apart from the later rounds' (sweep_schedule) */
+    int32_t sweep_schedule_first; /* the schedules of the first round (x + 10 x walk): the default
+                                     plan unless forced; the autotuner picks the later rounds'
+                                     (sweep_schedule) */
 } gbsdf_stats;
 
 /* Fill `opt` with defaults: reference mode, AUTO path, device 0, host triangles. */
